@@ -1,0 +1,179 @@
+// coherit_internal.cuh -- handle state, HBM layout and shared helpers.
+//
+// HBM layout of the resident genotypes (both copies hold every genotype):
+//   * SNP "slots": component g occupies slots [slot_start[g], slot_start[g] +
+//     m_g) followed by zero padding up to a multiple of 64; the total m_pad is
+//     a multiple of 128.  Padding slots have inv_sd = 0 and never contribute.
+//   * samples are padded with genotype code 0 up to n_pad (multiple of 128).
+//   * copy S ("sample rows", operand of Z S): 2 KB blocks (sample tile st of
+//     128 samples, panel p of 64 slots) at ((st * n_panels) + p) * 2048; row
+//     i%128 is 16 bytes holding the 64 slots of the panel.
+//   * copy T ("SNP rows", operand of Z^T V): 2 KB blocks (slot tile tt of 128
+//     slots, sample chunk q of 64 samples) at ((tt * n_chunks) + q) * 2048;
+//     row j%128 is 16 bytes holding the 64 samples of the chunk.
+//   * inside a 16-byte row, 32-bit word w holds elements 16w + 4s + b at bits
+//     8b + 2s (s, b in 0..3).  With this order, (word >> 2s) & 0x03030303
+//     yields four consecutive elements, one per byte, which the decoder turns
+//     into two BF16 pairs with one multiply and two byte permutes.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/coherit_gpu.h"
+
+namespace coherit {
+
+constexpr int kRowBytes = 16;
+constexpr int kBlockRows = 128;
+constexpr int kBlockBytes = kRowBytes * kBlockRows;  // 2048
+constexpr int kPanel = 64;                           // slots per panel / samples per chunk
+constexpr int kTile = 128;                           // rows per block
+
+// -------------------------------------------------------------- status
+void set_error(const char* fmt, ...);
+int cuda_status(cudaError_t e, const char* what);
+
+#define CO_CUDA(call)                                         \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) return ::coherit::cuda_status(_e, #call); \
+  } while (0)
+
+#define CO_CHECK(cond, code, ...)            \
+  do {                                       \
+    if (!(cond)) {                           \
+      ::coherit::set_error(__VA_ARGS__);     \
+      return (code);                         \
+    }                                        \
+  } while (0)
+
+// ------------------------------------------------- within-row element order
+__host__ __device__ __forceinline__ int row_word(int e) { return e >> 4; }
+__host__ __device__ __forceinline__ int row_shift(int e) {
+  const int r = e & 15;
+  return 8 * (r & 3) + 2 * (r >> 2);
+}
+
+// ------------------------------------------------ synthetic genotype hash
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// MAF threshold of SNP s on a 2^24 scale: U(0.05, 0.5).
+__host__ __device__ __forceinline__ uint32_t synth_maf_q24(uint64_t seed, int64_t s) {
+  const uint64_t h = splitmix64(seed * 0xD1B54A32D192ED03ull + static_cast<uint64_t>(s));
+  return 838861u + static_cast<uint32_t>((h >> 20) % 7549747ull);
+}
+
+// Genotype code of (sample i, SNP s): 0/1/2 allele count, 3 missing.
+__host__ __device__ __forceinline__ uint32_t synth_code(uint64_t seed, int64_t s, int64_t i,
+                                                        uint32_t maf_q24, uint32_t miss_q24) {
+  const uint64_t key = splitmix64(seed ^ (static_cast<uint64_t>(s) * 0x8CB92BA72F3D8DD7ull)) ^
+                       (static_cast<uint64_t>(i) * 0x9E3779B97F4A7C15ull);
+  const uint64_t h = splitmix64(key);
+  const uint32_t a1 = (static_cast<uint32_t>(h) & 0xFFFFFFu) < maf_q24;
+  const uint32_t a2 = (static_cast<uint32_t>(h >> 24) & 0xFFFFFFu) < maf_q24;
+  if (miss_q24 != 0u && static_cast<uint32_t>(h >> 48) * 256u < miss_q24) return 3u;
+  return a1 + a2;
+}
+
+// ------------------------------------------------------------- handle
+struct StatsSlot {
+  bool used = false;
+  float* mean = nullptr;        // m_pad, device
+  float* inv = nullptr;         // m_pad, device
+  uint8_t* row_mask = nullptr;  // n_pad bytes, device; nullptr = all samples
+  uint32_t* tmask = nullptr;    // n_chunks * 4 words: sample mask in row order (2 bits/sample)
+  int64_t n_sub = 0;
+  std::vector<double> comp_eff;
+  std::vector<double> comp_atom;
+  double eff_total = 0.0;
+  double atom_total = 0.0;
+};
+
+struct Workspace {
+  void* base = nullptr;
+  size_t bytes = 0;
+  int32_t k_max = 0;
+  int32_t nsplit = 0;
+};
+
+}  // namespace coherit
+
+struct coherit_geno {
+  int device = 0;
+  int64_t n = 0, n_pad = 0, m = 0, m_pad = 0;
+  int64_t n_panels = 0, n_chunks = 0, n_stiles = 0, n_ttiles = 0;
+  int32_t G = 1;
+  std::vector<int64_t> comp_m;           // G
+  std::vector<int64_t> comp_slot_start;  // G + 1 (slot offsets, multiples of 64)
+  std::vector<int64_t> comp_snp_start;   // G + 1 (cache SNP offsets)
+  int32_t* d_comp_of_slot = nullptr;     // m_pad
+  int64_t* d_comp_slot_start = nullptr;  // G + 1
+  int32_t* d_snp_of_slot = nullptr;      // m_pad (-1 = padding)
+  int64_t* d_slot_of_snp = nullptr;      // m
+  uint8_t* geno_s = nullptr;             // copy S
+  uint8_t* geno_t = nullptr;             // copy T
+  // missing-genotype lists (only when n_missing > 0)
+  int64_t n_missing = 0;
+  int64_t* d_csc_off = nullptr;  // m_pad + 1: samples with a missing genotype per slot
+  int32_t* d_csc_idx = nullptr;
+  int64_t* d_csr_off = nullptr;  // n_pad + 1: slots with a missing genotype per sample
+  int32_t* d_csr_idx = nullptr;
+  std::vector<coherit::StatsSlot> slots;
+  coherit::Workspace ws;
+  int* d_err = nullptr;
+  int sm_count = 0;
+  int64_t device_bytes = 0;
+};
+
+namespace coherit {
+
+// Launchers implemented in the .cu files.
+int build_layout_from_ref(coherit_geno* h, const uint8_t* d_packed, const int64_t* d_call_off,
+                          const int32_t* d_call_pw, const int32_t* d_snp_call,
+                          const int32_t* d_snp_col, cudaStream_t st);
+int build_layout_synthetic(coherit_geno* h, uint64_t seed, uint32_t miss_q24, cudaStream_t st);
+int build_copy_t(coherit_geno* h, cudaStream_t st);
+int build_missing_lists(coherit_geno* h, cudaStream_t st);
+int compute_slot_stats(coherit_geno* h, StatsSlot& s, const float* override_mean,
+                       const float* override_inv, float* mean_out, float* inv_out,
+                       int32_t* count_out, cudaStream_t st);
+int exact_diag_launch(coherit_geno* h, const StatsSlot& s, float* out, cudaStream_t st);
+
+// Operator launch description shared by the tensor-core and FP32 paths.
+struct OpDesc {
+  int mode = COHERIT_MODE_SUM;  // SUM / STACKED
+  bool xtv = false;             // output X^T V (m x k) instead of Z S
+  bool zxb = false;             // input is b (m x C): skip the first contraction
+  int precision = COHERIT_PREC_BF16X3;
+  int n_groups = 1;
+  std::vector<int32_t> col_start;  // n_groups + 1
+  std::vector<int32_t> slot_of_group;
+  std::vector<float> comp_scale;  // n_groups * G
+  std::vector<float> theta_e;     // n_groups (empty = none)
+  const float* snp_weight = nullptr;  // device, cache order
+  const float* V = nullptr;
+  int64_t ldv = 0;
+  int32_t k = 0;
+  float* out = nullptr;
+  int64_t ldo = 0;
+};
+
+int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st);
+int run_operator_fp32(coherit_geno* h, const OpDesc& d, cudaStream_t st);
+int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t nsplit);
+int ensure_ws_bytes(coherit_geno* h, size_t bytes);
+
+inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+inline int nsplit_of(int precision) {
+  return precision == COHERIT_PREC_BF16X3 ? 3 : precision == COHERIT_PREC_BF16X2 ? 2 : 1;
+}
+
+}  // namespace coherit

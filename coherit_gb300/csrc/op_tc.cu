@@ -1,0 +1,834 @@
+// op_tc.cu -- the genotype operator on sm_103a tensor cores.
+//
+// One application  out = sum_g s_g Z_g Z_g^T V  runs as two contractions over
+// the resident 2-bit genotypes (kv_impl.py:94-113 computes the same pair per
+// call block, with diff materialised in FP32):
+//
+//   K1 (slot tiles of 128 SNPs):  T = G0^T V            (K = samples)
+//       epilogue  S_j = w_j (T_j - mu_j 1^T V + mu_j sum_{i missing} V_i)
+//                 w_j = inv_sd_j^2 * s_g(j) [* snp weight]
+//                 S is split into BF16 terms in the B-tile layout of K2 and
+//                 r = sum_j mu_j S_j is accumulated in FP64.
+//   K2 (sample tiles of 128):     out = G0 S - 1 r^T (+ theta_e V)  (K = SNPs)
+//       then the sparse missing-genotype correction adds mu_j S_j back.
+//
+// G0 is the genotype matrix with missing codes read as 0; its entries
+// {0,1,2} are exact in BF16.  Mean imputation and centring are the FP32
+// rank-one terms above, so diff = G0 - mu (observed) / 0 (missing) exactly as
+// in kv_impl.py:69-91.  V and S are split into up to three BF16 terms
+// (hi + mid + lo) that all accumulate into one FP32 tensor-memory accumulator.
+//
+// Kernel anatomy (224 threads, 1 CTA of work per tile):
+//   warp 0  : bulk-copies 2 KB genotype blocks into a 16-deep shared ring
+//   warp 6  : bulk-copies B tiles (V or S split terms) into a shared ring
+//   warps 2-5: decode a genotype row (16 B = 64 codes) to 32 BF16 pairs and
+//             store them into a 4-deep tensor-memory A ring (tcgen05.st);
+//             afterwards they run the epilogue from the accumulator
+//   warp 1  : allocates tensor memory; lane 0 issues tcgen05.mma (A from
+//             tensor memory, B from shared memory) and commits to mbarriers.
+#include <cstdio>
+#include <algorithm>
+#include <cstring>
+
+#include "coherit_internal.cuh"
+#include "tc_ptx.cuh"
+
+namespace coherit {
+
+constexpr int kThreads = 224;
+constexpr int kWarpG = 0, kWarpMMA = 1, kWarpB = 6;
+constexpr int kRG = 16;      // genotype ring depth
+constexpr int kRA = 4;       // tensor-memory A ring depth (32 columns each)
+constexpr int kMaxRB = 16;   // B ring depth limit
+constexpr int kMaxGroups = 32;
+constexpr int kMaxScale = 256;
+constexpr int kBarrierBytes = 1024;
+
+struct EpiParams {
+  int n_groups, G, k, kp, nsplit, stacked, xtv, use_theta_e;
+  int64_t n, m_pad, ldv, ldo;
+  int32_t col_start[kMaxGroups + 1];
+  const float* gmean[kMaxGroups];
+  const float* ginv[kMaxGroups];
+  const uint8_t* gmask[kMaxGroups];
+  float cscale[kMaxScale];
+  float theta_e[kMaxGroups];
+  const int32_t* comp_of_slot;
+  const int32_t* snp_of_slot;
+  const float* snpw;   // cache order or nullptr
+  const float* cs;     // kp column sums of V
+  const float* vmiss;  // m_pad x kp or nullptr
+  __nv_bfloat16* sbuf; // K1 output: S split tiles
+  float* sf32;         // m_pad x kp or nullptr
+  double* rbuf;        // (stacked ? G : 1) x kp
+  float* xout;         // X^T V output (m x ldo) when xtv
+  const float* V;      // K2: residual term
+  float* out;          // K2 output
+};
+
+struct TcParams {
+  const uint8_t* geno;
+  int64_t n_chunks;    // K1: sample chunks per slot tile
+  int64_t n_panels;    // K2: panels per sample tile
+  const int64_t* comp_slot_start;  // device, G + 1
+  const uint8_t* bsrc;
+  int64_t b_chunk_bytes;
+  int RB;
+  uint32_t bslot_bytes;
+  uint32_t tmem_cols;
+  uint32_t acc_cols;
+  int* err;
+  EpiParams e;
+};
+
+__device__ __forceinline__ int group_of(const EpiParams& e, int c) {
+  int r = 0;
+  while (r + 1 < e.n_groups && c >= e.col_start[r + 1]) ++r;
+  return r;
+}
+
+// 16 bytes = 64 genotype codes of one row -> 32 words of BF16 pairs in K
+// order (word t = elements 2t, 2t+1; code 3 -> 0).
+__device__ __forceinline__ void decode_row(const uint4 raw, uint32_t (&a)[32]) {
+  const uint32_t L = 0x00008000u;  // low bytes of bf16(0), bf16(1), bf16(2), bf16(0)
+  const uint32_t H = 0x00403F00u;  // high bytes
+  const uint32_t ws[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+  for (int w = 0; w < 4; ++w) {
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const uint32_t t = (ws[w] >> (2 * s)) & 0x03030303u;
+      const uint32_t sel = t * 17u + 0x40404040u;
+      a[8 * w + 2 * s] = __byte_perm(L, H, sel);
+      a[8 * w + 2 * s + 1] = __byte_perm(L, H, sel >> 16);
+    }
+  }
+}
+
+__device__ __forceinline__ void split3(float v, __nv_bfloat16& hi, __nv_bfloat16& mid,
+                                       __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(v);
+  const float r1 = v - __bfloat162float(hi);
+  mid = __float2bfloat16_rn(r1);
+  const float r2 = r1 - __bfloat162float(mid);
+  lo = __float2bfloat16_rn(r2);
+}
+
+// Offset (elements) of (column c, K index kk) inside one split term of a B
+// tile: K-major canonical layout, core matrices of 8 columns x 8 K values.
+__host__ __device__ __forceinline__ int64_t btile_off(int c, int kk) {
+  return ((c >> 3) * 8 + (kk >> 3)) * 64 + (c & 7) * 8 + (kk & 7);
+}
+
+template <bool IS_K1>
+__global__ void __launch_bounds__(kThreads, 1) k_tc_op(const __grid_constant__ TcParams p) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint64_t* fullG = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* emptyG = fullG + kRG;
+  uint64_t* fullB = emptyG + kRG;
+  uint64_t* emptyB = fullB + kMaxRB;
+  uint64_t* decoded = emptyB + kMaxRB;
+  uint64_t* emptyA = decoded + kRA;
+  uint64_t* done = emptyA + kRA;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  uint8_t* gring = smem + kBarrierBytes;
+  uint8_t* bring = gring + kRG * kBlockBytes;
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const EpiParams& e = p.e;
+
+  const int64_t tile = blockIdx.x;
+  const int comp = blockIdx.y;
+  int64_t nch;
+  const uint8_t* gbase;
+  const uint8_t* bbase;
+  if (IS_K1) {
+    nch = p.n_chunks;
+    gbase = p.geno + tile * p.n_chunks * kBlockBytes;
+    bbase = p.bsrc;
+  } else {
+    int64_t p0 = 0, p1 = p.n_panels;
+    if (e.stacked) {
+      p0 = p.comp_slot_start[comp] / kPanel;
+      p1 = p.comp_slot_start[comp + 1] / kPanel;
+    }
+    nch = p1 - p0;
+    gbase = p.geno + (tile * p.n_panels + p0) * kBlockBytes;
+    bbase = p.bsrc + p0 * p.b_chunk_bytes;
+  }
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kRG; ++i) {
+      ptx::mbar_init(&fullG[i], 1);
+      ptx::mbar_init(&emptyG[i], 128);
+    }
+    for (int i = 0; i < kMaxRB; ++i) {
+      ptx::mbar_init(&fullB[i], 1);
+      ptx::mbar_init(&emptyB[i], 1);
+    }
+    for (int i = 0; i < kRA; ++i) {
+      ptx::mbar_init(&decoded[i], 128);
+      ptx::mbar_init(&emptyA[i], 1);
+    }
+    ptx::mbar_init(done, 1);
+    *abort_flag = 0;
+    ptx::fence_barrier_init();
+  }
+  if (warp == kWarpMMA) ptx::tmem_alloc(tmem_slot, p.tmem_cols);
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == kWarpG) {
+    // ---------------------------------------------- genotype block producer
+    if (lane == 0) {
+      int64_t issued = 0;
+      for (int64_t c = 0; c < nch; ++c) {
+        const int s = static_cast<int>(c % kRG);
+        const uint32_t u = static_cast<uint32_t>(c / kRG);
+        if (u > 0 && !ptx::mbar_wait(&emptyG[s], (u - 1) & 1, p.err, 11, abort_flag)) break;
+        ptx::mbar_arrive_expect_tx(&fullG[s], kBlockBytes);
+        ptx::bulk_g2s(gring + s * kBlockBytes, gbase + c * kBlockBytes, kBlockBytes, &fullG[s]);
+        issued = c + 1;
+      }
+      if (*abort_flag) {
+        // Let copies still in flight land before the CTA exits.
+        for (int64_t c = (issued > kRG ? issued - kRG : 0); c < issued; ++c) {
+          const int s = static_cast<int>(c % kRG);
+          volatile int no_abort = 0;
+          ptx::mbar_wait(&fullG[s], static_cast<uint32_t>(c / kRG) & 1, p.err, 18, &no_abort);
+        }
+      }
+    }
+  } else if (warp == kWarpB) {
+    // ---------------------------------------------------- B tile producer
+    if (lane == 0) {
+      int64_t issued = 0;
+      for (int64_t c = 0; c < nch; ++c) {
+        const int s = static_cast<int>(c % p.RB);
+        const uint32_t u = static_cast<uint32_t>(c / p.RB);
+        if (u > 0 && !ptx::mbar_wait(&emptyB[s], (u - 1) & 1, p.err, 12, abort_flag)) break;
+        ptx::mbar_arrive_expect_tx(&fullB[s], p.bslot_bytes);
+        ptx::bulk_g2s(bring + static_cast<size_t>(s) * p.bslot_bytes, bbase + c * p.b_chunk_bytes,
+                      p.bslot_bytes, &fullB[s]);
+        issued = c + 1;
+      }
+      if (*abort_flag) {
+        for (int64_t c = (issued > p.RB ? issued - p.RB : 0); c < issued; ++c) {
+          const int s = static_cast<int>(c % p.RB);
+          volatile int no_abort = 0;
+          ptx::mbar_wait(&fullB[s], static_cast<uint32_t>(c / p.RB) & 1, p.err, 19, &no_abort);
+        }
+      }
+    }
+  } else if (warp == kWarpMMA) {
+    // ------------------------------------------------------------ MMA issue
+    if (lane == 0) {
+      const uint32_t idesc = ptx::idesc_bf16_f32(128, e.kp);
+      const uint32_t bring_addr = ptx::smem_addr(bring);
+      int64_t c = 0;
+      for (; c < nch; ++c) {
+        const int as = static_cast<int>(c % kRA);
+        const int bs = static_cast<int>(c % p.RB);
+        if (!ptx::mbar_wait(&decoded[as], static_cast<uint32_t>(c / kRA) & 1, p.err, 13,
+                            abort_flag))
+          break;
+        if (!ptx::mbar_wait(&fullB[bs], static_cast<uint32_t>(c / p.RB) & 1, p.err, 14,
+                            abort_flag))
+          break;
+        ptx::tc_fence_after();
+        const uint32_t bslot = bring_addr + static_cast<uint32_t>(bs) * p.bslot_bytes;
+        const uint32_t a_col = tmem + p.acc_cols + static_cast<uint32_t>(as) * 32u;
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+          for (int t = 0; t < e.nsplit; ++t) {
+            const uint64_t bd = ptx::smem_desc(
+                bslot + static_cast<uint32_t>(t * e.kp * 128 + ks * 256), 128u, 1024u);
+            ptx::mma_ts(tmem, a_col + static_cast<uint32_t>(ks * 8), bd, idesc,
+                        (c | ks | t) != 0 ? 1u : 0u);
+          }
+        }
+        ptx::mma_commit(&emptyA[as]);
+        ptx::mma_commit(&emptyB[bs]);
+      }
+      if (nch == 0) {
+        ptx::mbar_arrive(done);
+      } else {
+        ptx::mma_commit(done);
+      }
+      if (*abort_flag) {
+        // Tensor memory is released below: let issued MMAs finish first.
+        volatile int no_abort = 0;
+        ptx::mbar_wait(done, 0, p.err, 20, &no_abort);
+      }
+    }
+  } else {
+    // --------------------------------------------- decoders, then epilogue
+    const int quarter = warp & 3;
+    const int row = quarter * 32 + lane;
+    const uint32_t lane_base = static_cast<uint32_t>(quarter * 32) << 16;
+    bool ok = true;
+    for (int64_t c = 0; c < nch; ++c) {
+      const int gs = static_cast<int>(c % kRG);
+      bool w_ok = ptx::mbar_wait(&fullG[gs], static_cast<uint32_t>(c / kRG) & 1, p.err, 15,
+                                 abort_flag);
+      if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
+      const uint4 raw = *reinterpret_cast<const uint4*>(gring + gs * kBlockBytes + row * kRowBytes);
+      ptx::mbar_arrive(&emptyG[gs]);
+      uint32_t a[32];
+      decode_row(raw, a);
+      const int as = static_cast<int>(c % kRA);
+      if (c >= kRA) {
+        w_ok = ptx::mbar_wait(&emptyA[as], static_cast<uint32_t>(c / kRA - 1) & 1, p.err, 16,
+                              abort_flag);
+        if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
+      }
+      ptx::tc_fence_after();
+      ptx::tmem_st32(tmem + lane_base + p.acc_cols + static_cast<uint32_t>(as) * 32u, a);
+      ptx::tmem_wait_st();
+      ptx::tc_fence_before();
+      ptx::mbar_arrive(&decoded[as]);
+    }
+    if (ok) {
+      const bool w_ok = ptx::mbar_wait(done, 0, p.err, 17, abort_flag);
+      ok = __all_sync(0xffffffffu, w_ok);
+    }
+    if (ok) {
+      ptx::tc_fence_after();
+      const int64_t rowid = tile * kTile + row;
+      if (IS_K1) {
+        // ------------------------------------------------ K1 epilogue
+        const int64_t j = rowid;  // slot
+        const int g = e.comp_of_slot[j];
+        const int gi = e.stacked ? g : 0;
+        const int32_t snp = e.snp_of_slot[j];
+        float wsnp = 1.f;
+        if (e.snpw != nullptr) wsnp = snp >= 0 ? e.snpw[snp] : 0.f;
+        const int64_t pnl = j / kPanel;
+        const int kk = static_cast<int>(j % kPanel);
+        const int g0 = __shfl_sync(0xffffffffu, gi, 0);
+        const bool uniform = __all_sync(0xffffffffu, gi == g0);
+        for (int c0 = 0; c0 < e.kp; c0 += 16) {
+          uint32_t r[16];
+          if (nch > 0) {
+            ptx::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(c0), r);
+            ptx::tmem_wait_ld();
+          } else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) r[i] = 0u;
+          }
+#pragma unroll 1
+          for (int i = 0; i < 16; ++i) {
+            const int c = c0 + i;
+            float sval = 0.f, mu = 0.f;
+            if (c < e.k) {
+              const int grp = group_of(e, c);
+              mu = e.gmean[grp][j];
+              const float iv = e.ginv[grp][j];
+              const float w = (e.xtv ? iv : iv * iv) * e.cscale[grp * e.G + g] * wsnp;
+              float corr = mu * e.cs[c];
+              if (e.vmiss != nullptr) corr -= mu * e.vmiss[j * e.kp + c];
+              sval = w * (__uint_as_float(r[i]) - corr);
+            }
+            if (e.xtv) {
+              if (snp >= 0 && c < e.k) e.xout[static_cast<int64_t>(snp) * e.ldo + c] = sval;
+              continue;
+            }
+            const int64_t base = pnl * (static_cast<int64_t>(e.nsplit) * e.kp * kPanel) +
+                                 btile_off(c, kk);
+            __nv_bfloat16 hi, mid, lo;
+            split3(sval, hi, mid, lo);
+            e.sbuf[base] = hi;
+            if (e.nsplit > 1) e.sbuf[base + static_cast<int64_t>(e.kp) * kPanel] = mid;
+            if (e.nsplit > 2) e.sbuf[base + 2 * static_cast<int64_t>(e.kp) * kPanel] = lo;
+            if (c >= e.k) continue;
+            if (e.sf32 != nullptr) e.sf32[j * e.kp + c] = sval;
+            double v = static_cast<double>(mu) * static_cast<double>(sval);
+            if (uniform) {
+#pragma unroll
+              for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+              if (lane == 0) atomicAdd(&e.rbuf[gi * e.kp + c], v);
+            } else {
+              atomicAdd(&e.rbuf[gi * e.kp + c], v);
+            }
+          }
+        }
+      } else {
+        // ------------------------------------------------ K2 epilogue
+        const int64_t i = rowid;  // sample
+        const int gi = e.stacked ? comp : 0;
+        float* outb = e.out + static_cast<int64_t>(gi) * e.n * e.ldo;
+        for (int c0 = 0; c0 < e.kp; c0 += 16) {
+          uint32_t r[16];
+          if (nch > 0) {
+            ptx::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(c0), r);
+            ptx::tmem_wait_ld();
+          } else {
+#pragma unroll
+            for (int t = 0; t < 16; ++t) r[t] = 0u;
+          }
+          if (i >= e.n) continue;
+#pragma unroll 1
+          for (int t = 0; t < 16; ++t) {
+            const int c = c0 + t;
+            if (c >= e.k) break;
+            const int grp = group_of(e, c);
+            float v = __uint_as_float(r[t]) - static_cast<float>(e.rbuf[gi * e.kp + c]);
+            if (e.use_theta_e) v += e.theta_e[grp] * e.V[i * e.ldv + c];
+            if (e.gmask[grp] != nullptr && e.gmask[grp][i] == 0) v = 0.f;
+            outb[i * e.ldo + c] = v;
+          }
+        }
+      }
+    }
+  }
+
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == kWarpMMA) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, p.tmem_cols);
+  }
+}
+
+// ------------------------------------------------------------ helper kernels
+
+// V (n x k, fp32) -> split BF16 B tiles for K1 + per-chunk FP64 column sums.
+// Rows outside a request's sample subset are read as zero.
+__global__ void k_prep_v(const float* __restrict__ V, int64_t ldv, int64_t n, int k, int kp,
+                         int nsplit, __nv_bfloat16* __restrict__ vt, double* __restrict__ cs_part,
+                         const __grid_constant__ EpiParams e) {
+  extern __shared__ float tile[];  // [64][kp + 1]
+  const int64_t q = blockIdx.x;
+  const int ld = kp + 1;
+  for (int idx = threadIdx.x; idx < kPanel * kp; idx += blockDim.x) {
+    const int r = idx / kp, c = idx % kp;
+    const int64_t i = q * kPanel + r;
+    float v = 0.f;
+    if (i < n && c < k) {
+      const uint8_t* mk = e.gmask[group_of(e, c)];
+      if (mk == nullptr || mk[i] != 0) v = V[i * ldv + c];
+    }
+    tile[r * ld + c] = v;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < kp; c += blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < kPanel; ++r) s += static_cast<double>(tile[r * ld + c]);
+    cs_part[q * kp + c] = s;
+  }
+  const int cg_n = kp / 8;
+  const int64_t chunk_elems = static_cast<int64_t>(nsplit) * kp * kPanel;
+  for (int idx = threadIdx.x; idx < chunk_elems; idx += blockDim.x) {
+    const int kr = idx & 7, cr = (idx >> 3) & 7, kg = (idx >> 6) & 7;
+    const int rest = idx >> 9;
+    const int cg = rest % cg_n, t = rest / cg_n;
+    const int c = cg * 8 + cr, kk = kg * 8 + kr;
+    __nv_bfloat16 hi, mid, lo;
+    split3(tile[kk * ld + c], hi, mid, lo);
+    vt[q * chunk_elems + idx] = t == 0 ? hi : (t == 1 ? mid : lo);
+  }
+}
+
+__global__ void k_colsum_finish(const double* __restrict__ cs_part, int64_t n_parts, int kp,
+                                float* __restrict__ cs) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= kp) return;
+  double s = 0.0;
+  for (int64_t q = 0; q < n_parts; ++q) s += cs_part[q * kp + c];
+  cs[c] = static_cast<float>(s);
+}
+
+// vmiss[j, c] = sum over samples i with a missing genotype at slot j of V[i, c].
+__global__ void k_vmiss(const int64_t* __restrict__ off, const int32_t* __restrict__ idx,
+                        int64_t m_pad, const float* __restrict__ V, int64_t ldv, int64_t n, int k,
+                        int kp, float* __restrict__ vmiss, const __grid_constant__ EpiParams e) {
+  const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (j >= m_pad) return;
+  for (int c = lane; c < kp; c += 32) {
+    double s = 0.0;
+    if (c < k) {
+      const uint8_t* mk = e.gmask[group_of(e, c)];
+      for (int64_t t = off[j]; t < off[j + 1]; ++t) {
+        const int64_t i = idx[t];
+        if (i < n && (mk == nullptr || mk[i] != 0)) s += static_cast<double>(V[i * ldv + c]);
+      }
+    }
+    vmiss[j * kp + c] = static_cast<float>(s);
+  }
+}
+
+// out[i, c] += mu_j S_j[c] over slots j where sample i's genotype is missing.
+__global__ void k_rowcorr(const int64_t* __restrict__ off, const int32_t* __restrict__ idx,
+                          int64_t n, const __grid_constant__ EpiParams e) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  for (int c = lane; c < e.k; c += 32) {
+    const int grp = group_of(e, c);
+    if (e.gmask[grp] != nullptr && e.gmask[grp][i] == 0) continue;
+    const float* mean = e.gmean[grp];
+    for (int64_t t = off[i]; t < off[i + 1]; ++t) {
+      const int64_t j = idx[t];
+      const int g = e.stacked ? e.comp_of_slot[j] : 0;
+      e.out[(static_cast<int64_t>(g) * e.n + i) * e.ldo + c] += mean[j] * e.sf32[j * e.kp + c];
+    }
+  }
+}
+
+// b (m x C, cache order) -> S = inv_sd * b split into K2 B tiles, r = sum mu S.
+__global__ void k_prep_s_from_b(const float* __restrict__ b, int64_t ldb,
+                                const __grid_constant__ EpiParams e) {
+  const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (j >= e.m_pad) return;
+  const int32_t snp = e.snp_of_slot[j];
+  const float mu = e.gmean[0][j];
+  const float iv = e.ginv[0][j];
+  const int64_t pnl = j / kPanel;
+  const int kk = static_cast<int>(j % kPanel);
+  for (int c = 0; c < e.kp; ++c) {
+    float sval = 0.f;
+    if (c < e.k && snp >= 0) sval = iv * b[static_cast<int64_t>(snp) * ldb + c];
+    const int64_t base =
+        pnl * (static_cast<int64_t>(e.nsplit) * e.kp * kPanel) + btile_off(c, kk);
+    __nv_bfloat16 hi, mid, lo;
+    split3(sval, hi, mid, lo);
+    e.sbuf[base] = hi;
+    if (e.nsplit > 1) e.sbuf[base + static_cast<int64_t>(e.kp) * kPanel] = mid;
+    if (e.nsplit > 2) e.sbuf[base + 2 * static_cast<int64_t>(e.kp) * kPanel] = lo;
+    if (c < e.k) {
+      if (e.sf32 != nullptr) e.sf32[j * e.kp + c] = sval;
+      if (sval != 0.f) atomicAdd(&e.rbuf[c], static_cast<double>(mu) * static_cast<double>(sval));
+    }
+  }
+}
+
+// ------------------------------------------------------------------ launcher
+
+static inline int max_kp_for(int nsplit) { return nsplit >= 3 ? 224 : 256; }
+
+struct WsLayout {
+  size_t vt, sbuf, cs_part, cs, rbuf, vmiss, sf32, total;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+static WsLayout ws_layout(const coherit_geno* h, int kp, int nsplit) {
+  WsLayout L;
+  size_t off = 0;
+  L.vt = off;
+  off = align256(off + static_cast<size_t>(h->n_chunks) * nsplit * kp * kPanel * 2);
+  L.sbuf = off;
+  off = align256(off + static_cast<size_t>(h->n_panels) * nsplit * kp * kPanel * 2);
+  L.cs_part = off;
+  off = align256(off + static_cast<size_t>(h->n_chunks) * kp * 8);
+  L.cs = off;
+  off = align256(off + static_cast<size_t>(kp) * 4);
+  L.rbuf = off;
+  off = align256(off + static_cast<size_t>(h->G) * kp * 8);
+  L.vmiss = off;
+  L.sf32 = off;
+  if (h->n_missing > 0) {
+    off = align256(off + static_cast<size_t>(h->m_pad) * kp * 4);
+    L.sf32 = off;
+    off = align256(off + static_cast<size_t>(h->m_pad) * kp * 4);
+  }
+  L.total = off;
+  return L;
+}
+
+int ensure_ws_bytes(coherit_geno* h, size_t bytes) {
+  if (h->ws.base != nullptr && h->ws.bytes >= bytes) return COHERIT_OK;
+  if (h->ws.base != nullptr) {
+    // The old buffer may still be read by queued work.
+    CO_CUDA(cudaDeviceSynchronize());
+    cudaFree(h->ws.base);
+    h->ws = Workspace();
+  }
+  CO_CUDA(cudaMalloc(&h->ws.base, bytes));
+  h->ws.bytes = bytes;
+  return COHERIT_OK;
+}
+
+int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t nsplit) {
+  const int kp = static_cast<int>(round_up(std::max(k_max, 1), 16));
+  const WsLayout L = ws_layout(h, kp, nsplit);
+  return ensure_ws_bytes(h, L.total);
+}
+
+static int fill_epi(coherit_geno* h, const OpDesc& d, int kp, int nsplit, EpiParams& e) {
+  memset(&e, 0, sizeof(e));
+  CO_CHECK(d.n_groups >= 1 && d.n_groups <= kMaxGroups, COHERIT_E_SHAPE,
+           "number of requests per launch must be in [1, %d]", kMaxGroups);
+  CO_CHECK(d.n_groups * h->G <= kMaxScale, COHERIT_E_SHAPE,
+           "requests x components must not exceed %d", kMaxScale);
+  e.n_groups = d.n_groups;
+  e.G = h->G;
+  e.k = d.k;
+  e.kp = kp;
+  e.nsplit = nsplit;
+  e.stacked = d.mode == COHERIT_MODE_STACKED ? 1 : 0;
+  e.xtv = d.xtv ? 1 : 0;
+  e.n = h->n;
+  e.m_pad = h->m_pad;
+  e.ldv = d.ldv;
+  e.ldo = d.ldo;
+  for (int r = 0; r <= d.n_groups; ++r) e.col_start[r] = d.col_start[r];
+  for (int r = 0; r < d.n_groups; ++r) {
+    const int s = d.slot_of_group[r];
+    CO_CHECK(s >= 0 && s < static_cast<int>(h->slots.size()) && h->slots[s].used,
+             COHERIT_E_INDEX, "stats slot %d is not initialised", s);
+    e.gmean[r] = h->slots[s].mean;
+    e.ginv[r] = h->slots[s].inv;
+    e.gmask[r] = h->slots[s].row_mask;
+    for (int g = 0; g < h->G; ++g) e.cscale[r * h->G + g] = d.comp_scale[r * h->G + g];
+    e.theta_e[r] = d.theta_e.empty() ? 0.f : d.theta_e[r];
+  }
+  e.use_theta_e = d.theta_e.empty() ? 0 : 1;
+  e.comp_of_slot = h->d_comp_of_slot;
+  e.snp_of_slot = h->d_snp_of_slot;
+  e.snpw = d.snp_weight;
+  e.V = d.V;
+  e.out = d.out;
+  e.xout = d.out;
+  return COHERIT_OK;
+}
+
+struct TcLaunchCfg {
+  int RB;
+  uint32_t bslot;
+  uint32_t tmem_cols, acc_cols;
+  size_t smem;
+};
+
+static TcLaunchCfg tc_config(int kp, int nsplit) {
+  TcLaunchCfg c;
+  c.acc_cols = static_cast<uint32_t>(round_up(kp, 32));
+  uint32_t need = c.acc_cols + kRA * 32;
+  uint32_t cols = 32;
+  while (cols < need) cols <<= 1;
+  c.tmem_cols = cols;
+  c.bslot = static_cast<uint32_t>(nsplit) * kp * kPanel * 2;
+  const size_t fixed = kBarrierBytes + kRG * kBlockBytes;
+  const int ctas_tmem = 512 / static_cast<int>(cols);
+  const size_t target = ctas_tmem >= 2 ? 100 * 1024 : 200 * 1024;
+  int rb = static_cast<int>((target - fixed) / c.bslot);
+  rb = std::max(2, std::min(kMaxRB, rb));
+  c.RB = rb;
+  c.smem = fixed + static_cast<size_t>(rb) * c.bslot;
+  // Never let more CTAs share an SM than its tensor memory can hold: a
+  // further CTA would block in tcgen05.alloc.
+  const size_t sm_bytes = 228 * 1024;
+  while (static_cast<int>(sm_bytes / (c.smem + 1024)) > ctas_tmem) c.smem += 4096;
+  return c;
+}
+
+int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
+  if (d.precision == COHERIT_PREC_FP32) return run_operator_fp32(h, d, st);
+  const int nsplit = nsplit_of(d.precision);
+  const int kmax = max_kp_for(nsplit);
+  if (d.k > kmax) {
+    // Column blocks: each re-reads the genotypes.
+    CO_CHECK(d.n_groups == 1, COHERIT_E_SHAPE,
+             "batched requests wider than %d columns in one launch are not supported", kmax);
+    const int nblk = (d.k + kmax - 1) / kmax;
+    const int step = static_cast<int>(round_up((d.k + nblk - 1) / nblk, 16));
+    for (int c0 = 0; c0 < d.k; c0 += step) {
+      OpDesc s = d;
+      s.k = std::min(step, d.k - c0);
+      s.V = d.V + c0;
+      s.out = d.out + c0;
+      s.col_start = {0, s.k};
+      int rc = run_operator(h, s, st);
+      if (rc != COHERIT_OK) return rc;
+    }
+    return COHERIT_OK;
+  }
+  const int kp = static_cast<int>(round_up(std::max(d.k, 1), 16));
+  int rc = ensure_workspace(h, kp, nsplit);
+  if (rc != COHERIT_OK) return rc;
+  const WsLayout L = ws_layout(h, kp, nsplit);
+  uint8_t* ws = static_cast<uint8_t*>(h->ws.base);
+  EpiParams e;
+  rc = fill_epi(h, d, kp, nsplit, e);
+  if (rc != COHERIT_OK) return rc;
+  auto* vt = reinterpret_cast<__nv_bfloat16*>(ws + L.vt);
+  auto* sbuf = reinterpret_cast<__nv_bfloat16*>(ws + L.sbuf);
+  auto* cs_part = reinterpret_cast<double*>(ws + L.cs_part);
+  auto* cs = reinterpret_cast<float*>(ws + L.cs);
+  auto* rbuf = reinterpret_cast<double*>(ws + L.rbuf);
+  float* vmiss = h->n_missing > 0 ? reinterpret_cast<float*>(ws + L.vmiss) : nullptr;
+  float* sf32 = h->n_missing > 0 ? reinterpret_cast<float*>(ws + L.sf32) : nullptr;
+  e.cs = cs;
+  e.vmiss = vmiss;
+  e.sbuf = sbuf;
+  e.sf32 = sf32;
+  e.rbuf = rbuf;
+  const int nr = e.stacked ? h->G : 1;
+  CO_CUDA(cudaMemsetAsync(rbuf, 0, sizeof(double) * nr * kp, st));
+
+  const TcLaunchCfg cfg = tc_config(kp, nsplit);
+  TcParams p;
+  memset(&p, 0, sizeof(p));
+  p.RB = cfg.RB;
+  p.bslot_bytes = cfg.bslot;
+  p.tmem_cols = cfg.tmem_cols;
+  p.acc_cols = cfg.acc_cols;
+  p.err = h->d_err;
+  p.n_chunks = h->n_chunks;
+  p.n_panels = h->n_panels;
+  p.b_chunk_bytes = static_cast<int64_t>(nsplit) * kp * kPanel * 2;
+
+  if (!d.zxb) {
+    const int prep_smem = kPanel * (kp + 1) * static_cast<int>(sizeof(float));
+    CO_CUDA(cudaFuncSetAttribute(k_prep_v, cudaFuncAttributeMaxDynamicSharedMemorySize, prep_smem));
+    k_prep_v<<<static_cast<unsigned>(h->n_chunks), 256, prep_smem, st>>>(
+        d.V, d.ldv, h->n, d.k, kp, nsplit, vt, cs_part, e);
+    k_colsum_finish<<<(kp + 127) / 128, 128, 0, st>>>(cs_part, h->n_chunks, kp, cs);
+    if (vmiss != nullptr)
+      k_vmiss<<<static_cast<unsigned>((h->m_pad + 7) / 8), 256, 0, st>>>(
+          h->d_csc_off, h->d_csc_idx, h->m_pad, d.V, d.ldv, h->n, d.k, kp, vmiss, e);
+    CO_CUDA(cudaGetLastError());
+    p.geno = h->geno_t;
+    p.bsrc = reinterpret_cast<const uint8_t*>(vt);
+    p.e = e;
+    CO_CUDA(cudaFuncSetAttribute(k_tc_op<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(cfg.smem)));
+    k_tc_op<true><<<dim3(static_cast<unsigned>(h->n_ttiles), 1), kThreads, cfg.smem, st>>>(p);
+    CO_CUDA(cudaGetLastError());
+    if (d.xtv) return COHERIT_OK;
+  } else {
+    // Z b: S = inv_sd * b computed directly.
+    CO_CHECK(h->n_missing == 0 || sf32 != nullptr, COHERIT_E_SHAPE, "workspace missing");
+    k_prep_s_from_b<<<static_cast<unsigned>((h->m_pad + 127) / 128), 128, 0, st>>>(d.V, d.ldv, e);
+    CO_CUDA(cudaGetLastError());
+  }
+  p.geno = h->geno_s;
+  p.bsrc = reinterpret_cast<const uint8_t*>(sbuf);
+  p.comp_slot_start = h->d_comp_slot_start;
+  p.e = e;
+  CO_CUDA(cudaFuncSetAttribute(k_tc_op<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(cfg.smem)));
+  k_tc_op<false><<<dim3(static_cast<unsigned>(h->n_stiles), static_cast<unsigned>(nr)), kThreads,
+                   cfg.smem, st>>>(p);
+  CO_CUDA(cudaGetLastError());
+  if (sf32 != nullptr) {
+    k_rowcorr<<<static_cast<unsigned>((h->n + 7) / 8), 256, 0, st>>>(h->d_csr_off, h->d_csr_idx,
+                                                                      h->n, e);
+    CO_CUDA(cudaGetLastError());
+  }
+  return COHERIT_OK;
+}
+
+}  // namespace coherit
+
+using namespace coherit;
+
+static int make_single(coherit_geno_t* h, int32_t slot, int32_t k, const float* comp_scale,
+                       OpDesc& d) {
+  CO_CHECK(h != nullptr, COHERIT_E_CLOSED, "genotype handle is closed");
+  CO_CHECK(k >= 1, COHERIT_E_SHAPE, "right-hand side must have at least one column");
+  CO_CHECK(slot >= 0 && slot < static_cast<int32_t>(h->slots.size()) && h->slots[slot].used,
+           COHERIT_E_INDEX, "stats slot %d is not initialised", slot);
+  d.n_groups = 1;
+  d.col_start = {0, k};
+  d.slot_of_group = {slot};
+  d.comp_scale.assign(h->G, 1.f);
+  if (comp_scale != nullptr)
+    for (int g = 0; g < h->G; ++g) d.comp_scale[g] = comp_scale[g];
+  d.k = k;
+  return COHERIT_OK;
+}
+
+extern "C" {
+
+int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision) {
+  CO_CHECK(h != nullptr, COHERIT_E_CLOSED, "genotype handle is closed");
+  const int kp = static_cast<int>(round_up(std::max(k_max, 1), 16));
+  if (precision == COHERIT_PREC_FP32)
+    return ensure_ws_bytes(h, static_cast<size_t>(h->m_pad) * kp * sizeof(float));
+  const int ns = nsplit_of(precision);
+  return ensure_workspace(h, std::min(kp, max_kp_for(ns)), ns);
+}
+
+int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t precision,
+                    const float* V, int64_t ldv, int32_t k, const float* comp_scale,
+                    int32_t use_theta_e, float theta_e, const float* snp_weight, float* out,
+                    int64_t ldo, void* stream) {
+  OpDesc d;
+  int rc = make_single(h, slot, k, comp_scale, d);
+  if (rc != COHERIT_OK) return rc;
+  CO_CHECK(mode == COHERIT_MODE_SUM || mode == COHERIT_MODE_STACKED, COHERIT_E_SHAPE,
+           "unknown operator mode %d", mode);
+  CO_CHECK(ldv >= k && ldo >= k, COHERIT_E_SHAPE, "row strides must be >= k");
+  CO_CHECK(V != nullptr && out != nullptr, COHERIT_E_SHAPE, "V and out are required");
+  d.mode = mode;
+  d.precision = precision;
+  if (use_theta_e && mode == COHERIT_MODE_SUM) d.theta_e = {theta_e};
+  d.snp_weight = snp_weight;
+  d.V = V;
+  d.ldv = ldv;
+  d.out = out;
+  d.ldo = ldo;
+  return run_operator(h, d, static_cast<cudaStream_t>(stream));
+}
+
+int coherit_geno_kv_batched(coherit_geno_t* h, int32_t n_requests, const int32_t* col_start,
+                            const int32_t* slots, int32_t precision, const float* V, int64_t ldv,
+                            int32_t k, const float* comp_scale, const float* theta_e, float* out,
+                            int64_t ldo, void* stream) {
+  CO_CHECK(h != nullptr, COHERIT_E_CLOSED, "genotype handle is closed");
+  CO_CHECK(n_requests >= 1, COHERIT_E_SHAPE, "need at least one request");
+  CO_CHECK(col_start[0] == 0 && col_start[n_requests] == k, COHERIT_E_SHAPE,
+           "column groups must cover [0, k)");
+  OpDesc d;
+  d.n_groups = n_requests;
+  d.col_start.assign(col_start, col_start + n_requests + 1);
+  for (int r = 0; r < n_requests; ++r)
+    CO_CHECK(col_start[r + 1] > col_start[r], COHERIT_E_SHAPE, "request %d has no columns", r);
+  d.slot_of_group.assign(slots, slots + n_requests);
+  d.comp_scale.assign(comp_scale, comp_scale + static_cast<size_t>(n_requests) * h->G);
+  if (theta_e != nullptr) d.theta_e.assign(theta_e, theta_e + n_requests);
+  d.precision = precision;
+  d.V = V;
+  d.ldv = ldv;
+  d.k = k;
+  d.out = out;
+  d.ldo = ldo;
+  return run_operator(h, d, static_cast<cudaStream_t>(stream));
+}
+
+int coherit_geno_xtv(coherit_geno_t* h, int32_t slot, int32_t precision, const float* V,
+                     int64_t ldv, int32_t k, const float* comp_scale, float* out, int64_t ldo,
+                     void* stream) {
+  OpDesc d;
+  int rc = make_single(h, slot, k, comp_scale, d);
+  if (rc != COHERIT_OK) return rc;
+  d.xtv = true;
+  d.precision = precision;
+  d.V = V;
+  d.ldv = ldv;
+  d.out = out;
+  d.ldo = ldo;
+  return run_operator(h, d, static_cast<cudaStream_t>(stream));
+}
+
+int coherit_geno_zxb(coherit_geno_t* h, int32_t slot, int32_t precision, const float* b,
+                     int64_t ldb, int32_t C, float* out, int64_t ldo, void* stream) {
+  OpDesc d;
+  int rc = make_single(h, slot, C, nullptr, d);
+  if (rc != COHERIT_OK) return rc;
+  d.zxb = true;
+  d.precision = precision;
+  d.V = b;
+  d.ldv = ldb;
+  d.out = out;
+  d.ldo = ldo;
+  return run_operator(h, d, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,88 @@
+"""Synthetic genotypes and phenotypes of the benchmark configurations.
+
+Genotypes come from a counter-based hash of (seed, SNP, sample): per-SNP MAF
+~ U(0.05, 0.5) and two Bernoulli(MAF) alleles (Hardy-Weinberg), optionally a
+missing code.  The CUDA library evaluates the same hash on the device to
+write the resident matrix directly; this module evaluates it on the host for
+the few SNPs a phenotype needs (its causal set).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_U = np.uint64
+
+
+def _splitmix64(x: np.ndarray) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        x = x + _U(0x9E3779B97F4A7C15)
+        x = (x ^ (x >> _U(30))) * _U(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> _U(27))) * _U(0x94D049BB133111EB)
+    return x ^ (x >> _U(31))
+
+
+def maf_q24(seed: int, snps) -> np.ndarray:
+    s = np.asarray(snps, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        h = _splitmix64(np.full(s.shape, seed, dtype=np.uint64) * _U(0xD1B54A32D192ED03) + s)
+    return (_U(838861) + (h >> _U(20)) % _U(7549747)).astype(np.uint32)
+
+
+def genotype_codes(seed: int, n: int, snps, missing_q24: int = 0) -> np.ndarray:
+    """Codes (n x len(snps), uint8; 3 = missing) of the given SNP indices."""
+    s = np.asarray(snps, dtype=np.uint64).reshape(-1)
+    i = np.arange(n, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        key_s = _splitmix64(np.full(s.shape, seed, dtype=np.uint64) ^ (s * _U(0x8CB92BA72F3D8DD7)))
+        key = key_s[None, :] ^ (i[:, None] * _U(0x9E3779B97F4A7C15))
+    h = _splitmix64(key)
+    maf = maf_q24(seed, s).astype(np.uint64)[None, :]
+    codes = ((h & _U(0xFFFFFF)) < maf).astype(np.uint8) + (
+        ((h >> _U(24)) & _U(0xFFFFFF)) < maf
+    ).astype(np.uint8)
+    if missing_q24:
+        codes[((h >> _U(48)) * _U(256)) < _U(missing_q24)] = 3
+    return codes
+
+
+def missing_rate_q24(rate: float) -> int:
+    if not 0.0 <= rate < 1.0:
+        raise ValueError("missing rate must lie in [0, 1)")
+    return int(round(rate * (1 << 24)))
+
+
+def phenotype(seed: int, n: int, m: int, *, h2: float, n_causal: int, missing_q24: int = 0,
+              n_covar: int = 0, pheno_seed: int | None = None, effect="normal",
+              noise_var: float | None = None):
+    """Phenotype with `n_causal` standardised-genotype effects scaled to h2.
+
+    Returns (y, X, causal_idx, beta) with X = [1, N(0,1) covariates].  The
+    genetic value uses standardised causal genotypes (missing -> mean), its
+    variance is rescaled to h2; the noise is N(0, 1 - h2) unless noise_var
+    is given.
+    """
+    rng = np.random.default_rng(seed if pheno_seed is None else pheno_seed)
+    causal = np.sort(rng.choice(m, size=min(n_causal, m), replace=False))
+    if effect == "laplace":
+        beta = rng.laplace(0.0, 0.1, size=causal.size)
+    else:
+        beta = rng.normal(size=causal.size)
+    g = np.zeros(n)
+    for s0 in range(0, causal.size, 512):
+        idx = causal[s0:s0 + 512]
+        codes = genotype_codes(seed, n, idx, missing_q24).astype(np.float64)
+        miss = codes == 3
+        codes[miss] = np.nan
+        mu = np.nanmean(codes, axis=0)
+        sd = np.nanstd(codes, axis=0)
+        sd[sd == 0] = 1.0
+        z = (codes - mu) / sd
+        z[np.isnan(z)] = 0.0
+        g += z @ beta[s0:s0 + 512]
+    vg = np.var(g)
+    if vg > 0:
+        g *= np.sqrt(h2 / vg)
+    ve = (1.0 - h2) if noise_var is None else noise_var
+    y = g + rng.normal(scale=np.sqrt(ve), size=n)
+    X = np.column_stack([np.ones(n), rng.normal(size=(n, n_covar))]) if n_covar >= 0 else None
+    return y.astype(np.float32), X.astype(np.float32), causal, beta

@@ -1,0 +1,229 @@
+/*
+ * coherit_gpu.h -- C ABI of the GB300 (sm_103a) genotype-operator library.
+ *
+ * The library owns 2-bit packed genotypes resident in HBM and applies the
+ * standardised genomic-relationship operator of COHERIT/GPU_REML to blocks of
+ * right-hand sides:
+ *
+ *     K V = sum_b Z_b (Z_b^T V) / m_eff          (kv_impl.py:9-12)
+ *
+ * where Z_b is the mean-imputed, centred, 1/sd-scaled genotype slice of call
+ * block b (kv_impl.py:69-91).  Every entry point takes plain pointers and
+ * sizes; device pointers are CUDA device addresses on the handle's device and
+ * `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ * All device work is enqueued on `stream`; no entry point synchronises the
+ * stream unless its comment says so.
+ *
+ * Every function returns a status code (COHERIT_OK on success).  The Python
+ * layer maps them onto the exception types of the reference:
+ *   COHERIT_E_SHAPE          -> ValueError      (geno_stream.py:1188-1252, kv_impl.py:538-571)
+ *   COHERIT_E_INDEX          -> IndexError      (geno_stream.py:2687-2690)
+ *   COHERIT_E_NONFINITE      -> FloatingPointError (pcg.py:117-119)
+ *   COHERIT_E_NOT_CONVERGED  -> FloatingPointError (reml.py:770-776)
+ *   COHERIT_E_CLOSED         -> RuntimeError    (geno_stream.py:2610-2614)
+ *   COHERIT_E_OOM, _CUDA, _TIMEOUT, _UNSUPPORTED -> RuntimeError / MemoryError
+ * coherit_last_error() returns a thread-local message for the last failure.
+ */
+#ifndef COHERIT_GPU_H
+#define COHERIT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define COHERIT_OK 0
+#define COHERIT_E_SHAPE 1
+#define COHERIT_E_NONFINITE 2
+#define COHERIT_E_NOT_CONVERGED 3
+#define COHERIT_E_OOM 4
+#define COHERIT_E_TIMEOUT 5
+#define COHERIT_E_CLOSED 6
+#define COHERIT_E_CUDA 7
+#define COHERIT_E_INDEX 8
+#define COHERIT_E_UNSUPPORTED 9
+
+/* Arithmetic of one operator application.
+ *  FP32    : CUDA-core FP32 decode/centre/two contractions; the "plain FP32"
+ *            form of the reference's Precision.HIGHEST matmuls (kv_impl.py:107-113).
+ *  BF16X3  : tcgen05 tensor cores, genotypes exact in BF16, right-hand sides
+ *            split into three BF16 terms (~FP32 accuracy), FP32 accumulation.
+ *  BF16X2 / BF16X1 : fewer split terms (faster, less accurate; for sketches). */
+#define COHERIT_PREC_FP32 0
+#define COHERIT_PREC_BF16X3 1
+#define COHERIT_PREC_BF16X2 2
+#define COHERIT_PREC_BF16X1 3
+
+/* Operator output forms. */
+#define COHERIT_MODE_SUM 0      /* out = sum_g scale_g K_g V (+ theta_e V)         */
+#define COHERIT_MODE_STACKED 1  /* out[g] = scale_g K_g V, shape (G, n, k)          */
+
+typedef struct coherit_geno coherit_geno_t;
+
+const char* coherit_last_error(void);
+int coherit_version(void);
+/* Number of devices and whether device `dev` is a tcgen05-capable part. */
+int coherit_device_info(int dev, int* sm_major, int* sm_minor, int* n_sm, int64_t* hbm_bytes);
+
+/* ---------------------------------------------------------------- genotypes */
+
+/* Build the resident genotype matrix from the reference's packed cache.
+ * Replaces GenoBlockStreamer's tmpfile/ring cache (geno_stream.py:1323-1331,
+ * :2358-2396) and its per-call H2D streaming (kv_impl.py:300-320).
+ *   packed            : concatenation over calls c of row-major (n, ceil(w_c/4))
+ *                       uint8 blocks; SNP 4j+s of a row sits at bits 2s..2s+1 of
+ *                       byte j; codes 0/1/2 = allele count, 3 = missing
+ *                       (kv_impl.py:58-66, geno_stream.py:1263).  Host memory
+ *                       unless packed_on_device != 0.
+ *   call_widths       : n_calls true widths (geno_stream.py:1303)
+ *   call_component_ids: n_calls component ids (NULL = all component 0);
+ *                       calls of one component must be contiguous
+ *                       (geno_stream.py:469-505).                              */
+int coherit_geno_create_packed(const uint8_t* packed, int64_t n, int32_t n_calls,
+                               const int32_t* call_widths, const int32_t* call_component_ids,
+                               int32_t n_components, int packed_on_device, int device,
+                               void* stream, coherit_geno_t** out);
+
+/* Build a synthetic resident matrix (no host copy): per-SNP MAF ~ U(0.05, 0.5)
+ * and genotypes ~ Binomial(2, MAF) drawn from a counter-based hash of
+ * (seed, snp, sample); `missing_q24` = missing rate * 2^24 (0 = none).  The
+ * same generator is restated in the oracle so both see identical genotypes.
+ * component_sizes: n_components SNP counts (NULL = one component of m).      */
+int coherit_geno_create_synthetic(int64_t n, int64_t m, const int32_t* component_sizes,
+                                  int32_t n_components, uint64_t seed, uint32_t missing_q24,
+                                  int device, void* stream, coherit_geno_t** out);
+
+int coherit_geno_destroy(coherit_geno_t* h);
+
+/* Shapes: n samples, m SNPs, padded extents of the HBM layout, components,
+ * number of missing genotype entries, bytes held on the device.             */
+int coherit_geno_info(const coherit_geno_t* h, int64_t* n, int64_t* m, int64_t* n_pad,
+                      int64_t* m_pad, int32_t* n_components, int64_t* n_missing,
+                      int64_t* device_bytes);
+
+/* Copy back the reference-layout packed bytes of call-sized column range
+ * [snp_start, snp_start+width) as a row-major (n, ceil(width/4)) host block
+ * (the bytes GenoBlockStreamer._pop_cached returns, geno_stream.py:2605-2617). */
+int coherit_geno_read_packed(coherit_geno_t* h, int64_t snp_start, int32_t width,
+                             uint8_t* out_host, void* stream);
+
+/* ------------------------------------------------------------ standardisation */
+
+/* Compute per-SNP statistics of stats slot `slot` over the samples selected by
+ * `sample_mask` (n host bytes, nonzero = keep; NULL = all samples), following
+ * the reference's FP32 formulas (geno_stream.py:1780-1792):
+ *     mean = s1/max(cnt,1); var = max(s2/max(cnt,1) - mean^2, 0);
+ *     inv_sd = 1/sqrt(max(var,1e-6)) if cnt>0 and var>0 else 0.
+ * Slot 0 is the full-sample slot used by default.  Outputs (host, length m,
+ * cache order; any may be NULL): mean, inv_sd, count of observed genotypes.
+ * Synchronises `stream`.                                                    */
+int coherit_geno_compute_stats(coherit_geno_t* h, int32_t slot, const uint8_t* sample_mask,
+                               float* mean_out, float* inv_sd_out, int32_t* count_out,
+                               void* stream);
+
+/* Install externally supplied standardisation (standardization_override,
+ * geno_stream.py:1283-1292) into slot `slot`.  mean/inv_sd: host, length m. */
+int coherit_geno_set_stats(coherit_geno_t* h, int32_t slot, const uint8_t* sample_mask,
+                           const float* mean, const float* inv_sd, void* stream);
+
+/* Free a stats slot (slot > 0). */
+int coherit_geno_release_stats(coherit_geno_t* h, int32_t slot);
+
+/* Per-component effective SNP counts m_eff (#inv_sd>0) and mean-diagonal atoms
+ * tr(K_g)/n of slot `slot` (geno_stream.py:1409-1444); host arrays of length
+ * n_components; the totals over all components go to *eff_total / *atom_total.
+ */
+int coherit_geno_stats_summary(const coherit_geno_t* h, int32_t slot, double* comp_eff,
+                               double* comp_atom, double* eff_total, double* atom_total);
+
+/* Exact sample-wise diagonal of the whole-matrix GRM, diag(K)_i =
+ * sum_j z_ij^2 / m_eff in FP64 (geno_stream.py:2780-2821).  out: device, n.   */
+int coherit_geno_exact_diag(coherit_geno_t* h, int32_t slot, float* out, void* stream);
+
+/* ------------------------------------------------------------------ operator */
+
+/* Reserve the operator workspace for right-hand-side blocks of up to k_max
+ * columns so later calls allocate nothing (needed before stream capture).   */
+int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision);
+
+/* Genotype operator on V (device, n x k, row stride ldv floats).
+ * MODE_SUM:     out[i,c] = sum_g comp_scale[g] (Z_g Z_g^T V)[i,c] + theta_e V[i,c]
+ * MODE_STACKED: out[g*n*ldo + i*ldo + c] = comp_scale[g] (Z_g Z_g^T V)[i,c]
+ * comp_scale (host, n_components): per-component multiplier applied to
+ * Z_g Z_g^T, e.g. 1/m_eff,g for kv(normalize=True) (kv_impl.py:320-324),
+ * theta_g/m_eff,g for the weighted H.V (kv_impl.py:1116-1131).
+ * snp_weight: optional device array (m, cache order) of per-SNP kernel weights
+ * (kv_impl.py:139-160); NULL = none.
+ * Replaces kv_impl_streamed (kv_impl.py:268-326), kv_impl_partitioned_weighted
+ * (:1089-1135), kv_impl_partitioned_stacked (:1138-1187),
+ * kv_impl_snp_weighted_streamed (:329-379).                                 */
+int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t precision,
+                    const float* V, int64_t ldv, int32_t k, const float* comp_scale,
+                    int32_t use_theta_e, float theta_e, const float* snp_weight,
+                    float* out, int64_t ldo, void* stream);
+
+/* Batched operator for independent requests sharing the genotypes: columns
+ * [col_start[r], col_start[r+1]) of V belong to request r, which uses stats
+ * slot slots[r] (its own sample subset, mean, sd, m_eff), per-component scale
+ * comp_scale[r*G + g] and residual weight theta_e[r] (NULL = none).  Rows
+ * outside a request's subset are returned as zero; V must be zero there.   */
+int coherit_geno_kv_batched(coherit_geno_t* h, int32_t n_requests, const int32_t* col_start,
+                            const int32_t* slots, int32_t precision, const float* V,
+                            int64_t ldv, int32_t k, const float* comp_scale,
+                            const float* theta_e, float* out, int64_t ldo, void* stream);
+
+/* X^T V: out (device, m x k, row stride ldo, cache SNP order) =
+ * scale[g(j)] * inv_sd_j * (diff^T V)_j   (kv_impl.py:163-185, :382-439).     */
+int coherit_geno_xtv(coherit_geno_t* h, int32_t slot, int32_t precision, const float* V,
+                     int64_t ldv, int32_t k, const float* comp_scale, float* out, int64_t ldo,
+                     void* stream);
+
+/* Z b: out (device, n x C, row stride ldo) = sum_j diff_ij inv_sd_j b[j,:]
+ * for b (device, m x C, row stride ldb, cache order) (kv_impl.py:221-265).   */
+int coherit_geno_zxb(coherit_geno_t* h, int32_t slot, int32_t precision, const float* b,
+                     int64_t ldb, int32_t C, float* out, int64_t ldo, void* stream);
+
+/* Device-side error flag: returns COHERIT_E_TIMEOUT if any kernel of this
+ * handle gave up on a bounded wait since the last call (and clears it).
+ * Synchronises `stream`.                                                    */
+int coherit_geno_check(coherit_geno_t* h, void* stream);
+
+/* -------------------------------------------------------- solver primitives */
+
+/* Column reductions over n rows for k columns (device arrays, row strides):
+ *   op 0: out[c] = sum_i A[i,c] * B[i,c]     op 1: out[c] = sum_i A[i,c]^2
+ * accumulated in FP64; out is device, k doubles.                            */
+int coherit_colreduce(int32_t op, int64_t n, int32_t k, const float* A, int64_t lda,
+                      const float* B, int64_t ldb, double* out, void* stream);
+
+/* Fused block-PCG state update (pcg.py:31-48): given the column sums
+ * denom = sum(P*AP), rs and the active mask, computes
+ * alpha = active&valid ? rs/denom : 0, X += P alpha, R -= AP alpha, and sets
+ * *breakdown (device int) if an active column had a non-positive or
+ * non-finite curvature. rs/denom device doubles, active device uint8.        */
+int coherit_pcg_state_update(int64_t n, int32_t k, float* X, int64_t ldx, float* R,
+                             int64_t ldr, const float* P, int64_t ldp, const float* AP,
+                             int64_t ldap, const double* rs, const double* denom,
+                             const uint8_t* active, int32_t* breakdown, void* stream);
+
+/* Fused block-PCG direction update (pcg.py:51-65): given rs_new = sum(R*Z),
+ * rnorm^2 = sum(R*R), rs_old and threshold, writes active = rnorm > thr,
+ * beta = active ? rs_new/(rs_old>0 ? rs_old : 1) : 0, P = active ? Z + P beta : 0,
+ * rs_old <- active ? rs_new : 0, rnorm_out <- sqrt(rnorm^2).                  */
+int coherit_pcg_direction_update(int64_t n, int32_t k, float* P, int64_t ldp,
+                                 const float* Z, int64_t ldz, const double* rs_new,
+                                 const double* rnorm2, double* rs_old, const double* threshold,
+                                 uint8_t* active, double* rnorm_out, void* stream);
+
+/* One-tile tensor-core self-test (no counterpart in the reference): computes
+ * D(128x16) = A(128x16) B(16x16)^T for fixed small integers with A taken from
+ * tensor memory (variant 0) or shared memory (variant 1) and copies D to
+ * out_host (128*16 floats, row-major).  Synchronises `stream`.              */
+int coherit_selftest_mma(int32_t variant, float* out_host, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COHERIT_GPU_H */

@@ -1,0 +1,49 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every declared symbol."""
+import ctypes
+import re
+from pathlib import Path
+
+from coherit_gb300 import _lib, build_ext
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "coherit_gpu.h"
+
+
+def declared_symbols():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"\b(coherit_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_builds_and_loads():
+    path = build_ext.build()
+    assert path.exists()
+    lib = ctypes.CDLL(str(path))
+    assert lib.coherit_version() == 1
+
+
+def test_every_declared_symbol_is_exported_and_bound():
+    lib = _lib.load()
+    declared = declared_symbols()
+    assert len(declared) >= 20
+    for name in declared:
+        assert hasattr(lib, name), f"{name} declared in coherit_gpu.h but not exported"
+    assert set(declared) == set(_lib.exported_symbols())
+
+
+def test_status_mapping():
+    import pytest
+
+    with pytest.raises(ValueError):
+        _lib.check(_lib.E_SHAPE)
+    with pytest.raises(IndexError):
+        _lib.check(_lib.E_INDEX)
+    with pytest.raises(FloatingPointError):
+        _lib.check(_lib.E_NONFINITE)
+    with pytest.raises(RuntimeError):
+        _lib.check(_lib.E_CLOSED)
+    _lib.check(_lib.OK)
+
+
+def test_null_handle_is_rejected_without_gpu():
+    lib = _lib.load()
+    assert lib.coherit_geno_info(None, None, None, None, None, None, None, None) == _lib.E_CLOSED
+    assert lib.coherit_geno_check(None, None) == _lib.E_CLOSED

@@ -1,0 +1,247 @@
+"""Parity of the CUDA genotype operator with the FP64 oracle (GPU).
+
+Tolerance: every output column within 1e-5 relative (2-norm) of the FP64
+oracle on the same genotypes and statistics; statistics and packed bytes
+bit-exact.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import geno as og
+from coherit_gb300 import _lib, synth
+from coherit_gb300.geno_stream import ArraySource, GenoBlockStreamer, SyntheticSource
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def col_rel(out, ref):
+    out = np.asarray(out, np.float64)
+    ref = np.asarray(ref, np.float64)
+    if out.ndim == 1:
+        out, ref = out[:, None], ref[:, None]
+    num = np.linalg.norm(out - ref, axis=0)
+    den = np.maximum(np.linalg.norm(ref, axis=0), 1e-300)
+    return float(np.max(num / den))
+
+
+def oracle_codes(seed, n, m, miss):
+    return og.synth_codes(seed, n, np.arange(m), missing_q24=synth.missing_rate_q24(miss))
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+def test_mma_selftest_tile(cuda, variant):
+    lib = _lib.load()
+    out = np.zeros(128 * 16, dtype=np.float32)
+    _lib.check(lib.coherit_selftest_mma(variant, out.ctypes.data, _lib.stream_ptr()), "selftest")
+    m = np.arange(128)[:, None, None]
+    n = np.arange(16)[None, :, None]
+    k = np.arange(16)[None, None, :]
+    a = ((m * 3 + k * 5) % 7) - 3
+    b = ((n * 2 + k) % 5) - 2
+    expect = np.sum(a * b, axis=2).astype(np.float32)
+    np.testing.assert_array_equal(out.reshape(128, 16), expect)
+
+
+def _streamer(n, m, seed=1, miss=0.0, comps=None, precision="bf16x3", call_width=131072):
+    src = SyntheticSource(n, m, seed=seed, missing_rate=miss)
+    return GenoBlockStreamer(src, component_block_sizes=comps, precision=precision,
+                             call_width=call_width)
+
+
+@pytest.mark.parametrize("miss", [0.0, 0.04])
+def test_synthetic_layout_stats_bit_exact(cuda, miss):
+    n, m = 333, 1000
+    st = _streamer(n, m, seed=7, miss=miss, call_width=384)
+    codes = oracle_codes(7, n, m, miss)
+    for c in range(st._n_calls):
+        s0, w = int(st._call_snp_starts[c]), int(st._call_true_widths[c])
+        np.testing.assert_array_equal(st._pop_cached(c), og.pack_block(codes[:, s0:s0 + w]))
+    mean, inv, cnt = og.stats(codes)
+    np.testing.assert_array_equal(st._means_host, mean)
+    np.testing.assert_array_equal(st._inv_sds_host, inv)
+    np.testing.assert_array_equal(st._count_host, cnt)
+    assert st.info()["n_missing"] == int(np.sum(codes == 3))
+    cnt_, s1, s2 = og.raw_counts(codes)
+    _, _, eff, atom = og.stats_summary(cnt_, s1, s2, mean, inv, n)
+    assert float(st._eff_m_const) == eff
+    np.testing.assert_allclose(float(st.diag()), atom, rtol=1e-6)
+    st.close()
+
+
+def test_array_source_round_trip_and_partition(cuda):
+    n, m = 150, 257
+    codes = oracle_codes(3, n, m, 0.05)
+    g = codes.astype(np.int8)
+    g[codes == 3] = -127
+    st = GenoBlockStreamer(ArraySource(g, missing_val=-127), call_width=100,
+                           component_block_sizes=[57, 200], precision="bf16x3")
+    for c in range(st._n_calls):
+        s0, w = int(st._call_snp_starts[c]), int(st._call_true_widths[c])
+        np.testing.assert_array_equal(st._pop_cached(c), og.pack_block(codes[:, s0:s0 + w]))
+    assert st._call_component_ids.tolist() == [0, 1, 1]
+    mean, inv, cnt = og.stats(codes)
+    np.testing.assert_array_equal(st._means_host, mean)
+    np.testing.assert_array_equal(st._inv_sds_host, inv)
+    st.close()
+    with pytest.raises(RuntimeError):
+        st.kv(np.zeros((n, 1), np.float32))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+@pytest.mark.parametrize("n,m,k,miss", [
+    (1000, 3000, 7, 0.0),
+    (1000, 3000, 7, 0.03),
+    (130, 70, 1, 0.0),
+    (257, 1500, 20, 0.01),
+    (600, 2000, 130, 0.0),
+])
+def test_kv_matches_fp64_oracle(cuda, precision, n, m, k, miss):
+    st = _streamer(n, m, seed=11, miss=miss, precision=precision)
+    codes = oracle_codes(11, n, m, miss)
+    mean, inv = st._means_host, st._inv_sds_host
+    eff = float(st._eff_m_const)
+    rng = np.random.default_rng(k)
+    V = rng.normal(size=(n, k)).astype(np.float32)
+    out = st.kv(torch.as_tensor(V, device=cuda)).cpu().numpy()
+    ref = og.kv_f64(codes, mean, inv, V, comp_scale=[1 / eff])
+    err = col_rel(out, ref)
+    assert err < TOL, f"{precision}: max column relative error {err:.3e}"
+    st.check()
+    st.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_vector_rhs_and_unnormalized(cuda, precision):
+    n, m = 300, 500
+    st = _streamer(n, m, seed=5, precision=precision)
+    codes = oracle_codes(5, n, m, 0.0)
+    v = np.random.default_rng(0).normal(size=n).astype(np.float32)
+    out = st.kv(v, normalize=False).cpu().numpy()
+    assert out.shape == (n,)
+    ref = og.kv_f64(codes, st._means_host, st._inv_sds_host, v)
+    assert col_rel(out, ref) < TOL
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_components_stacked_weighted(cuda, precision):
+    n, m = 500, 2100
+    comps = [700, 1300, 100]
+    st = _streamer(n, m, seed=13, miss=0.02, comps=comps, precision=precision)
+    codes = oracle_codes(13, n, m, 0.02)
+    mean, inv = st._means_host, st._inv_sds_host
+    comp = np.repeat(np.arange(3), comps)
+    effs = st._component_eff_m_host.astype(np.float64)
+    V = np.random.default_rng(1).normal(size=(n, 5)).astype(np.float32)
+    stacked = st.stacked_component_kv(V).cpu().numpy()
+    ref = og.kv_f64(codes, mean, inv, V, comp_of_snp=comp, comp_scale=1 / effs, stacked=True,
+                    n_components=3)
+    for g in range(3):
+        assert col_rel(stacked[g], ref[g]) < TOL
+    one = st.component_kv(V, 1).cpu().numpy()
+    assert col_rel(one, ref[1]) < TOL
+    theta = np.asarray([0.3, 0.5, 0.2])
+    hv = st.weighted_component_hv(theta, 0.7, V).cpu().numpy()
+    ref_hv = og.kv_f64(codes, mean, inv, V, comp_of_snp=comp, comp_scale=theta / effs,
+                       n_components=3, theta_e=0.7)
+    assert col_rel(hv, ref_hv) < TOL
+    atoms = st.build_projected_core_atoms(torch.linalg.qr(
+        torch.as_tensor(V, device=cuda))[0], subtract_identity=False).cpu().numpy()
+    U = np.linalg.qr(V.astype(np.float64))[0]
+    for g in range(3):
+        sel = comp == g
+        XtU = og.xtv_f64(codes[:, sel], mean[sel], inv[sel], U)
+        np.testing.assert_allclose(np.abs(atoms[g]), np.abs(XtU.T @ XtU / effs[g]), rtol=1e-4,
+                                   atol=1e-5)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_xtv_zxb_exact_diag(cuda, precision):
+    n, m = 400, 900
+    st = _streamer(n, m, seed=17, miss=0.02, precision=precision)
+    codes = oracle_codes(17, n, m, 0.02)
+    mean, inv = st._means_host, st._inv_sds_host
+    V = np.random.default_rng(2).normal(size=(n, 3)).astype(np.float32)
+    xt = st.xtv(V).cpu().numpy()
+    assert col_rel(xt, og.xtv_f64(codes, mean, inv, V)) < TOL
+    b = np.random.default_rng(3).normal(size=(m, 2)).astype(np.float32)
+    zb = st.zxb(b).cpu().numpy()
+    assert col_rel(zb, og.zxb_f64(codes, mean, inv, b)) < TOL
+    d = st.exact_diag().cpu().numpy()
+    np.testing.assert_allclose(d, og.exact_diag(codes, mean, inv, float(st._eff_m_const)),
+                               rtol=1e-6)
+
+
+def test_batched_subsets_equal_single_requests(cuda):
+    n, m = 700, 1600
+    st = _streamer(n, m, seed=19, miss=0.01, precision="bf16x3")
+    lib = _lib.load()
+    codes = oracle_codes(19, n, m, 0.01)
+    rng = np.random.default_rng(4)
+    masks = [rng.random(n) < f for f in (0.3, 0.9, 0.6)]
+    widths = [3, 5, 2]
+    stream = _lib.stream_ptr()
+    slots = []
+    for r, mk in enumerate(masks):
+        mean = np.zeros(m, np.float32)
+        inv = np.zeros(m, np.float32)
+        _lib.check(lib.coherit_geno_compute_stats(
+            st.handle, r + 1, mk.astype(np.uint8).ctypes.data, mean.ctypes.data,
+            inv.ctypes.data, None, stream))
+        om, oi, _ = og.stats(codes, mk)
+        np.testing.assert_array_equal(mean, om)
+        np.testing.assert_array_equal(inv, oi)
+        slots.append((mean, inv))
+    col_start = np.concatenate([[0], np.cumsum(widths)]).astype(np.int32)
+    k = int(col_start[-1])
+    V = rng.normal(size=(n, k)).astype(np.float32)
+    scale = np.asarray([1.0 / np.count_nonzero(s[1] > 0) for s in slots], np.float32)
+    theta = np.asarray([0.2, 0.0, 1.5], np.float32)
+    Vd = torch.as_tensor(V, device=cuda)
+    out = torch.empty_like(Vd)
+    _lib.check(lib.coherit_geno_kv_batched(
+        st.handle, 3, col_start.ctypes.data, np.asarray([1, 2, 3], np.int32).ctypes.data,
+        _lib.PREC_BF16X3, Vd.data_ptr(), k, k, scale.ctypes.data, theta.ctypes.data,
+        out.data_ptr(), k, stream))
+    out = out.cpu().numpy()
+    for r, mk in enumerate(masks):
+        sl = slice(col_start[r], col_start[r + 1])
+        ref = og.kv_f64(codes, slots[r][0], slots[r][1], V[:, sl], comp_scale=[scale[r]],
+                        sample_mask=mk, theta_e=float(theta[r]))
+        assert col_rel(out[mk, sl], ref[mk]) < TOL
+        assert np.all(out[~mk, sl] == 0)
+    st.check()
+
+
+def test_wide_rhs_column_blocks(cuda):
+    n, m, k = 260, 800, 300
+    st = _streamer(n, m, seed=23, precision="bf16x3")
+    codes = oracle_codes(23, n, m, 0.0)
+    V = np.random.default_rng(5).normal(size=(n, k)).astype(np.float32)
+    out = st.kv(V).cpu().numpy()
+    ref = og.kv_f64(codes, st._means_host, st._inv_sds_host, V,
+                    comp_scale=[1 / float(st._eff_m_const)])
+    assert col_rel(out, ref) < TOL
+
+
+def test_standardization_override(cuda):
+    n, m = 200, 300
+    codes = oracle_codes(29, n, m, 0.05)
+    g = codes.astype(np.int8)
+    g[codes == 3] = -127
+    rng = np.random.default_rng(6)
+    mo = rng.uniform(0.1, 1.9, size=m).astype(np.float32)
+    io = rng.uniform(0.5, 2.0, size=m).astype(np.float32)
+    io[::17] = 0
+    st = GenoBlockStreamer(ArraySource(g), standardization_override=(mo, io), precision="bf16x3")
+    V = rng.normal(size=(n, 4)).astype(np.float32)
+    eff = float(np.count_nonzero(io > 0))
+    assert float(st._eff_m_const) == eff
+    out = st.kv(V).cpu().numpy()
+    assert col_rel(out, og.kv_f64(codes, mo, io, V, comp_scale=[1 / eff])) < TOL
+    cnt, s1, s2 = og.raw_counts(codes)
+    _, _, _, atom = og.stats_summary(cnt, s1, s2, mo, io, n, override=True)
+    np.testing.assert_allclose(float(st.diag()), atom, rtol=1e-6)
