@@ -54,6 +54,7 @@ _f32 = C.c_float
 _SIGNATURES = {
     "coherit_last_error": (C.c_char_p, []),
     "coherit_version": (C.c_int, []),
+    "coherit_launch_count": (C.c_int64, []),
     "coherit_device_info": (C.c_int, [C.c_int, _p, _p, _p, _p]),
     "coherit_geno_create_packed": (
         C.c_int,

@@ -34,6 +34,8 @@ constexpr int kTile = 128;                           // rows per block
 
 // -------------------------------------------------------------- status
 void set_error(const char* fmt, ...);
+// Process-wide count of kernels this library has launched.
+void note_launch();
 int cuda_status(cudaError_t e, const char* what);
 
 #define CO_CUDA(call)                                         \

@@ -2,6 +2,7 @@
 // cache or from the synthetic generator), the two HBM layouts, per-SNP
 // statistics, missing-genotype lists, exact diagonal, and the C entry points
 // that manage the handle.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -13,6 +14,9 @@
 namespace coherit {
 
 static thread_local std::string g_last_error;
+static std::atomic<int64_t> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const char* fmt, ...) {
   char buf[1024];
@@ -323,7 +327,7 @@ int build_layout_from_ref(coherit_geno* h, const uint8_t* d_packed, const int64_
   if (work > 0)
     k_build_s_from_ref<<<grid_of(work, 256), 256, 0, st>>>(
         h->geno_s, h->n, h->n_pad, h->n_panels, d_packed, d_call_off, d_call_pw, d_snp_call,
-        d_snp_col, h->d_snp_of_slot);
+        d_snp_col, h->d_snp_of_slot); note_launch();
   CO_CUDA(cudaGetLastError());
   return build_copy_t(h, st);
 }
@@ -332,7 +336,7 @@ int build_layout_synthetic(coherit_geno* h, uint64_t seed, uint32_t miss_q24, cu
   const int64_t work = h->n_pad * h->n_panels;
   if (work > 0)
     k_build_s_synth<<<grid_of(work, 256), 256, 0, st>>>(h->geno_s, h->n, h->n_pad, h->n_panels,
-                                                        h->d_snp_of_slot, seed, miss_q24);
+                                                        h->d_snp_of_slot, seed, miss_q24); note_launch();
   CO_CUDA(cudaGetLastError());
   return build_copy_t(h, st);
 }
@@ -340,7 +344,7 @@ int build_layout_synthetic(coherit_geno* h, uint64_t seed, uint32_t miss_q24, cu
 int build_copy_t(coherit_geno* h, cudaStream_t st) {
   if (h->n_ttiles > 0 && h->n_chunks > 0) {
     dim3 grid(static_cast<unsigned>(h->n_chunks), static_cast<unsigned>(h->n_ttiles));
-    k_build_t_from_s<<<grid, 128, 0, st>>>(h->geno_t, h->geno_s, h->n_panels, h->n_chunks);
+    k_build_t_from_s<<<grid, 128, 0, st>>>(h->geno_t, h->geno_s, h->n_panels, h->n_chunks); note_launch();
   }
   CO_CUDA(cudaGetLastError());
   return COHERIT_OK;
@@ -358,7 +362,7 @@ int build_missing_lists(coherit_geno* h, cudaStream_t st) {
   d_n2 = d_n1 + h->m_pad;
   d_n3 = d_n2 + h->m_pad;
   k_slot_counts<<<grid_of(h->m_pad, 128), 128, 0, st>>>(h->geno_t, h->m_pad, h->n_chunks, nullptr,
-                                                        d_n1, d_n2, d_n3);
+                                                        d_n1, d_n2, d_n3); note_launch();
   std::vector<int64_t> slot_miss(h->m_pad);
   cudaError_t e = cudaMemcpyAsync(slot_miss.data(), d_n3, sizeof(int64_t) * h->m_pad,
                                   cudaMemcpyDeviceToHost, st);
@@ -373,7 +377,7 @@ int build_missing_lists(coherit_geno* h, cudaStream_t st) {
   exclusive_scan_host(slot_miss, csc_off);
   CO_CUDA(cudaMalloc(&d_sc, sizeof(int64_t) * h->n_pad));
   k_sample_missing_counts<<<grid_of(h->n_pad, 128), 128, 0, st>>>(h->geno_s, h->n_pad,
-                                                                   h->n_panels, d_sc);
+                                                                   h->n_panels, d_sc); note_launch();
   std::vector<int64_t> samp_miss(h->n_pad);
   e = cudaMemcpyAsync(samp_miss.data(), d_sc, sizeof(int64_t) * h->n_pad, cudaMemcpyDeviceToHost,
                       st);
@@ -392,9 +396,9 @@ int build_missing_lists(coherit_geno* h, cudaStream_t st) {
   CO_CUDA(cudaMemcpyAsync(h->d_csr_off, csr_off.data(), sizeof(int64_t) * (h->n_pad + 1),
                           cudaMemcpyHostToDevice, st));
   k_fill_csc<<<grid_of(h->m_pad, 128), 128, 0, st>>>(h->geno_t, h->m_pad, h->n_chunks,
-                                                     h->d_csc_off, h->d_csc_idx);
+                                                     h->d_csc_off, h->d_csc_idx); note_launch();
   k_fill_csr<<<grid_of(h->n_pad, 128), 128, 0, st>>>(h->geno_s, h->n_pad, h->n_panels,
-                                                     h->d_csr_off, h->d_csr_idx);
+                                                     h->d_csr_off, h->d_csr_idx); note_launch();
   CO_CUDA(cudaGetLastError());
   CO_CUDA(cudaStreamSynchronize(st));
   return COHERIT_OK;
@@ -415,14 +419,14 @@ int compute_slot_stats(coherit_geno* h, StatsSlot& s, const float* override_mean
   int64_t* d_n2 = d_cnt + mp;
   int64_t* d_n3 = d_cnt + 2 * mp;
   k_slot_counts<<<grid_of(mp, 128), 128, 0, st>>>(h->geno_t, mp, h->n_chunks, s.tmask, d_n1, d_n2,
-                                                  d_n3);
+                                                  d_n3); note_launch();
   std::vector<int32_t> snp_of_slot(mp);
   std::vector<float> mean(mp, 0.f), inv(mp, 0.f);
   std::vector<int64_t> n1(mp), n2(mp), n3(mp);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && override_mean == nullptr) {
     k_slot_stats<<<grid_of(mp, 256), 256, 0, st>>>(mp, s.n_sub, d_n1, d_n2, d_n3,
-                                                   h->d_snp_of_slot, s.mean, s.inv);
+                                                   h->d_snp_of_slot, s.mean, s.inv); note_launch();
     e = cudaGetLastError();
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(mean.data(), s.mean, sizeof(float) * mp, cudaMemcpyDeviceToHost, st);
@@ -494,7 +498,7 @@ int exact_diag_launch(coherit_geno* h, const StatsSlot& s, float* out, cudaStrea
   const double inv_eff = s.eff_total > 0.0 ? 1.0 / s.eff_total : 0.0;
   if (h->n > 0)
     k_exact_diag<<<grid_of(h->n, 128), 128, 0, st>>>(h->geno_s, h->n, h->n_panels, s.mean, s.inv,
-                                                     s.row_mask, inv_eff, out);
+                                                     s.row_mask, inv_eff, out); note_launch();
   CO_CUDA(cudaGetLastError());
   return COHERIT_OK;
 }
@@ -580,7 +584,7 @@ static int init_slot(coherit_geno* h, int32_t slot, const uint8_t* sample_mask, 
     CO_CUDA(cudaMalloc(&s.tmask, sizeof(uint32_t) * 4 * h->n_chunks));
     CO_CUDA(cudaMemcpyAsync(s.row_mask, rm.data(), h->n_pad, cudaMemcpyHostToDevice, st));
     k_build_tmask<<<grid_of(h->n_chunks, 128), 128, 0, st>>>(s.row_mask, h->n, h->n_chunks,
-                                                             s.tmask);
+                                                             s.tmask); note_launch();
     CO_CUDA(cudaGetLastError());
   }
   return COHERIT_OK;
@@ -624,6 +628,8 @@ extern "C" {
 const char* coherit_last_error(void) { return g_last_error.c_str(); }
 
 int coherit_version(void) { return 1; }
+
+int64_t coherit_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int coherit_device_info(int dev, int* sm_major, int* sm_minor, int* n_sm, int64_t* hbm_bytes) {
   cudaDeviceProp prop;
@@ -784,7 +790,7 @@ int coherit_geno_read_packed(coherit_geno_t* h, int64_t snp_start, int32_t width
   uint8_t* d = nullptr;
   CO_CUDA(cudaMalloc(&d, bytes));
   k_read_packed<<<grid_of(bytes, 256), 256, 0, st>>>(d, h->geno_s, h->n, h->n_panels,
-                                                     h->d_slot_of_snp, snp_start, width);
+                                                     h->d_slot_of_snp, snp_start, width); note_launch();
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(out_host, d, bytes, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

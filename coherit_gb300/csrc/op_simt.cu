@@ -211,15 +211,15 @@ int run_operator_fp32(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
   p.sf = static_cast<float*>(h->ws.base);
   const unsigned cblocks = static_cast<unsigned>((kp + kSimtCols - 1) / kSimtCols);
   if (d.zxb) {
-    k_simt_prep_b<<<static_cast<unsigned>((h->m_pad + 127) / 128), 128, 0, st>>>(p, d.V, d.ldv);
+    k_simt_prep_b<<<static_cast<unsigned>((h->m_pad + 127) / 128), 128, 0, st>>>(p, d.V, d.ldv); note_launch();
     p.use_theta_e = 0;
   } else {
-    k_simt_k1<<<dim3(static_cast<unsigned>(h->m_pad / kSimtRows), cblocks), 256, 0, st>>>(p);
+    k_simt_k1<<<dim3(static_cast<unsigned>(h->m_pad / kSimtRows), cblocks), 256, 0, st>>>(p); note_launch();
   }
   CO_CUDA(cudaGetLastError());
   if (d.xtv) return COHERIT_OK;
   const unsigned nz = p.stacked ? static_cast<unsigned>(h->G) : 1u;
-  k_simt_k2<<<dim3(static_cast<unsigned>(h->n_pad / kSimtRows), cblocks, nz), 256, 0, st>>>(p);
+  k_simt_k2<<<dim3(static_cast<unsigned>(h->n_pad / kSimtRows), cblocks, nz), 256, 0, st>>>(p); note_launch();
   CO_CUDA(cudaGetLastError());
   return COHERIT_OK;
 }

@@ -18,14 +18,7 @@
 // in kv_impl.py:69-91.  V and S are split into up to three BF16 terms
 // (hi + mid + lo) that all accumulate into one FP32 tensor-memory accumulator.
 //
-// Kernel anatomy (224 threads, 1 CTA of work per tile):
-//   warp 0  : bulk-copies 2 KB genotype blocks into a 16-deep shared ring
-//   warp 6  : bulk-copies B tiles (V or S split terms) into a shared ring
-//   warps 2-5: decode a genotype row (16 B = 64 codes) to 32 BF16 pairs and
-//             store them into a 4-deep tensor-memory A ring (tcgen05.st);
-//             afterwards they run the epilogue from the accumulator
-//   warp 1  : allocates tensor memory; lane 0 issues tcgen05.mma (A from
-//             tensor memory, B from shared memory) and commits to mbarriers.
+// Kernel anatomy: see tc_kernel.cuh.
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
@@ -35,11 +28,12 @@
 
 namespace coherit {
 
-constexpr int kThreads = 224;
-constexpr int kWarpG = 0, kWarpMMA = 1, kWarpB = 6;
-constexpr int kRG = 16;      // genotype ring depth
-constexpr int kRA = 4;       // tensor-memory A ring depth (32 columns each)
-constexpr int kMaxRB = 16;   // B ring depth limit
+constexpr int kSets = 3;        // decoder warp sets (chunks in flight through the A ring)
+constexpr int kThreads = 32 * (3 + 4 * kSets);
+constexpr int kWarpG = 0, kWarpMMA = 1, kWarpB = 2, kWarpDec0 = 3;
+constexpr int kRG = 24;        // genotype ring depth (2 KB blocks)
+constexpr int kMaxRA = 8;      // tensor-memory A ring depth limit (32 columns each)
+constexpr int kMaxRB = 16;     // B ring depth limit
 constexpr int kMaxGroups = 32;
 constexpr int kMaxScale = 256;
 constexpr int kBarrierBytes = 1024;
@@ -74,6 +68,7 @@ struct TcParams {
   const uint8_t* bsrc;
   int64_t b_chunk_bytes;
   int RB;
+  int RA;
   uint32_t bslot_bytes;
   uint32_t tmem_cols;
   uint32_t acc_cols;
@@ -87,11 +82,17 @@ __device__ __forceinline__ int group_of(const EpiParams& e, int c) {
   return r;
 }
 
-// 16 bytes = 64 genotype codes of one row -> 32 words of BF16 pairs in K
-// order (word t = elements 2t, 2t+1; code 3 -> 0).
+// Decoding: a row of the genotype layout holds element 16w + 4s + b at bits
+// 8b + 2s of word w, so (word >> 2s) & 0x03030303 yields four consecutive
+// codes, one per byte.  t*17 + 0x40404040 turns each code c into the byte
+// selector pair (c, c+4) of __byte_perm over the table bytes
+// L = {0x00, 0x80, 0x00, 0x00}, H = {0x00, 0x3F, 0x40, 0x00}, i.e. the low and
+// high bytes of bf16(0), bf16(1), bf16(2) and bf16(0) for code 3 (missing).
+// 16 bytes = 64 codes -> 32 words of BF16 pairs in K order (word t =
+// elements 2t, 2t+1).
 __device__ __forceinline__ void decode_row(const uint4 raw, uint32_t (&a)[32]) {
-  const uint32_t L = 0x00008000u;  // low bytes of bf16(0), bf16(1), bf16(2), bf16(0)
-  const uint32_t H = 0x00403F00u;  // high bytes
+  const uint32_t L = 0x00008000u;
+  const uint32_t H = 0x00403F00u;
   const uint32_t ws[4] = {raw.x, raw.y, raw.z, raw.w};
 #pragma unroll
   for (int w = 0; w < 4; ++w) {
@@ -120,279 +121,75 @@ __host__ __device__ __forceinline__ int64_t btile_off(int c, int kk) {
   return ((c >> 3) * 8 + (kk >> 3)) * 64 + (c & 7) * 8 + (kk & 7);
 }
 
-template <bool IS_K1>
-__global__ void __launch_bounds__(kThreads, 1) k_tc_op(const __grid_constant__ TcParams p) {
-  extern __shared__ __align__(1024) uint8_t smem[];
-  uint64_t* fullG = reinterpret_cast<uint64_t*>(smem);
-  uint64_t* emptyG = fullG + kRG;
-  uint64_t* fullB = emptyG + kRG;
-  uint64_t* emptyB = fullB + kMaxRB;
-  uint64_t* decoded = emptyB + kMaxRB;
-  uint64_t* emptyA = decoded + kRA;
-  uint64_t* done = emptyA + kRA;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-  uint8_t* gring = smem + kBarrierBytes;
-  uint8_t* bring = gring + kRG * kBlockBytes;
-
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  const EpiParams& e = p.e;
-
-  const int64_t tile = blockIdx.x;
-  const int comp = blockIdx.y;
-  int64_t nch;
-  const uint8_t* gbase;
-  const uint8_t* bbase;
-  if (IS_K1) {
-    nch = p.n_chunks;
-    gbase = p.geno + tile * p.n_chunks * kBlockBytes;
-    bbase = p.bsrc;
-  } else {
-    int64_t p0 = 0, p1 = p.n_panels;
-    if (e.stacked) {
-      p0 = p.comp_slot_start[comp] / kPanel;
-      p1 = p.comp_slot_start[comp + 1] / kPanel;
-    }
-    nch = p1 - p0;
-    gbase = p.geno + (tile * p.n_panels + p0) * kBlockBytes;
-    bbase = p.bsrc + p0 * p.b_chunk_bytes;
-  }
-
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < kRG; ++i) {
-      ptx::mbar_init(&fullG[i], 1);
-      ptx::mbar_init(&emptyG[i], 128);
-    }
-    for (int i = 0; i < kMaxRB; ++i) {
-      ptx::mbar_init(&fullB[i], 1);
-      ptx::mbar_init(&emptyB[i], 1);
-    }
-    for (int i = 0; i < kRA; ++i) {
-      ptx::mbar_init(&decoded[i], 128);
-      ptx::mbar_init(&emptyA[i], 1);
-    }
-    ptx::mbar_init(done, 1);
-    *abort_flag = 0;
-    ptx::fence_barrier_init();
-  }
-  if (warp == kWarpMMA) ptx::tmem_alloc(tmem_slot, p.tmem_cols);
-  ptx::tc_fence_before();
-  __syncthreads();
-  ptx::tc_fence_after();
-  const uint32_t tmem = *tmem_slot;
-
-  if (warp == kWarpG) {
-    // ---------------------------------------------- genotype block producer
-    if (lane == 0) {
-      int64_t issued = 0;
-      for (int64_t c = 0; c < nch; ++c) {
-        const int s = static_cast<int>(c % kRG);
-        const uint32_t u = static_cast<uint32_t>(c / kRG);
-        if (u > 0 && !ptx::mbar_wait(&emptyG[s], (u - 1) & 1, p.err, 11, abort_flag)) break;
-        ptx::mbar_arrive_expect_tx(&fullG[s], kBlockBytes);
-        ptx::bulk_g2s(gring + s * kBlockBytes, gbase + c * kBlockBytes, kBlockBytes, &fullG[s]);
-        issued = c + 1;
-      }
-      if (*abort_flag) {
-        // Let copies still in flight land before the CTA exits.
-        for (int64_t c = (issued > kRG ? issued - kRG : 0); c < issued; ++c) {
-          const int s = static_cast<int>(c % kRG);
-          volatile int no_abort = 0;
-          ptx::mbar_wait(&fullG[s], static_cast<uint32_t>(c / kRG) & 1, p.err, 18, &no_abort);
-        }
-      }
-    }
-  } else if (warp == kWarpB) {
-    // ---------------------------------------------------- B tile producer
-    if (lane == 0) {
-      int64_t issued = 0;
-      for (int64_t c = 0; c < nch; ++c) {
-        const int s = static_cast<int>(c % p.RB);
-        const uint32_t u = static_cast<uint32_t>(c / p.RB);
-        if (u > 0 && !ptx::mbar_wait(&emptyB[s], (u - 1) & 1, p.err, 12, abort_flag)) break;
-        ptx::mbar_arrive_expect_tx(&fullB[s], p.bslot_bytes);
-        ptx::bulk_g2s(bring + static_cast<size_t>(s) * p.bslot_bytes, bbase + c * p.b_chunk_bytes,
-                      p.bslot_bytes, &fullB[s]);
-        issued = c + 1;
-      }
-      if (*abort_flag) {
-        for (int64_t c = (issued > p.RB ? issued - p.RB : 0); c < issued; ++c) {
-          const int s = static_cast<int>(c % p.RB);
-          volatile int no_abort = 0;
-          ptx::mbar_wait(&fullB[s], static_cast<uint32_t>(c / p.RB) & 1, p.err, 19, &no_abort);
-        }
-      }
-    }
-  } else if (warp == kWarpMMA) {
-    // ------------------------------------------------------------ MMA issue
-    if (lane == 0) {
-      const uint32_t idesc = ptx::idesc_bf16_f32(128, e.kp);
-      const uint32_t bring_addr = ptx::smem_addr(bring);
-      int64_t c = 0;
-      for (; c < nch; ++c) {
-        const int as = static_cast<int>(c % kRA);
-        const int bs = static_cast<int>(c % p.RB);
-        if (!ptx::mbar_wait(&decoded[as], static_cast<uint32_t>(c / kRA) & 1, p.err, 13,
-                            abort_flag))
-          break;
-        if (!ptx::mbar_wait(&fullB[bs], static_cast<uint32_t>(c / p.RB) & 1, p.err, 14,
-                            abort_flag))
-          break;
-        ptx::tc_fence_after();
-        const uint32_t bslot = bring_addr + static_cast<uint32_t>(bs) * p.bslot_bytes;
-        const uint32_t a_col = tmem + p.acc_cols + static_cast<uint32_t>(as) * 32u;
+// K1 epilogue for one 16-column chunk of slot j: S = w (T - mu 1^T V + mu vmiss)
+// split into BF16 terms (K2's B tiles), r += mu S; or the X^T V output.
+__device__ __forceinline__ void epilogue_k1(const EpiParams& e, int64_t j, int c0,
+                                            const float (&T)[16], int lane) {
+  const int g = e.comp_of_slot[j];
+  const int gi = e.stacked ? g : 0;
+  const int32_t snp = e.snp_of_slot[j];
+  float wsnp = 1.f;
+  if (e.snpw != nullptr) wsnp = snp >= 0 ? e.snpw[snp] : 0.f;
+  const int64_t pnl = j / kPanel;
+  const int kk = static_cast<int>(j % kPanel);
+  const int g0 = __shfl_sync(0xffffffffu, gi, 0);
+  const bool uniform = __all_sync(0xffffffffu, gi == g0);
+  const int64_t term = static_cast<int64_t>(e.kp) * kPanel;
 #pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-          for (int t = 0; t < e.nsplit; ++t) {
-            const uint64_t bd = ptx::smem_desc(
-                bslot + static_cast<uint32_t>(t * e.kp * 128 + ks * 256), 128u, 1024u);
-            ptx::mma_ts(tmem, a_col + static_cast<uint32_t>(ks * 8), bd, idesc,
-                        (c | ks | t) != 0 ? 1u : 0u);
-          }
-        }
-        ptx::mma_commit(&emptyA[as]);
-        ptx::mma_commit(&emptyB[bs]);
-      }
-      if (nch == 0) {
-        ptx::mbar_arrive(done);
-      } else {
-        ptx::mma_commit(done);
-      }
-      if (*abort_flag) {
-        // Tensor memory is released below: let issued MMAs finish first.
-        volatile int no_abort = 0;
-        ptx::mbar_wait(done, 0, p.err, 20, &no_abort);
-      }
+  for (int i = 0; i < 16; ++i) {
+    const int c = c0 + i;
+    float sval = 0.f, mu = 0.f;
+    if (c < e.k) {
+      const int grp = group_of(e, c);
+      mu = e.gmean[grp][j];
+      const float iv = e.ginv[grp][j];
+      const float w = (e.xtv ? iv : iv * iv) * e.cscale[grp * e.G + g] * wsnp;
+      float corr = mu * e.cs[c];
+      if (e.vmiss != nullptr) corr -= mu * e.vmiss[j * e.kp + c];
+      sval = w * (T[i] - corr);
     }
-  } else {
-    // --------------------------------------------- decoders, then epilogue
-    const int quarter = warp & 3;
-    const int row = quarter * 32 + lane;
-    const uint32_t lane_base = static_cast<uint32_t>(quarter * 32) << 16;
-    bool ok = true;
-    for (int64_t c = 0; c < nch; ++c) {
-      const int gs = static_cast<int>(c % kRG);
-      bool w_ok = ptx::mbar_wait(&fullG[gs], static_cast<uint32_t>(c / kRG) & 1, p.err, 15,
-                                 abort_flag);
-      if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
-      const uint4 raw = *reinterpret_cast<const uint4*>(gring + gs * kBlockBytes + row * kRowBytes);
-      ptx::mbar_arrive(&emptyG[gs]);
-      uint32_t a[32];
-      decode_row(raw, a);
-      const int as = static_cast<int>(c % kRA);
-      if (c >= kRA) {
-        w_ok = ptx::mbar_wait(&emptyA[as], static_cast<uint32_t>(c / kRA - 1) & 1, p.err, 16,
-                              abort_flag);
-        if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
-      }
-      ptx::tc_fence_after();
-      ptx::tmem_st32(tmem + lane_base + p.acc_cols + static_cast<uint32_t>(as) * 32u, a);
-      ptx::tmem_wait_st();
-      ptx::tc_fence_before();
-      ptx::mbar_arrive(&decoded[as]);
+    if (e.xtv) {
+      if (snp >= 0 && c < e.k) e.xout[static_cast<int64_t>(snp) * e.ldo + c] = sval;
+      continue;
     }
-    if (ok) {
-      const bool w_ok = ptx::mbar_wait(done, 0, p.err, 17, abort_flag);
-      ok = __all_sync(0xffffffffu, w_ok);
-    }
-    if (ok) {
-      ptx::tc_fence_after();
-      const int64_t rowid = tile * kTile + row;
-      if (IS_K1) {
-        // ------------------------------------------------ K1 epilogue
-        const int64_t j = rowid;  // slot
-        const int g = e.comp_of_slot[j];
-        const int gi = e.stacked ? g : 0;
-        const int32_t snp = e.snp_of_slot[j];
-        float wsnp = 1.f;
-        if (e.snpw != nullptr) wsnp = snp >= 0 ? e.snpw[snp] : 0.f;
-        const int64_t pnl = j / kPanel;
-        const int kk = static_cast<int>(j % kPanel);
-        const int g0 = __shfl_sync(0xffffffffu, gi, 0);
-        const bool uniform = __all_sync(0xffffffffu, gi == g0);
-        for (int c0 = 0; c0 < e.kp; c0 += 16) {
-          uint32_t r[16];
-          if (nch > 0) {
-            ptx::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(c0), r);
-            ptx::tmem_wait_ld();
-          } else {
+    const int64_t base = pnl * (e.nsplit * term) + btile_off(c, kk);
+    __nv_bfloat16 hi, mid, lo;
+    split3(sval, hi, mid, lo);
+    e.sbuf[base] = hi;
+    if (e.nsplit > 1) e.sbuf[base + term] = mid;
+    if (e.nsplit > 2) e.sbuf[base + 2 * term] = lo;
+    if (c >= e.k) continue;
+    if (e.sf32 != nullptr) e.sf32[j * e.kp + c] = sval;
+    double v = static_cast<double>(mu) * static_cast<double>(sval);
+    if (uniform) {
 #pragma unroll
-            for (int i = 0; i < 16; ++i) r[i] = 0u;
-          }
-#pragma unroll 1
-          for (int i = 0; i < 16; ++i) {
-            const int c = c0 + i;
-            float sval = 0.f, mu = 0.f;
-            if (c < e.k) {
-              const int grp = group_of(e, c);
-              mu = e.gmean[grp][j];
-              const float iv = e.ginv[grp][j];
-              const float w = (e.xtv ? iv : iv * iv) * e.cscale[grp * e.G + g] * wsnp;
-              float corr = mu * e.cs[c];
-              if (e.vmiss != nullptr) corr -= mu * e.vmiss[j * e.kp + c];
-              sval = w * (__uint_as_float(r[i]) - corr);
-            }
-            if (e.xtv) {
-              if (snp >= 0 && c < e.k) e.xout[static_cast<int64_t>(snp) * e.ldo + c] = sval;
-              continue;
-            }
-            const int64_t base = pnl * (static_cast<int64_t>(e.nsplit) * e.kp * kPanel) +
-                                 btile_off(c, kk);
-            __nv_bfloat16 hi, mid, lo;
-            split3(sval, hi, mid, lo);
-            e.sbuf[base] = hi;
-            if (e.nsplit > 1) e.sbuf[base + static_cast<int64_t>(e.kp) * kPanel] = mid;
-            if (e.nsplit > 2) e.sbuf[base + 2 * static_cast<int64_t>(e.kp) * kPanel] = lo;
-            if (c >= e.k) continue;
-            if (e.sf32 != nullptr) e.sf32[j * e.kp + c] = sval;
-            double v = static_cast<double>(mu) * static_cast<double>(sval);
-            if (uniform) {
-#pragma unroll
-              for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-              if (lane == 0) atomicAdd(&e.rbuf[gi * e.kp + c], v);
-            } else {
-              atomicAdd(&e.rbuf[gi * e.kp + c], v);
-            }
-          }
-        }
-      } else {
-        // ------------------------------------------------ K2 epilogue
-        const int64_t i = rowid;  // sample
-        const int gi = e.stacked ? comp : 0;
-        float* outb = e.out + static_cast<int64_t>(gi) * e.n * e.ldo;
-        for (int c0 = 0; c0 < e.kp; c0 += 16) {
-          uint32_t r[16];
-          if (nch > 0) {
-            ptx::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(c0), r);
-            ptx::tmem_wait_ld();
-          } else {
-#pragma unroll
-            for (int t = 0; t < 16; ++t) r[t] = 0u;
-          }
-          if (i >= e.n) continue;
-#pragma unroll 1
-          for (int t = 0; t < 16; ++t) {
-            const int c = c0 + t;
-            if (c >= e.k) break;
-            const int grp = group_of(e, c);
-            float v = __uint_as_float(r[t]) - static_cast<float>(e.rbuf[gi * e.kp + c]);
-            if (e.use_theta_e) v += e.theta_e[grp] * e.V[i * e.ldv + c];
-            if (e.gmask[grp] != nullptr && e.gmask[grp][i] == 0) v = 0.f;
-            outb[i * e.ldo + c] = v;
-          }
-        }
-      }
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      if (lane == 0) atomicAdd(&e.rbuf[gi * e.kp + c], v);
+    } else {
+      atomicAdd(&e.rbuf[gi * e.kp + c], v);
     }
-  }
-
-  ptx::tc_fence_before();
-  __syncthreads();
-  if (warp == kWarpMMA) {
-    ptx::tc_fence_after();
-    ptx::tmem_dealloc(tmem, p.tmem_cols);
   }
 }
+
+// K2 epilogue for one 16-column chunk of sample i: out = acc - r (+ theta_e V), masked.
+__device__ __forceinline__ void epilogue_k2(const EpiParams& e, int64_t i, int comp, int c0,
+                                            const float (&T)[16]) {
+  if (i >= e.n) return;
+  const int gi = e.stacked ? comp : 0;
+  float* outb = e.out + static_cast<int64_t>(gi) * e.n * e.ldo;
+#pragma unroll
+  for (int t = 0; t < 16; ++t) {
+    const int c = c0 + t;
+    if (c >= e.k) break;
+    const int grp = group_of(e, c);
+    float v = T[t] - static_cast<float>(e.rbuf[gi * e.kp + c]);
+    if (e.use_theta_e) v += e.theta_e[grp] * e.V[i * e.ldv + c];
+    if (e.gmask[grp] != nullptr && e.gmask[grp][i] == 0) v = 0.f;
+    outb[i * e.ldo + c] = v;
+  }
+}
+
+#include "tc_kernel.cuh"
 
 // ------------------------------------------------------------ helper kernels
 
@@ -599,23 +396,30 @@ static int fill_epi(coherit_geno* h, const OpDesc& d, int kp, int nsplit, EpiPar
 }
 
 struct TcLaunchCfg {
-  int RB;
+  int RB, RA;
+  bool side;
   uint32_t bslot;
   uint32_t tmem_cols, acc_cols;
   size_t smem;
 };
 
+// Accumulator: NSPLIT*kp columns when the split terms sit side by side in N
+// (one MMA per K step, N <= 256), kp columns otherwise.  The A ring takes the
+// remaining tensor-memory columns (4..8 slots of 32).
 static TcLaunchCfg tc_config(int kp, int nsplit) {
   TcLaunchCfg c;
-  c.acc_cols = static_cast<uint32_t>(round_up(kp, 32));
-  uint32_t need = c.acc_cols + kRA * 32;
+  c.side = nsplit > 1 && nsplit * kp <= 256;
+  const int acc = c.side ? nsplit * kp : kp;
+  c.acc_cols = static_cast<uint32_t>(round_up(acc, 32));
+  const uint32_t need = c.acc_cols + 4 * 32;
   uint32_t cols = 32;
   while (cols < need) cols <<= 1;
   c.tmem_cols = cols;
+  c.RA = std::min<int>(kMaxRA, static_cast<int>((cols - c.acc_cols) / 32));
   c.bslot = static_cast<uint32_t>(nsplit) * kp * kPanel * 2;
   const size_t fixed = kBarrierBytes + kRG * kBlockBytes;
   const int ctas_tmem = 512 / static_cast<int>(cols);
-  const size_t target = ctas_tmem >= 2 ? 100 * 1024 : 200 * 1024;
+  const size_t target = ctas_tmem >= 2 ? 112 * 1024 : 220 * 1024;
   int rb = static_cast<int>((target - fixed) / c.bslot);
   rb = std::max(2, std::min(kMaxRB, rb));
   c.RB = rb;
@@ -625,6 +429,21 @@ static TcLaunchCfg tc_config(int kp, int nsplit) {
   const size_t sm_bytes = 228 * 1024;
   while (static_cast<int>(sm_bytes / (c.smem + 1024)) > ctas_tmem) c.smem += 4096;
   return c;
+}
+
+template <bool IS_K1>
+static int launch_tc(int nsplit, bool side, dim3 grid, size_t smem, cudaStream_t st,
+                     const TcParams& p) {
+  auto go = [&](auto kern) -> int {
+    CO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem)));
+    kern<<<grid, kThreads, smem, st>>>(p); note_launch();
+    CO_CUDA(cudaGetLastError());
+    return COHERIT_OK;
+  };
+  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false>);
+  if (nsplit == 2) return side ? go(k_tc_op<IS_K1, 2, true>) : go(k_tc_op<IS_K1, 2, false>);
+  return side ? go(k_tc_op<IS_K1, 3, true>) : go(k_tc_op<IS_K1, 3, false>);
 }
 
 int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
@@ -675,6 +494,7 @@ int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
   TcParams p;
   memset(&p, 0, sizeof(p));
   p.RB = cfg.RB;
+  p.RA = cfg.RA;
   p.bslot_bytes = cfg.bslot;
   p.tmem_cols = cfg.tmem_cols;
   p.acc_cols = cfg.acc_cols;
@@ -687,38 +507,36 @@ int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
     const int prep_smem = kPanel * (kp + 1) * static_cast<int>(sizeof(float));
     CO_CUDA(cudaFuncSetAttribute(k_prep_v, cudaFuncAttributeMaxDynamicSharedMemorySize, prep_smem));
     k_prep_v<<<static_cast<unsigned>(h->n_chunks), 256, prep_smem, st>>>(
-        d.V, d.ldv, h->n, d.k, kp, nsplit, vt, cs_part, e);
-    k_colsum_finish<<<(kp + 127) / 128, 128, 0, st>>>(cs_part, h->n_chunks, kp, cs);
+        d.V, d.ldv, h->n, d.k, kp, nsplit, vt, cs_part, e); note_launch();
+    k_colsum_finish<<<(kp + 127) / 128, 128, 0, st>>>(cs_part, h->n_chunks, kp, cs); note_launch();
     if (vmiss != nullptr)
       k_vmiss<<<static_cast<unsigned>((h->m_pad + 7) / 8), 256, 0, st>>>(
-          h->d_csc_off, h->d_csc_idx, h->m_pad, d.V, d.ldv, h->n, d.k, kp, vmiss, e);
+          h->d_csc_off, h->d_csc_idx, h->m_pad, d.V, d.ldv, h->n, d.k, kp, vmiss, e); note_launch();
     CO_CUDA(cudaGetLastError());
     p.geno = h->geno_t;
     p.bsrc = reinterpret_cast<const uint8_t*>(vt);
     p.e = e;
-    CO_CUDA(cudaFuncSetAttribute(k_tc_op<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(cfg.smem)));
-    k_tc_op<true><<<dim3(static_cast<unsigned>(h->n_ttiles), 1), kThreads, cfg.smem, st>>>(p);
-    CO_CUDA(cudaGetLastError());
+    rc = launch_tc<true>(nsplit, cfg.side, dim3(static_cast<unsigned>(h->n_ttiles), 1), cfg.smem,
+                         st, p);
+    if (rc != COHERIT_OK) return rc;
     if (d.xtv) return COHERIT_OK;
   } else {
     // Z b: S = inv_sd * b computed directly.
     CO_CHECK(h->n_missing == 0 || sf32 != nullptr, COHERIT_E_SHAPE, "workspace missing");
-    k_prep_s_from_b<<<static_cast<unsigned>((h->m_pad + 127) / 128), 128, 0, st>>>(d.V, d.ldv, e);
+    k_prep_s_from_b<<<static_cast<unsigned>((h->m_pad + 127) / 128), 128, 0, st>>>(d.V, d.ldv, e); note_launch();
     CO_CUDA(cudaGetLastError());
   }
   p.geno = h->geno_s;
   p.bsrc = reinterpret_cast<const uint8_t*>(sbuf);
   p.comp_slot_start = h->d_comp_slot_start;
   p.e = e;
-  CO_CUDA(cudaFuncSetAttribute(k_tc_op<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               static_cast<int>(cfg.smem)));
-  k_tc_op<false><<<dim3(static_cast<unsigned>(h->n_stiles), static_cast<unsigned>(nr)), kThreads,
-                   cfg.smem, st>>>(p);
-  CO_CUDA(cudaGetLastError());
+  rc = launch_tc<false>(nsplit, cfg.side,
+                        dim3(static_cast<unsigned>(h->n_stiles), static_cast<unsigned>(nr)),
+                        cfg.smem, st, p);
+  if (rc != COHERIT_OK) return rc;
   if (sf32 != nullptr) {
     k_rowcorr<<<static_cast<unsigned>((h->n + 7) / 8), 256, 0, st>>>(h->d_csr_off, h->d_csr_idx,
-                                                                      h->n, e);
+                                                                      h->n, e); note_launch();
     CO_CUDA(cudaGetLastError());
   }
   return COHERIT_OK;

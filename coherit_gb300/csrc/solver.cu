@@ -203,7 +203,7 @@ int coherit_colreduce(int32_t op, int64_t n, int32_t k, const float* A, int64_t 
   int64_t gx = (n + 63) / 64;
   if (gx > 1024) gx = 1024;
   dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>((k + kRedCols - 1) / kRedCols));
-  k_colreduce<<<grid, kRedThreads, 0, st>>>(op, n, k, A, lda, B, ldb, out);
+  k_colreduce<<<grid, kRedThreads, 0, st>>>(op, n, k, A, lda, B, ldb, out); note_launch();
   CO_CUDA(cudaGetLastError());
   return COHERIT_OK;
 }
@@ -215,7 +215,7 @@ int coherit_pcg_state_update(int64_t n, int32_t k, float* X, int64_t ldx, float*
   CO_CHECK(k >= 1 && k <= 8192, COHERIT_E_SHAPE, "k=%d outside [1, 8192]", k);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   k_pcg_state<<<elem_grid(n * k), 256, sizeof(float) * k, st>>>(n, k, X, ldx, R, ldr, P, ldp, AP,
-                                                                ldap, rs, denom, active, breakdown);
+                                                                ldap, rs, denom, active, breakdown); note_launch();
   CO_CUDA(cudaGetLastError());
   return COHERIT_OK;
 }
@@ -227,9 +227,9 @@ int coherit_pcg_direction_update(int64_t n, int32_t k, float* P, int64_t ldp, co
   CO_CHECK(k >= 1 && k <= 4096, COHERIT_E_SHAPE, "k=%d outside [1, 4096]", k);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   k_pcg_dir<<<elem_grid(n * k), 256, 2 * sizeof(float) * k, st>>>(n, k, P, ldp, Z, ldz, rs_new,
-                                                                  rnorm2, rs_old, threshold);
+                                                                  rnorm2, rs_old, threshold); note_launch();
   k_pcg_dir_scalars<<<(k + 127) / 128, 128, 0, st>>>(k, rs_new, rnorm2, rs_old, threshold, active,
-                                                     rnorm_out);
+                                                     rnorm_out); note_launch();
   CO_CUDA(cudaGetLastError());
   return COHERIT_OK;
 }
@@ -245,7 +245,7 @@ int coherit_selftest_mma(int32_t variant, float* out_host, void* stream) {
   CO_CUDA(cudaMalloc(&d_err, sizeof(int)));
   cudaMemsetAsync(d_out, 0xFF, sizeof(float) * 128 * 16, st);
   cudaMemsetAsync(d_err, 0, sizeof(int), st);
-  k_probe_mma<<<1, 128, 0, st>>>(variant, d_out, d_err);
+  k_probe_mma<<<1, 128, 0, st>>>(variant, d_out, d_err); note_launch();
   cudaError_t e = cudaGetLastError();
   int err = 0;
   if (e == cudaSuccess)

@@ -1,0 +1,246 @@
+// tc_kernel.cuh -- the tcgen05 mainloop + epilogues of the genotype operator.
+//
+// One CTA owns a 128-row tile (K1: 128 SNP slots, K2: 128 samples) and walks
+// K in chunks of 64 (K1: samples, K2: SNP slots).  Per chunk:
+//   warp 0   bulk-copies the 2 KB genotype block into a 24-deep shared ring;
+//   warp 2   bulk-copies the B tile (all split terms of V or S for these 64
+//            K values) into a shared ring;
+//   warps 3.. decode in kSets sets of 4 warps (one per tensor-memory lane
+//            quarter); a set turns the 16-byte rows (64 codes) of one chunk
+//            into 32 BF16 pairs per row stored with tcgen05.st into an A ring
+//            in tensor memory, and the sets take successive chunks so that
+//            several store round trips are in flight;
+//   warp 1   lane 0 issues the MMAs.  With SIDE the split terms sit side by
+//            side in N (one MMA of N = NSPLIT*kp per 16-wide K step, the
+//            epilogue sums the column groups); otherwise each term is its own
+//            MMA into one accumulator.
+// Barrier arrivals from the decoders are per warp.  All waits are bounded.
+
+template <bool IS_K1, int NSPLIT, bool SIDE>
+__global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ TcParams p) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint64_t* fullG = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* emptyG = fullG + kRG;
+  uint64_t* fullB = emptyG + kRG;
+  uint64_t* emptyB = fullB + kMaxRB;
+  uint64_t* decoded = emptyB + kMaxRB;
+  uint64_t* emptyA = decoded + kMaxRA;
+  uint64_t* done = emptyA + kMaxRA;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  uint8_t* gring = smem + kBarrierBytes;
+  uint8_t* bring = gring + kRG * kBlockBytes;
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const EpiParams& e = p.e;
+  const int kp = e.kp;
+  const int RA = p.RA;
+  const int RB = p.RB;
+
+  const int64_t tile = blockIdx.x;
+  const int comp = blockIdx.y;
+  int64_t nch;
+  const uint8_t* gbase;
+  const uint8_t* bbase;
+  if (IS_K1) {
+    nch = p.n_chunks;
+    gbase = p.geno + tile * p.n_chunks * kBlockBytes;
+    bbase = p.bsrc;
+  } else {
+    int64_t p0 = 0, p1 = p.n_panels;
+    if (e.stacked) {
+      p0 = p.comp_slot_start[comp] / kPanel;
+      p1 = p.comp_slot_start[comp + 1] / kPanel;
+    }
+    nch = p1 - p0;
+    gbase = p.geno + (tile * p.n_panels + p0) * kBlockBytes;
+    bbase = p.bsrc + p0 * p.b_chunk_bytes;
+  }
+
+  if (threadIdx.x == 0) {
+    // Each chunk is consumed and decoded by one set of 4 warps.
+    for (int i = 0; i < kRG; ++i) {
+      ptx::mbar_init(&fullG[i], 1);
+      ptx::mbar_init(&emptyG[i], 4);
+    }
+    for (int i = 0; i < kMaxRB; ++i) {
+      ptx::mbar_init(&fullB[i], 1);
+      ptx::mbar_init(&emptyB[i], 1);
+    }
+    for (int i = 0; i < kMaxRA; ++i) {
+      ptx::mbar_init(&decoded[i], 4);
+      ptx::mbar_init(&emptyA[i], 1);
+    }
+    ptx::mbar_init(done, 1);
+    *abort_flag = 0;
+    ptx::fence_barrier_init();
+  }
+  if (warp == kWarpMMA) ptx::tmem_alloc(tmem_slot, p.tmem_cols);
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == kWarpG) {
+    // ---------------------------------------------- genotype block producer
+    if (lane == 0) {
+      int64_t issued = 0;
+      for (int64_t c = 0; c < nch; ++c) {
+        const int s = static_cast<int>(c % kRG);
+        const uint32_t u = static_cast<uint32_t>(c / kRG);
+        if (u > 0 && !ptx::mbar_wait(&emptyG[s], (u - 1) & 1, p.err, 11, abort_flag)) break;
+        ptx::mbar_arrive_expect_tx(&fullG[s], kBlockBytes);
+        ptx::bulk_g2s(gring + s * kBlockBytes, gbase + c * kBlockBytes, kBlockBytes, &fullG[s]);
+        issued = c + 1;
+      }
+      if (*abort_flag) {
+        // Let copies still in flight land before the CTA exits.
+        for (int64_t c = (issued > kRG ? issued - kRG : 0); c < issued; ++c) {
+          volatile int no_abort = 0;
+          ptx::mbar_wait(&fullG[c % kRG], static_cast<uint32_t>(c / kRG) & 1, p.err, 18,
+                         &no_abort);
+        }
+      }
+    }
+  } else if (warp == kWarpB) {
+    // ---------------------------------------------------- B tile producer
+    if (lane == 0) {
+      int64_t issued = 0;
+      for (int64_t c = 0; c < nch; ++c) {
+        const int s = static_cast<int>(c % RB);
+        const uint32_t u = static_cast<uint32_t>(c / RB);
+        if (u > 0 && !ptx::mbar_wait(&emptyB[s], (u - 1) & 1, p.err, 12, abort_flag)) break;
+        ptx::mbar_arrive_expect_tx(&fullB[s], p.bslot_bytes);
+        ptx::bulk_g2s(bring + static_cast<size_t>(s) * p.bslot_bytes, bbase + c * p.b_chunk_bytes,
+                      p.bslot_bytes, &fullB[s]);
+        issued = c + 1;
+      }
+      if (*abort_flag) {
+        for (int64_t c = (issued > RB ? issued - RB : 0); c < issued; ++c) {
+          volatile int no_abort = 0;
+          ptx::mbar_wait(&fullB[c % RB], static_cast<uint32_t>(c / RB) & 1, p.err, 19, &no_abort);
+        }
+      }
+    }
+  } else if (warp == kWarpMMA) {
+    // ------------------------------------------------------------ MMA issue
+    if (lane == 0) {
+      const uint32_t idesc = ptx::idesc_bf16_f32(128, SIDE ? NSPLIT * kp : kp);
+      const uint64_t bdesc0 = ptx::smem_desc(ptx::smem_addr(bring), 128u, 1024u);
+      const uint32_t term_off = static_cast<uint32_t>(kp * 128) >> 4;
+      for (int64_t c = 0; c < nch; ++c) {
+        const int as = static_cast<int>(c % RA);
+        const int bs = static_cast<int>(c % RB);
+        if (!ptx::mbar_wait(&decoded[as], static_cast<uint32_t>(c / RA) & 1, p.err, 13,
+                            abort_flag))
+          break;
+        if (!ptx::mbar_wait(&fullB[bs], static_cast<uint32_t>(c / RB) & 1, p.err, 14, abort_flag))
+          break;
+        ptx::tc_fence_after();
+        const uint64_t bslot = bdesc0 + ((static_cast<uint64_t>(bs) * p.bslot_bytes) >> 4);
+        const uint32_t a_col = tmem + p.acc_cols + static_cast<uint32_t>(as) * 32u;
+        const uint32_t first = c == 0 ? 0u : 1u;
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+          if (SIDE) {
+            ptx::mma_ts(tmem, a_col + ks * 8, bslot + ks * 16, idesc, ks == 0 ? first : 1u);
+          } else {
+#pragma unroll
+            for (int t = 0; t < NSPLIT; ++t)
+              ptx::mma_ts(tmem, a_col + ks * 8, bslot + ks * 16 + t * term_off, idesc,
+                          (ks == 0 && t == 0) ? first : 1u);
+          }
+        }
+        ptx::mma_commit(&emptyA[as]);
+        ptx::mma_commit(&emptyB[bs]);
+      }
+      if (nch == 0) {
+        ptx::mbar_arrive(done);
+      } else {
+        ptx::mma_commit(done);
+      }
+      if (*abort_flag) {
+        // Tensor memory is released below: let issued MMAs finish first.
+        volatile int no_abort = 0;
+        ptx::mbar_wait(done, 0, p.err, 20, &no_abort);
+      }
+    }
+  } else {
+    // --------------------------------------------- decoders, then epilogue
+    // Decoder warp sets: set s handles chunks s, s + kSets, ...; within a set
+    // the 4 warps cover the 4 tensor-memory lane quarters (128 rows).
+    const int dw = warp - kWarpDec0;
+    const int quarter = warp & 3;
+    const int set = dw >> 2;
+    const int row = quarter * 32 + lane;
+    const uint32_t lane_base = static_cast<uint32_t>(quarter * 32) << 16;
+    bool ok = true;
+    for (int64_t c = set; c < nch; c += kSets) {
+      const int gs = static_cast<int>(c % kRG);
+      bool w_ok = ptx::mbar_wait(&fullG[gs], static_cast<uint32_t>(c / kRG) & 1, p.err, 15,
+                                 abort_flag);
+      if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
+      const uint4 raw = *reinterpret_cast<const uint4*>(gring + gs * kBlockBytes + row * kRowBytes);
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&emptyG[gs]);
+      uint32_t a[32];
+      decode_row(raw, a);
+      const int as = static_cast<int>(c % RA);
+      if (c >= RA) {
+        w_ok = ptx::mbar_wait(&emptyA[as], static_cast<uint32_t>(c / RA - 1) & 1, p.err, 16,
+                              abort_flag);
+        if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
+      }
+      ptx::tc_fence_after();
+      ptx::tmem_st32(tmem + lane_base + p.acc_cols + static_cast<uint32_t>(as) * 32u, a);
+      ptx::tmem_wait_st();
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&decoded[as]);
+    }
+    if (ok) {
+      const bool w_ok = ptx::mbar_wait(done, 0, p.err, 17, abort_flag);
+      ok = __all_sync(0xffffffffu, w_ok);
+    }
+    if (ok) {
+      ptx::tc_fence_after();
+      const int64_t rowid = tile * kTile + row;
+      // Column chunks of 16 rotate over the kSets warps of a quarter.
+      for (int c0 = 16 * set; c0 < kp; c0 += 16 * kSets) {
+        float T[16];
+        if (nch > 0) {
+          uint32_t r[16];
+          ptx::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(c0), r);
+          ptx::tmem_wait_ld();
+#pragma unroll
+          for (int i = 0; i < 16; ++i) T[i] = __uint_as_float(r[i]);
+          if (SIDE) {
+#pragma unroll
+            for (int t = 1; t < NSPLIT; ++t) {
+              ptx::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(t * kp + c0), r);
+              ptx::tmem_wait_ld();
+#pragma unroll
+              for (int i = 0; i < 16; ++i) T[i] += __uint_as_float(r[i]);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) T[i] = 0.f;
+        }
+        if (IS_K1) {
+          epilogue_k1(e, rowid, c0, T, lane);
+        } else {
+          epilogue_k2(e, rowid, comp, c0, T);
+        }
+      }
+    }
+  }
+
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == kWarpMMA) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, p.tmem_cols);
+  }
+}

@@ -305,6 +305,9 @@ class GenoBlockStreamer:
         )
         self._has_sparse_backend = False
         self._exact_diag_dev = None
+        # Operator applications issued through this streamer (count, total
+        # right-hand-side columns), used to scale per-application costs.
+        self.op_stats = {"apps": 0, "cols": 0}
 
     # ------------------------------------------------------------ building
     def _pack_from_source(self, source) -> np.ndarray:
@@ -459,6 +462,8 @@ class GenoBlockStreamer:
             out = torch.empty((self.n, k), dtype=torch.float32, device=self.dev)
         if k == 0:
             return out
+        self.op_stats["apps"] += 1
+        self.op_stats["cols"] += k
         cs = np.ascontiguousarray(comp_scale, dtype=np.float32)
         if cs.size != G:
             raise ValueError(f"expected {G} component scales, got {cs.size}")

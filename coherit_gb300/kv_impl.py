@@ -1,0 +1,329 @@
+"""Streaming-driver entry points with the signatures of GPU_REML's kv_impl.py.
+
+The reference drives one jitted kernel per call block and streams each
+packed block from the host (kv_impl.py:268-1339).  Here the genotypes are
+resident in HBM; when ``pop_block`` / ``streamers`` are this package's
+``GenoBlockStreamer`` objects the functions dispatch straight to the
+resident operator (one or two kernel launches per application).  Any other
+``pop_block`` callable is honoured too: its blocks and the given per-call
+statistics are uploaded once into a transient resident matrix, so callers
+that build blocks themselves keep working.
+
+Mathematical contract (kv_impl.py:9-12):
+    out = (1/eff_m) * sum_c Z_c (Z_c^T V)
+with Z_c the mean-imputed, centred, 1/sd-scaled genotypes of call c.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Callable, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geno_stream import GenoBlockStreamer, as_rhs
+
+
+def _owner(pop_block) -> GenoBlockStreamer | None:
+    owner = getattr(pop_block, "__self__", None)
+    return owner if isinstance(owner, GenoBlockStreamer) else None
+
+
+def _flat_stats(true_widths, means_by_call, inv_by_call):
+    tw = np.asarray(torch.as_tensor(true_widths).cpu(), dtype=np.int64).reshape(-1)
+    mb = np.asarray(torch.as_tensor(means_by_call).cpu(), dtype=np.float32)
+    ib = np.asarray(torch.as_tensor(inv_by_call).cpu(), dtype=np.float32)
+    mean = np.concatenate([mb[c, : tw[c]] for c in range(tw.size)]) if tw.size else np.zeros(0, np.float32)
+    inv = np.concatenate([ib[c, : tw[c]] for c in range(tw.size)]) if tw.size else np.zeros(0, np.float32)
+    return tw, np.ascontiguousarray(mean), np.ascontiguousarray(inv)
+
+
+class _TransientGeno:
+    """Resident copy of caller-supplied packed blocks with given statistics."""
+
+    def __init__(self, n, n_calls, pop_block, true_widths, means_by_call, inv_by_call, device):
+        self.lib = _lib.load()
+        tw, mean, inv = _flat_stats(true_widths, means_by_call, inv_by_call)
+        blocks = []
+        for c in range(n_calls):
+            blk = np.ascontiguousarray(np.asarray(pop_block(c), dtype=np.uint8))
+            pw = (int(tw[c]) + 3) // 4
+            if blk.shape != (n, pw):
+                raise ValueError(f"pop_block({c}) returned {blk.shape}, expected {(n, pw)}")
+            blocks.append(blk.reshape(-1))
+        packed = np.ascontiguousarray(np.concatenate(blocks))
+        widths = tw.astype(np.int32)
+        self.h = C.c_void_p()
+        self.n = n
+        self.m = int(tw.sum())
+        self.dev = device
+        stream = _lib.stream_ptr()
+        _lib.check(self.lib.coherit_geno_create_packed(
+            packed.ctypes.data, n, n_calls, widths.ctypes.data, None, 1, 0, device.index, stream,
+            C.byref(self.h)), "transient genotypes")
+        _lib.check(self.lib.coherit_geno_set_stats(
+            self.h, 0, None, mean.ctypes.data, inv.ctypes.data, stream), "transient stats")
+
+    def kv(self, V, scale, snp_weight=None, precision=_lib.PREC_BF16X3):
+        V2, squeeze = as_rhs(V, self.dev)
+        k = V2.shape[1]
+        out = torch.empty_like(V2)
+        cs = np.asarray([scale], np.float32)
+        sw = None if snp_weight is None else torch.as_tensor(snp_weight, dtype=torch.float32,
+                                                            device=self.dev).contiguous()
+        _lib.check(self.lib.coherit_geno_kv(
+            self.h, 0, _lib.MODE_SUM, precision, V2.data_ptr(), k, k, cs.ctypes.data, 0, 0.0,
+            _lib.ptr(sw), out.data_ptr(), k, _lib.stream_ptr()), "kv")
+        return out[:, 0] if squeeze else out
+
+    def xtv(self, V, scale, precision=_lib.PREC_BF16X3):
+        V2, squeeze = as_rhs(V, self.dev)
+        k = V2.shape[1]
+        out = torch.empty((self.m, k), dtype=torch.float32, device=self.dev)
+        cs = np.asarray([scale], np.float32)
+        _lib.check(self.lib.coherit_geno_xtv(
+            self.h, 0, precision, V2.data_ptr(), k, k, cs.ctypes.data, out.data_ptr(), k,
+            _lib.stream_ptr()), "xtv")
+        return out[:, 0] if squeeze else out
+
+    def zxb(self, b, precision=_lib.PREC_BF16X3):
+        b = torch.as_tensor(b, dtype=torch.float32, device=self.dev)
+        squeeze = b.ndim == 1
+        b2 = (b[:, None] if squeeze else b).contiguous()
+        Cc = b2.shape[1]
+        out = torch.empty((self.n, Cc), dtype=torch.float32, device=self.dev)
+        _lib.check(self.lib.coherit_geno_zxb(
+            self.h, 0, precision, b2.data_ptr(), Cc, Cc, out.data_ptr(), Cc, _lib.stream_ptr()),
+            "zxb")
+        return out[:, 0] if squeeze else out
+
+    def close(self):
+        if self.h:
+            self.lib.coherit_geno_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _device(V) -> torch.device:
+    if isinstance(V, torch.Tensor) and V.is_cuda:
+        return V.device
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _eff(eff_m) -> float:
+    return float(torch.as_tensor(eff_m).reshape(()).item())
+
+
+def kv_impl_streamed(V, true_widths, means_by_call, inv_by_call, eff_m, *, n: int, n_calls: int,
+                     pop_block: Callable[[int], np.ndarray], missing_val: int = 3,
+                     normalize: bool = True):
+    """K V over all call blocks (kv_impl.py:268-326)."""
+    if int(missing_val) != 3:
+        raise ValueError("packed genotypes use code 3 for missing values")
+    eff = _eff(eff_m)
+    scale = (1.0 / eff) if (normalize and eff > 0) else 1.0
+    st = _owner(pop_block)
+    if st is not None and means_by_call is st._means_by_call and inv_by_call is st._inv_by_call:
+        return st._kv_raw(V, comp_scale=np.full(st.n_components, scale))
+    if n_calls == 0:
+        V2, squeeze = as_rhs(V, _device(V))
+        out = torch.zeros_like(V2)
+        return out[:, 0] if squeeze else out
+    tg = _TransientGeno(n, n_calls, pop_block, true_widths, means_by_call, inv_by_call, _device(V))
+    try:
+        return tg.kv(V, scale)
+    finally:
+        tg.close()
+
+
+def kv_impl_snp_weighted_streamed(V, true_widths, means_by_call, inv_by_call, weights_by_call,
+                                  denom, *, n: int, n_calls: int, pop_block, missing_val: int = 3):
+    """Z diag(w) Z^T V / denom for per-SNP weights (kv_impl.py:329-379)."""
+    tw, _, _ = _flat_stats(true_widths, means_by_call, inv_by_call)
+    wb = np.asarray(torch.as_tensor(weights_by_call).cpu(), dtype=np.float32)
+    w = np.concatenate([wb[c, : tw[c]] for c in range(tw.size)]) if tw.size else np.zeros(0, np.float32)
+    d = float(torch.as_tensor(denom).reshape(()).item())
+    st = _owner(pop_block)
+    if st is not None and means_by_call is st._means_by_call and inv_by_call is st._inv_by_call:
+        return st.snp_weighted_kv(V, w, d)
+    tg = _TransientGeno(n, n_calls, pop_block, true_widths, means_by_call, inv_by_call, _device(V))
+    try:
+        return tg.kv(V, 1.0 / d, snp_weight=w)
+    finally:
+        tg.close()
+
+
+def xtv_impl_streamed(V, m: int, snp_starts, true_widths, means_by_call, inv_by_call, *,
+                      n_calls: int, pop_block, missing_val: int = 3, normalize: bool = False,
+                      eff_m=None):
+    """X^T V = inv_sd * diff^T V, shape (m, k) (kv_impl.py:382-439)."""
+    if normalize and eff_m is None:
+        raise ValueError("xtv_impl_streamed(normalize=True) requires eff_m.")
+    scale = 1.0
+    if normalize:
+        eff = _eff(eff_m)
+        scale = 1.0 / eff if eff > 0 else 1.0
+    st = _owner(pop_block)
+    if st is not None and means_by_call is st._means_by_call and inv_by_call is st._inv_by_call:
+        out = st.xtv(V, normalize=False)
+        return out * scale if scale != 1.0 else out
+    n = as_rhs(V, _device(V))[0].shape[0]
+    tg = _TransientGeno(n, n_calls, pop_block, true_widths, means_by_call, inv_by_call, _device(V))
+    try:
+        return tg.xtv(V, scale)
+    finally:
+        tg.close()
+
+
+def xtv_impl_multi_streamed(V, streamers: Sequence[GenoBlockStreamer], call_plan, *,
+                            missing_val: int = 3, normalize: bool = False):
+    """Per-streamer X^T V (kv_impl.py:442-497)."""
+    if not streamers:
+        raise ValueError("xtv_impl_multi_streamed requires at least one streamer.")
+    return tuple(st.xtv(V, normalize=normalize) for st in streamers)
+
+
+def xtv_impl_multi_streamed_concat(V, streamers, call_plan, *, missing_val: int = 3,
+                                   normalize: bool = False):
+    parts = xtv_impl_multi_streamed(V, streamers, call_plan, missing_val=missing_val,
+                                    normalize=normalize)
+    return parts[0] if len(parts) == 1 else torch.cat(parts, dim=0)
+
+
+def zxb_impl_streamed(b_by_call, true_widths, means_by_call, inv_by_call, *, n: int, n_calls: int,
+                      pop_block, missing_val: int = 3, component_ids=None, n_components: int = 0):
+    """Test prediction g = Z b, total and per component (kv_impl.py:524-602)."""
+    bb = torch.as_tensor(b_by_call)
+    if bb.ndim != 2:
+        raise ValueError("zxb_impl_streamed expects b_by_call with shape (n_calls, max_unpack_width).")
+    if bb.shape[0] != int(n_calls):
+        raise ValueError(
+            f"zxb_impl_streamed b_by_call row mismatch: expected n_calls={int(n_calls)}, "
+            f"got {int(bb.shape[0])}.")
+    tw, _, _ = _flat_stats(true_widths, means_by_call, inv_by_call)
+    if component_ids is not None:
+        component_ids = np.asarray(component_ids, dtype=np.int32).reshape(-1)
+        if component_ids.shape[0] != int(n_calls):
+            raise ValueError(
+                f"zxb_impl_streamed component_ids must have shape ({int(n_calls)},), "
+                f"got {component_ids.shape}.")
+        if int(n_components) <= 0:
+            raise ValueError("zxb_impl_streamed requires n_components > 0 when component_ids is provided.")
+        if np.any(component_ids < 0) or np.any(component_ids >= int(n_components)):
+            raise ValueError(
+                f"zxb_impl_streamed component_ids entries must lie in [0, {int(n_components)}).")
+    dev = bb.device if bb.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    bbc = bb.to(dev, torch.float32)
+    flat = torch.cat([bbc[c, : int(tw[c])] for c in range(int(n_calls))]) if n_calls else \
+        torch.zeros(0, device=dev)
+    st = _owner(pop_block)
+    runner = st if (st is not None and means_by_call is st._means_by_call
+                    and inv_by_call is st._inv_by_call) else None
+    tg = None
+    if runner is None:
+        tg = _TransientGeno(n, n_calls, pop_block, true_widths, means_by_call, inv_by_call, dev)
+        runner = tg
+    try:
+        if component_ids is None:
+            total = runner.zxb(flat)
+            return total, tuple(torch.zeros(n, device=dev) for _ in range(int(n_components)))
+        starts = np.concatenate([[0], np.cumsum(tw)])
+        B = torch.zeros((flat.shape[0], int(n_components)), device=dev)
+        for c in range(int(n_calls)):
+            B[starts[c]: starts[c + 1], int(component_ids[c])] = flat[starts[c]: starts[c + 1]]
+        comps = runner.zxb(B)
+        return comps.sum(dim=1), tuple(comps[:, g] for g in range(int(n_components)))
+    finally:
+        if tg is not None:
+            tg.close()
+
+
+def kv_impl_multi_streamed_weighted(V, streamers: Sequence[GenoBlockStreamer], call_plan, theta_g,
+                                    *, theta_e=None, missing_val: int = 3):
+    """sum_g theta_g K_g V (+ theta_e V) over several streamers (kv_impl.py:911-973)."""
+    if not streamers:
+        raise ValueError("kv_impl_multi_streamed_weighted requires at least one streamer.")
+    tg = np.asarray(torch.as_tensor(theta_g).cpu(), dtype=np.float64).reshape(-1)
+    acc = None
+    for g, st in enumerate(streamers):
+        term = st.weighted_component_hv(np.full(st.n_components, tg[g]),
+                                        theta_e if (g == 0 and theta_e is not None) else None, V)
+        acc = term if acc is None else acc + term
+    return acc
+
+
+def kv_impl_multi_streamed_stacked(V, streamers, call_plan, *, missing_val: int = 3,
+                                  normalize: bool = True):
+    """One K_g V per streamer stacked on axis 0 (kv_impl.py:976-1039)."""
+    if not streamers:
+        raise ValueError("kv_impl_multi_streamed_stacked requires at least one streamer.")
+    return torch.stack([st.kv(V, normalize=normalize) for st in streamers])
+
+
+def kv_impl_partitioned_component(V, streamer: GenoBlockStreamer, *, component_idx: int,
+                                  missing_val: int = 3, normalize: bool = True):
+    """kv_impl.py:1042-1086"""
+    return streamer.component_kv(V, component_idx, normalize=normalize)
+
+
+def kv_impl_partitioned_weighted(V, streamer: GenoBlockStreamer, theta_g, *, theta_e=None,
+                                 missing_val: int = 3):
+    """kv_impl.py:1089-1135"""
+    return streamer.weighted_component_hv(theta_g, theta_e, V)
+
+
+def kv_impl_partitioned_stacked(V, streamer: GenoBlockStreamer, *, missing_val: int = 3,
+                                normalize: bool = True):
+    """kv_impl.py:1138-1187"""
+    return streamer.stacked_component_kv(V, normalize=normalize)
+
+
+def build_projected_core_atom_streamed(U, streamer: GenoBlockStreamer, *, missing_val: int = 3,
+                                       subtract_identity: bool = True):
+    """kv_impl.py:1190-1229"""
+    if torch.as_tensor(U).ndim != 2:
+        raise ValueError("build_projected_core_atom_streamed expects U with shape (n, k).")
+    return streamer.build_projected_core_atom(U, subtract_identity=subtract_identity)
+
+
+def build_projected_core_atoms_multi_streamed(U, streamers, call_plan, *, missing_val: int = 3,
+                                              subtract_identity: bool = True):
+    """kv_impl.py:1232-1285"""
+    if torch.as_tensor(U).ndim != 2:
+        raise ValueError("build_projected_core_atoms_multi_streamed expects U with shape (n, k).")
+    if not streamers:
+        raise ValueError("build_projected_core_atoms_multi_streamed requires at least one streamer.")
+    return torch.stack([st.build_projected_core_atom(U, subtract_identity=subtract_identity)
+                        for st in streamers])
+
+
+def build_projected_core_atoms_partitioned(U, streamer: GenoBlockStreamer, *, missing_val: int = 3,
+                                           subtract_identity: bool = True):
+    """kv_impl.py:1287-1339"""
+    if torch.as_tensor(U).ndim != 2:
+        raise ValueError("build_projected_core_atoms_partitioned expects U with shape (n, k).")
+    return streamer.build_projected_core_atoms(U, subtract_identity=subtract_identity)
+
+
+__all__ = [
+    "kv_impl_streamed",
+    "kv_impl_snp_weighted_streamed",
+    "xtv_impl_streamed",
+    "xtv_impl_multi_streamed",
+    "xtv_impl_multi_streamed_concat",
+    "zxb_impl_streamed",
+    "kv_impl_multi_streamed_weighted",
+    "kv_impl_multi_streamed_stacked",
+    "kv_impl_partitioned_component",
+    "kv_impl_partitioned_weighted",
+    "kv_impl_partitioned_stacked",
+    "build_projected_core_atom_streamed",
+    "build_projected_core_atoms_multi_streamed",
+    "build_projected_core_atoms_partitioned",
+]

@@ -63,6 +63,9 @@ typedef struct coherit_geno coherit_geno_t;
 
 const char* coherit_last_error(void);
 int coherit_version(void);
+/* Number of kernels the library has launched in this process (no counterpart
+ * in the reference; lets callers count device work inside a timed region). */
+int64_t coherit_launch_count(void);
 /* Number of devices and whether device `dev` is a tcgen05-capable part. */
 int coherit_device_info(int dev, int* sm_major, int* sm_minor, int* n_sm, int64_t* hbm_bytes);
 
