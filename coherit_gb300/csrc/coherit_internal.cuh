@@ -2,9 +2,10 @@
 //
 // HBM layout of the resident genotypes (both copies hold every genotype):
 //   * SNP "slots": component g occupies slots [slot_start[g], slot_start[g] +
-//     m_g) followed by zero padding up to a multiple of 64; the total m_pad is
-//     a multiple of 128.  Padding slots have inv_sd = 0 and never contribute.
-//   * samples are padded with genotype code 0 up to n_pad (multiple of 128).
+//     m_g) followed by zero padding up to a multiple of kAlign (128); the
+//     total m_pad is a multiple of kAlign.  Padding slots have inv_sd = 0 and
+//     never contribute.
+//   * samples are padded with genotype code 0 up to n_pad (multiple of kAlign).
 //   * copy S ("sample rows", operand of Z S): 2 KB blocks (sample tile st of
 //     128 samples, panel p of 64 slots) at ((st * n_panels) + p) * 2048; row
 //     i%128 is 16 bytes holding the 64 slots of the panel.
@@ -31,6 +32,13 @@ constexpr int kBlockRows = 128;
 constexpr int kBlockBytes = kRowBytes * kBlockRows;  // 2048
 constexpr int kPanel = 64;                           // slots per panel / samples per chunk
 constexpr int kTile = 128;                           // rows per block
+// Blocks per pipeline stage of the tensor-core operator: components and the
+// sample count are padded to multiples of kStageBlocks * 64 (and of 128).
+#ifndef COHERIT_STAGE_BLOCKS
+#define COHERIT_STAGE_BLOCKS 2
+#endif
+constexpr int kStageBlocks = COHERIT_STAGE_BLOCKS;
+constexpr int kAlign = kPanel * kStageBlocks > kTile ? kPanel * kStageBlocks : kTile;
 
 // -------------------------------------------------------------- status
 void set_error(const char* fmt, ...);
@@ -132,6 +140,8 @@ struct coherit_geno {
   coherit::Workspace ws;
   int* d_err = nullptr;
   int sm_count = 0;
+  int smem_optin = 232448;   // max dynamic shared memory per CTA
+  int smem_per_sm = 233472;  // shared memory per SM
   int64_t device_bytes = 0;
 };
 

@@ -514,12 +514,12 @@ static int alloc_common(coherit_geno* h, int64_t n, const std::vector<int64_t>& 
   h->comp_slot_start.assign(h->G + 1, 0);
   h->comp_snp_start.assign(h->G + 1, 0);
   for (int g = 0; g < h->G; ++g) {
-    h->comp_slot_start[g + 1] = h->comp_slot_start[g] + round_up(comp_m[g], kPanel);
+    h->comp_slot_start[g + 1] = h->comp_slot_start[g] + round_up(comp_m[g], kAlign);
     h->comp_snp_start[g + 1] = h->comp_snp_start[g] + comp_m[g];
   }
   h->m = h->comp_snp_start[h->G];
-  h->m_pad = round_up(std::max<int64_t>(h->comp_slot_start[h->G], 1), kTile);
-  h->n_pad = round_up(std::max<int64_t>(n, 1), kTile);
+  h->m_pad = round_up(std::max<int64_t>(h->comp_slot_start[h->G], 1), kAlign);
+  h->n_pad = round_up(std::max<int64_t>(n, 1), kAlign);
   h->n_panels = h->m_pad / kPanel;
   h->n_chunks = h->n_pad / kPanel;
   h->n_stiles = h->n_pad / kTile;
@@ -529,6 +529,11 @@ static int alloc_common(coherit_geno* h, int64_t n, const std::vector<int64_t>& 
   int sm = 0;
   CO_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device));
   h->sm_count = sm;
+  int v = 0;
+  CO_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+  h->smem_optin = v;
+  CO_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device));
+  h->smem_per_sm = v;
   CO_CUDA(cudaMalloc(&h->geno_s, gbytes));
   CO_CUDA(cudaMalloc(&h->geno_t, gbytes));
   CO_CUDA(cudaMalloc(&h->d_comp_of_slot, sizeof(int32_t) * h->m_pad));

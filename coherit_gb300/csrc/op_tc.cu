@@ -28,11 +28,21 @@
 
 namespace coherit {
 
-constexpr int kSets = 3;        // decoder warp sets (chunks in flight through the A ring)
+#ifndef COHERIT_SETS
+#define COHERIT_SETS 3
+#endif
+#ifndef COHERIT_TMEM_MIN_SLOTS
+#define COHERIT_TMEM_MIN_SLOTS 3
+#endif
+constexpr int kSets = COHERIT_SETS;  // decoder warp sets (stages in flight through the A ring)
 constexpr int kThreads = 32 * (3 + 4 * kSets);
 constexpr int kWarpG = 0, kWarpMMA = 1, kWarpB = 2, kWarpDec0 = 3;
-constexpr int kRG = 24;        // genotype ring depth (2 KB blocks)
-constexpr int kMaxRA = 8;      // tensor-memory A ring depth limit (32 columns each)
+constexpr int kRG = 12;        // genotype ring depth (stages of kStageBlocks 2 KB blocks)
+// Tensor-memory A ring depth limit (slots of 32 * kStageBlocks columns).  Depths
+// up to 6 are the configurations exercised on GB300; a 7-slot ring with a
+// 64-column accumulator raised an illegal-instruction fault whose cause was
+// not found, so the policy never builds one.
+constexpr int kMaxRA = 6;
 constexpr int kMaxRB = 16;     // B ring depth limit
 constexpr int kMaxGroups = 32;
 constexpr int kMaxScale = 256;
@@ -230,13 +240,21 @@ __global__ void k_prep_v(const float* __restrict__ V, int64_t ldv, int64_t n, in
   }
 }
 
-__global__ void k_colsum_finish(const double* __restrict__ cs_part, int64_t n_parts, int kp,
-                                float* __restrict__ cs) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= kp) return;
+// One CTA per column: strided partial sums, then a fixed-order tree (deterministic).
+__global__ void __launch_bounds__(256) k_colsum_finish(const double* __restrict__ cs_part,
+                                                       int64_t n_parts, int kp,
+                                                       float* __restrict__ cs) {
+  __shared__ double red[256];
+  const int c = blockIdx.x;
   double s = 0.0;
-  for (int64_t q = 0; q < n_parts; ++q) s += cs_part[q * kp + c];
-  cs[c] = static_cast<float>(s);
+  for (int64_t q = threadIdx.x; q < n_parts; q += 256) s += cs_part[q * kp + c];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cs[c] = static_cast<float>(red[0]);
 }
 
 // vmiss[j, c] = sum over samples i with a missing genotype at slot j of V[i, c].
@@ -306,7 +324,14 @@ __global__ void k_prep_s_from_b(const float* __restrict__ b, int64_t ldb,
 
 // ------------------------------------------------------------------ launcher
 
-static inline int max_kp_for(int nsplit) { return nsplit >= 3 ? 224 : 256; }
+// Widest right-hand-side block of one launch: two B ring slots (one stage of
+// all split terms each) next to the genotype ring must fit the 227 KB of
+// dynamic shared memory, and N <= 256.
+static inline int max_kp_for(const coherit_geno* h, int nsplit) {
+  const int budget = h->smem_optin - 4096 - kBarrierBytes - kRG * kStageBlocks * kBlockBytes;
+  const int per_col = 2 * kStageBlocks * nsplit * kPanel * 2;
+  return std::min(256, (budget / per_col) / 16 * 16);
+}
 
 struct WsLayout {
   size_t vt, sbuf, cs_part, cs, rbuf, vmiss, sf32, total;
@@ -405,29 +430,33 @@ struct TcLaunchCfg {
 
 // Accumulator: NSPLIT*kp columns when the split terms sit side by side in N
 // (one MMA per K step, N <= 256), kp columns otherwise.  The A ring takes the
-// remaining tensor-memory columns (4..8 slots of 32).
-static TcLaunchCfg tc_config(int kp, int nsplit) {
+// remaining tensor-memory columns (3..8 slots of 32 * kStageBlocks).
+static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
   TcLaunchCfg c;
   c.side = nsplit > 1 && nsplit * kp <= 256;
   const int acc = c.side ? nsplit * kp : kp;
   c.acc_cols = static_cast<uint32_t>(round_up(acc, 32));
-  const uint32_t need = c.acc_cols + 4 * 32;
+  const uint32_t slot_cols = 32u * kStageBlocks;
+  const uint32_t need = c.acc_cols + COHERIT_TMEM_MIN_SLOTS * slot_cols;
   uint32_t cols = 32;
   while (cols < need) cols <<= 1;
   c.tmem_cols = cols;
-  c.RA = std::min<int>(kMaxRA, static_cast<int>((cols - c.acc_cols) / 32));
-  c.bslot = static_cast<uint32_t>(nsplit) * kp * kPanel * 2;
-  const size_t fixed = kBarrierBytes + kRG * kBlockBytes;
+  c.RA = std::min<int>(kMaxRA, static_cast<int>((cols - c.acc_cols) / slot_cols));
+  c.bslot = static_cast<uint32_t>(kStageBlocks) * nsplit * kp * kPanel * 2;
+  const size_t fixed = kBarrierBytes + static_cast<size_t>(kRG) * kStageBlocks * kBlockBytes;
   const int ctas_tmem = 512 / static_cast<int>(cols);
-  const size_t target = ctas_tmem >= 2 ? 112 * 1024 : 220 * 1024;
+  const size_t cap = static_cast<size_t>(h->smem_optin);
+  const size_t target = ctas_tmem >= 2 ? std::min<size_t>(112 * 1024, cap) : cap - 4096;
   int rb = static_cast<int>((target - fixed) / c.bslot);
   rb = std::max(2, std::min(kMaxRB, rb));
+  while (rb > 2 && fixed + static_cast<size_t>(rb) * c.bslot > cap) --rb;
   c.RB = rb;
   c.smem = fixed + static_cast<size_t>(rb) * c.bslot;
   // Never let more CTAs share an SM than its tensor memory can hold: a
   // further CTA would block in tcgen05.alloc.
-  const size_t sm_bytes = 228 * 1024;
-  while (static_cast<int>(sm_bytes / (c.smem + 1024)) > ctas_tmem) c.smem += 4096;
+  const size_t sm_bytes = static_cast<size_t>(h->smem_per_sm);
+  while (static_cast<int>(sm_bytes / (c.smem + 1024)) > ctas_tmem && c.smem + 4096 <= cap)
+    c.smem += 4096;
   return c;
 }
 
@@ -449,7 +478,7 @@ static int launch_tc(int nsplit, bool side, dim3 grid, size_t smem, cudaStream_t
 int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
   if (d.precision == COHERIT_PREC_FP32) return run_operator_fp32(h, d, st);
   const int nsplit = nsplit_of(d.precision);
-  const int kmax = max_kp_for(nsplit);
+  const int kmax = max_kp_for(h, nsplit);
   if (d.k > kmax) {
     // Column blocks: each re-reads the genotypes.
     CO_CHECK(d.n_groups == 1, COHERIT_E_SHAPE,
@@ -490,7 +519,7 @@ int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
   const int nr = e.stacked ? h->G : 1;
   CO_CUDA(cudaMemsetAsync(rbuf, 0, sizeof(double) * nr * kp, st));
 
-  const TcLaunchCfg cfg = tc_config(kp, nsplit);
+  const TcLaunchCfg cfg = tc_config(h, kp, nsplit);
   TcParams p;
   memset(&p, 0, sizeof(p));
   p.RB = cfg.RB;
@@ -508,7 +537,7 @@ int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
     CO_CUDA(cudaFuncSetAttribute(k_prep_v, cudaFuncAttributeMaxDynamicSharedMemorySize, prep_smem));
     k_prep_v<<<static_cast<unsigned>(h->n_chunks), 256, prep_smem, st>>>(
         d.V, d.ldv, h->n, d.k, kp, nsplit, vt, cs_part, e); note_launch();
-    k_colsum_finish<<<(kp + 127) / 128, 128, 0, st>>>(cs_part, h->n_chunks, kp, cs); note_launch();
+    k_colsum_finish<<<kp, 256, 0, st>>>(cs_part, h->n_chunks, kp, cs); note_launch();
     if (vmiss != nullptr)
       k_vmiss<<<static_cast<unsigned>((h->m_pad + 7) / 8), 256, 0, st>>>(
           h->d_csc_off, h->d_csc_idx, h->m_pad, d.V, d.ldv, h->n, d.k, kp, vmiss, e); note_launch();
@@ -570,7 +599,7 @@ int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision) {
   if (precision == COHERIT_PREC_FP32)
     return ensure_ws_bytes(h, static_cast<size_t>(h->m_pad) * kp * sizeof(float));
   const int ns = nsplit_of(precision);
-  return ensure_workspace(h, std::min(kp, max_kp_for(ns)), ns);
+  return ensure_workspace(h, std::min(kp, max_kp_for(h, ns)), ns);
 }
 
 int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t precision,

@@ -1,8 +1,9 @@
 // tc_kernel.cuh -- the tcgen05 mainloop + epilogues of the genotype operator.
 //
 // One CTA owns a 128-row tile (K1: 128 SNP slots, K2: 128 samples) and walks
-// K in chunks of 64 (K1: samples, K2: SNP slots).  Per chunk:
-//   warp 0   bulk-copies the 2 KB genotype block into a 24-deep shared ring;
+// K in stages of kStageBlocks x 64 (K1: samples, K2: SNP slots).  Per stage:
+//   warp 0   bulk-copies the kStageBlocks consecutive 2 KB genotype blocks into
+//            a shared ring;
 //   warp 2   bulk-copies the B tile (all split terms of V or S for these 64
 //            K values) into a shared ring;
 //   warps 3.. decode in kSets sets of 4 warps (one per tensor-memory lane
@@ -17,7 +18,7 @@
 // Barrier arrivals from the decoders are per warp.  All waits are bounded.
 
 template <bool IS_K1, int NSPLIT, bool SIDE>
-__global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ TcParams p) {
+__global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __grid_constant__ TcParams p) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint64_t* fullG = reinterpret_cast<uint64_t*>(smem);
   uint64_t* emptyG = fullG + kRG;
@@ -28,8 +29,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ T
   uint64_t* done = emptyA + kMaxRA;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  constexpr int kStageBytes = kStageBlocks * kBlockBytes;
   uint8_t* gring = smem + kBarrierBytes;
-  uint8_t* bring = gring + kRG * kBlockBytes;
+  uint8_t* bring = gring + kRG * kStageBytes;
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -43,8 +45,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ T
   int64_t nch;
   const uint8_t* gbase;
   const uint8_t* bbase;
+  // nch counts pipeline stages of kStageBlocks consecutive 2 KB blocks.
   if (IS_K1) {
-    nch = p.n_chunks;
+    nch = p.n_chunks / kStageBlocks;
     gbase = p.geno + tile * p.n_chunks * kBlockBytes;
     bbase = p.bsrc;
   } else {
@@ -53,10 +56,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ T
       p0 = p.comp_slot_start[comp] / kPanel;
       p1 = p.comp_slot_start[comp + 1] / kPanel;
     }
-    nch = p1 - p0;
+    nch = (p1 - p0) / kStageBlocks;
     gbase = p.geno + (tile * p.n_panels + p0) * kBlockBytes;
     bbase = p.bsrc + p0 * p.b_chunk_bytes;
   }
+  const int64_t stage_b_bytes = kStageBlocks * p.b_chunk_bytes;
 
   if (threadIdx.x == 0) {
     // Each chunk is consumed and decoded by one set of 4 warps.
@@ -76,6 +80,22 @@ __global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ T
     *abort_flag = 0;
     ptx::fence_barrier_init();
   }
+  // Self-check of the launch configuration: every tensor-memory column the
+  // CTA touches (accumulator + A ring) must lie inside its allocation, and the
+  // rings must fit their barrier arrays; otherwise record an error and exit
+  // before touching tensor memory.
+  {
+    const uint32_t acc_need = SIDE ? static_cast<uint32_t>(NSPLIT * e.kp) : static_cast<uint32_t>(e.kp);
+    const bool cfg_ok = p.RA >= 1 && p.RA <= kMaxRA && p.RB >= 1 && p.RB <= kMaxRB &&
+                        acc_need <= p.acc_cols && (p.acc_cols & 31u) == 0 &&
+                        p.acc_cols + static_cast<uint32_t>(p.RA) * 32u * kStageBlocks <= p.tmem_cols &&
+                        p.tmem_cols >= 32 && p.tmem_cols <= 512 &&
+                        (p.tmem_cols & (p.tmem_cols - 1)) == 0 && acc_need <= 256 && (e.kp & 15) == 0;
+    if (!cfg_ok) {
+      if (threadIdx.x == 0) atomicCAS(p.err, 0, 30);
+      return;
+    }
+  }
   if (warp == kWarpMMA) ptx::tmem_alloc(tmem_slot, p.tmem_cols);
   ptx::tc_fence_before();
   __syncthreads();
@@ -90,8 +110,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ T
         const int s = static_cast<int>(c % kRG);
         const uint32_t u = static_cast<uint32_t>(c / kRG);
         if (u > 0 && !ptx::mbar_wait(&emptyG[s], (u - 1) & 1, p.err, 11, abort_flag)) break;
-        ptx::mbar_arrive_expect_tx(&fullG[s], kBlockBytes);
-        ptx::bulk_g2s(gring + s * kBlockBytes, gbase + c * kBlockBytes, kBlockBytes, &fullG[s]);
+        ptx::mbar_arrive_expect_tx(&fullG[s], kStageBytes);
+        ptx::bulk_g2s(gring + s * kStageBytes, gbase + c * kStageBytes, kStageBytes, &fullG[s]);
         issued = c + 1;
       }
       if (*abort_flag) {
@@ -112,7 +132,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ T
         const uint32_t u = static_cast<uint32_t>(c / RB);
         if (u > 0 && !ptx::mbar_wait(&emptyB[s], (u - 1) & 1, p.err, 12, abort_flag)) break;
         ptx::mbar_arrive_expect_tx(&fullB[s], p.bslot_bytes);
-        ptx::bulk_g2s(bring + static_cast<size_t>(s) * p.bslot_bytes, bbase + c * p.b_chunk_bytes,
+        ptx::bulk_g2s(bring + static_cast<size_t>(s) * p.bslot_bytes, bbase + c * stage_b_bytes,
                       p.bslot_bytes, &fullB[s]);
         issued = c + 1;
       }
@@ -139,17 +159,23 @@ __global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ T
           break;
         ptx::tc_fence_after();
         const uint64_t bslot = bdesc0 + ((static_cast<uint64_t>(bs) * p.bslot_bytes) >> 4);
-        const uint32_t a_col = tmem + p.acc_cols + static_cast<uint32_t>(as) * 32u;
+        const uint32_t a_slot = tmem + p.acc_cols + static_cast<uint32_t>(as) * (32u * kStageBlocks);
         const uint32_t first = c == 0 ? 0u : 1u;
 #pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-          if (SIDE) {
-            ptx::mma_ts(tmem, a_col + ks * 8, bslot + ks * 16, idesc, ks == 0 ? first : 1u);
-          } else {
+        for (int b = 0; b < kStageBlocks; ++b) {
+          const uint64_t bblk = bslot + ((static_cast<uint64_t>(b) * p.b_chunk_bytes) >> 4);
+          const uint32_t a_col = a_slot + 32u * b;
 #pragma unroll
-            for (int t = 0; t < NSPLIT; ++t)
-              ptx::mma_ts(tmem, a_col + ks * 8, bslot + ks * 16 + t * term_off, idesc,
-                          (ks == 0 && t == 0) ? first : 1u);
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint32_t acc0 = (b == 0 && ks == 0) ? first : 1u;
+            if (SIDE) {
+              ptx::mma_ts(tmem, a_col + ks * 8, bblk + ks * 16, idesc, acc0);
+            } else {
+#pragma unroll
+              for (int t = 0; t < NSPLIT; ++t)
+                ptx::mma_ts(tmem, a_col + ks * 8, bblk + ks * 16 + t * term_off, idesc,
+                            t == 0 ? acc0 : 1u);
+            }
           }
         }
         ptx::mma_commit(&emptyA[as]);
@@ -181,11 +207,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ T
       bool w_ok = ptx::mbar_wait(&fullG[gs], static_cast<uint32_t>(c / kRG) & 1, p.err, 15,
                                  abort_flag);
       if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
-      const uint4 raw = *reinterpret_cast<const uint4*>(gring + gs * kBlockBytes + row * kRowBytes);
+      uint4 raw[kStageBlocks];
+#pragma unroll
+      for (int b = 0; b < kStageBlocks; ++b)
+        raw[b] = *reinterpret_cast<const uint4*>(gring + gs * kStageBytes + b * kBlockBytes +
+                                                 row * kRowBytes);
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&emptyG[gs]);
-      uint32_t a[32];
-      decode_row(raw, a);
       const int as = static_cast<int>(c % RA);
       if (c >= RA) {
         w_ok = ptx::mbar_wait(&emptyA[as], static_cast<uint32_t>(c / RA - 1) & 1, p.err, 16,
@@ -193,7 +221,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_tc_op(const __grid_constant__ T
         if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
       }
       ptx::tc_fence_after();
-      ptx::tmem_st32(tmem + lane_base + p.acc_cols + static_cast<uint32_t>(as) * 32u, a);
+#pragma unroll
+      for (int b = 0; b < kStageBlocks; ++b) {
+        uint32_t a[32];
+        decode_row(raw[b], a);
+        ptx::tmem_st32(tmem + lane_base + p.acc_cols +
+                           static_cast<uint32_t>(as * kStageBlocks + b) * 32u, a);
+      }
       ptx::tmem_wait_st();
       ptx::tc_fence_before();
       __syncwarp();
