@@ -180,6 +180,10 @@ struct OpDesc {
 
 int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st);
 int run_operator_fp32(coherit_geno* h, const OpDesc& d, cudaStream_t st);
+// Tensor-core operator with its workspace in caller-provided device memory
+// (`bytes` long); never allocates; rejects shapes whose workspace is larger.
+int run_operator_in_scratch(coherit_geno* h, const OpDesc& d, void* scratch, size_t bytes,
+                            cudaStream_t st);
 int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t nsplit);
 int ensure_ws_bytes(coherit_geno* h, size_t bytes);
 

@@ -475,6 +475,17 @@ static int launch_tc(int nsplit, bool side, dim3 grid, size_t smem, cudaStream_t
   return side ? go(k_tc_op<IS_K1, 3, true>) : go(k_tc_op<IS_K1, 3, false>);
 }
 
+// Column-block width when k exceeds what one launch holds (each block
+// re-reads the genotypes); k itself otherwise.
+static int column_step(int k, int kmax) {
+  if (k <= kmax) return k;
+  const int nblk = (k + kmax - 1) / kmax;
+  return static_cast<int>(round_up((k + nblk - 1) / nblk, 16));
+}
+
+static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit, uint8_t* ws,
+                           cudaStream_t st);
+
 int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
   if (d.precision == COHERIT_PREC_FP32) return run_operator_fp32(h, d, st);
   const int nsplit = nsplit_of(d.precision);
@@ -483,8 +494,7 @@ int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
     // Column blocks: each re-reads the genotypes.
     CO_CHECK(d.n_groups == 1, COHERIT_E_SHAPE,
              "batched requests wider than %d columns in one launch are not supported", kmax);
-    const int nblk = (d.k + kmax - 1) / kmax;
-    const int step = static_cast<int>(round_up((d.k + nblk - 1) / nblk, 16));
+    const int step = column_step(d.k, kmax);
     for (int c0 = 0; c0 < d.k; c0 += step) {
       OpDesc s = d;
       s.k = std::min(step, d.k - c0);
@@ -499,10 +509,44 @@ int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
   const int kp = static_cast<int>(round_up(std::max(d.k, 1), 16));
   int rc = ensure_workspace(h, kp, nsplit);
   if (rc != COHERIT_OK) return rc;
+  return launch_operator(h, d, kp, nsplit, static_cast<uint8_t*>(h->ws.base), st);
+}
+
+int run_operator_in_scratch(coherit_geno* h, const OpDesc& d, void* scratch, size_t bytes,
+                            cudaStream_t st) {
+  CO_CHECK(d.precision != COHERIT_PREC_FP32, COHERIT_E_UNSUPPORTED,
+           "the fixed-scratch operator runs the tensor-core precisions only");
+  CO_CHECK(d.precision >= COHERIT_PREC_BF16X3 && d.precision <= COHERIT_PREC_BF16X1,
+           COHERIT_E_SHAPE, "unknown precision %d", d.precision);
+  CO_CHECK(d.n_groups == 1, COHERIT_E_SHAPE, "the fixed-scratch operator takes one request");
+  const int nsplit = nsplit_of(d.precision);
+  const int step = column_step(d.k, max_kp_for(h, nsplit));
+  const int kp = static_cast<int>(round_up(std::max(step, 1), 16));
+  const size_t need = ws_layout(h, kp, nsplit).total;
+  CO_CHECK(need <= bytes, COHERIT_E_SHAPE,
+           "operator needs %zu bytes of scratch for n=%lld, m_pad=%lld, %d columns per launch; "
+           "the fixed scratch holds %zu bytes (use coherit_geno_kv)",
+           need, static_cast<long long>(h->n), static_cast<long long>(h->m_pad), kp, bytes);
+  for (int c0 = 0; c0 < d.k; c0 += step) {
+    OpDesc s = d;
+    s.k = std::min(step, d.k - c0);
+    s.V = d.V + c0;
+    s.out = d.out + c0;
+    s.col_start = {0, s.k};
+    const int kps = static_cast<int>(round_up(s.k, 16));
+    int rc = launch_operator(h, s, kps, nsplit, static_cast<uint8_t*>(scratch), st);
+    if (rc != COHERIT_OK) return rc;
+  }
+  return COHERIT_OK;
+}
+
+// One launch sequence (prep, K1, K2, corrections) for k <= max_kp_for columns
+// with the workspace at `ws` (laid out by ws_layout(h, kp, nsplit)).
+static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit, uint8_t* ws,
+                           cudaStream_t st) {
   const WsLayout L = ws_layout(h, kp, nsplit);
-  uint8_t* ws = static_cast<uint8_t*>(h->ws.base);
   EpiParams e;
-  rc = fill_epi(h, d, kp, nsplit, e);
+  int rc = fill_epi(h, d, kp, nsplit, e);
   if (rc != COHERIT_OK) return rc;
   auto* vt = reinterpret_cast<__nv_bfloat16*>(ws + L.vt);
   auto* sbuf = reinterpret_cast<__nv_bfloat16*>(ws + L.sbuf);

@@ -166,6 +166,27 @@ int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t preci
                     int32_t use_theta_e, float theta_e, const float* snp_weight,
                     float* out, int64_t ldo, void* stream);
 
+/* coherit_geno_kv with the same arguments and results, but the workspace is a
+ * fixed 64 MiB static device array instead of the handle's growable buffer,
+ * so the call allocates no device memory (no counterpart in the reference).
+ * For callers that cannot allocate or free during a solve: the per-handle
+ * buffer grows with cudaMalloc on the first wider call, and growing it runs
+ * cudaFree after a device-wide synchronisation, which stalls every other
+ * stream of a process that runs several solves at once.
+ *   - tensor-core precisions only (COHERIT_PREC_FP32 -> COHERIT_E_UNSUPPORTED);
+ *   - the workspace of one launch, about 2*nsplit*kp*(n_pad + m_pad) bytes
+ *     (+ 8*kp*m_pad with missing genotypes; kp = columns per launch rounded
+ *     up to 16), must fit 64 MiB, else COHERIT_E_SHAPE;
+ *   - the handle's device must be current; the first call on a device
+ *     resolves the array's address (cudaGetSymbolAddress), so make it before
+ *     any stream capture;
+ *   - calls on one device share the array: calls in flight at the same time
+ *     on different streams race; calls ordered on one stream are safe.     */
+int coherit_geno_kv_noalloc(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t precision,
+                            const float* V, int64_t ldv, int32_t k, const float* comp_scale,
+                            int32_t use_theta_e, float theta_e, const float* snp_weight,
+                            float* out, int64_t ldo, void* stream);
+
 /* Batched operator for independent requests sharing the genotypes: columns
  * [col_start[r], col_start[r+1]) of V belong to request r, which uses stats
  * slot slots[r] (its own sample subset, mean, sd, m_eff), per-component scale
