@@ -1,0 +1,432 @@
+"""Continuous-batching REML serving over one resident genotype matrix.
+
+Requests (a phenotype, optional covariates and an optional sample subset)
+are admitted while active slots and the HBM budget allow.  Every admitted
+request runs the ordinary ``fit_reml`` (strict AI-REML, affine SLQ) in its
+own worker thread; its genotype-operator applications do not launch kernels
+themselves but are handed to a batcher, which concatenates the pending
+right-hand sides of all active requests column-wise and applies the operator
+to all of them in one ``coherit_geno_kv_batched`` launch (each request with
+its own statistics slot -- mean, inverse sd and m_eff over its sample subset
+-- its own scale theta_g/m_eff and residual weight theta_e).  A request that
+arrives while others are in flight is admitted as soon as a slot frees up,
+and its operator work joins the running fits' launches.
+
+A request over a sample subset S is solved in the compressed index space of
+S (vectors of length |S|); the batcher scatters them into the n-row block
+and gathers the rows of S back, which is exactly K_S = Z_S Z_S^T / m_eff(S)
+with Z_S standardised over S -- the matrix a streamer built on the subset
+(``GenoBlockStreamer(..., sample_mask=S)``, geno_stream.py:1230-1247) applies.
+
+All device work goes to the device's default stream, so the batched launches
+and the fits' own tensor arithmetic are ordered without extra events.  Calls
+into the genotype library on the shared handle are serialised by one lock.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import threading
+import time
+from collections import deque
+from concurrent.futures import Future
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geno_stream import GenoBlockStreamer
+from .reml import fit_reml
+
+# Widest right-hand-side block one batched launch takes per precision: the
+# B-operand ring of the tensor-core operator must hold two pipeline stages of
+# all split terms in shared memory (227 KB per CTA on GB300).
+_MAX_BATCH_COLS = {"bf16x3": 112, "bf16x2": 176, "bf16x1": 256}
+
+
+@dataclasses.dataclass
+class ServeResult:
+    request_id: int
+    var_components: np.ndarray
+    heritability: float
+    loglik: float
+    n_samples: int
+    arrival: float
+    start: float
+    finish: float
+    history: list
+
+    @property
+    def latency(self) -> float:
+        return self.finish - self.arrival
+
+
+@dataclasses.dataclass
+class _Request:
+    rid: int
+    y: np.ndarray
+    covar: Optional[np.ndarray]
+    mask: Optional[np.ndarray]
+    arrival: float
+    future: Future
+    fit_kwargs: dict
+    n_sub: int
+    bytes_estimate: int
+    slot: int = 0
+    idx: Optional[torch.Tensor] = None
+    eff: float = 0.0
+    atom: float = 0.0
+
+
+class _Op:
+    __slots__ = ("req", "V", "scale", "theta_e", "done", "out", "error")
+
+    def __init__(self, req, V, scale, theta_e):
+        self.req = req
+        self.V = V
+        self.scale = scale
+        self.theta_e = theta_e
+        self.done = threading.Event()
+        self.out = None
+        self.error = None
+
+
+class _Batcher:
+    """Collects operator applications of concurrent fits into batched launches.
+
+    A launch goes out when every active fit has an application pending, or
+    ``window_s`` after the first pending one arrived, whichever is first.
+    """
+
+    def __init__(self, streamer: GenoBlockStreamer, precision: str, window_s: float,
+                 max_cols: int, lib_lock: threading.Lock):
+        self.st = streamer
+        self.prec = _lib.PRECISIONS[precision]
+        self.window_s = float(window_s)
+        self.max_cols = int(max_cols)
+        self.lib_lock = lib_lock
+        self.cv = threading.Condition()
+        self.pending: list[_Op] = []
+        self.n_active = 0
+        self.stop = False
+        self.launches = 0
+        self.columns = 0
+        self.requests_per_launch: list[int] = []
+        self.thread = threading.Thread(target=self._loop, name="coherit-batcher", daemon=True)
+        self.thread.start()
+
+    def set_active(self, delta: int) -> None:
+        with self.cv:
+            self.n_active += delta
+            self.cv.notify_all()
+
+    def apply(self, req: _Request, V: torch.Tensor, scale: float, theta_e) -> torch.Tensor:
+        vec = V.ndim == 1
+        V2 = (V[:, None] if vec else V).to(torch.float32).contiguous()
+        if V2.shape[0] != req.n_sub:
+            raise ValueError(f"V has {V2.shape[0]} rows, the request has {req.n_sub} samples")
+        op = _Op(req, V2, float(scale), None if theta_e is None else float(theta_e))
+        with self.cv:
+            if self.stop:
+                raise RuntimeError("REMLServer is closed.")
+            self.pending.append(op)
+            self.cv.notify_all()
+        op.done.wait()
+        if op.error is not None:
+            raise op.error
+        return op.out[:, 0] if vec else op.out
+
+    def close(self) -> None:
+        with self.cv:
+            self.stop = True
+            self.cv.notify_all()
+        self.thread.join(timeout=30)
+
+    def _take(self) -> list[_Op]:
+        with self.cv:
+            while not self.pending and not self.stop:
+                self.cv.wait()
+            if not self.pending:
+                return []
+            deadline = time.perf_counter() + self.window_s
+            while len(self.pending) < self.n_active and not self.stop:
+                left = deadline - time.perf_counter()
+                if left <= 0:
+                    break
+                self.cv.wait(timeout=left)
+            batch, rest, cols = [], [], 0
+            for op in self.pending:
+                k = op.V.shape[1]
+                if batch and cols + k > self.max_cols:
+                    rest.append(op)
+                else:
+                    batch.append(op)
+                    cols += k
+            self.pending = rest
+            return batch
+
+    def _loop(self) -> None:
+        while True:
+            batch = self._take()
+            if not batch:
+                return
+            try:
+                self._launch(batch)
+            except BaseException as err:  # handed to every fit in the batch
+                for op in batch:
+                    op.error = err
+            for op in batch:
+                op.done.set()
+
+    def _launch(self, batch: list[_Op]) -> None:
+        st = self.st
+        widths = [op.V.shape[1] for op in batch]
+        K = int(sum(widths))
+        col_start = np.zeros(len(batch) + 1, dtype=np.int32)
+        col_start[1:] = np.cumsum(widths)
+        Vf = torch.zeros((st.n, K), dtype=torch.float32, device=st.dev)
+        for op, c0, k in zip(batch, col_start[:-1], widths):
+            if op.req.idx is None:
+                Vf[:, c0:c0 + k] = op.V
+            else:
+                Vf[op.req.idx, c0:c0 + k] = op.V
+        slots = np.asarray([op.req.slot for op in batch], dtype=np.int32)
+        scale = np.asarray([op.scale for op in batch], dtype=np.float32)
+        te = np.asarray([0.0 if op.theta_e is None else op.theta_e for op in batch],
+                        dtype=np.float32)
+        out = torch.empty_like(Vf)
+        with self.lib_lock:
+            _lib.check(_lib.load().coherit_geno_kv_batched(
+                st.handle, len(batch), col_start.ctypes.data, slots.ctypes.data, self.prec,
+                Vf.data_ptr(), K, K, scale.ctypes.data, te.ctypes.data, out.data_ptr(), K,
+                _lib.stream_ptr()), "batched kv")
+        st.op_stats["apps"] += 1
+        st.op_stats["cols"] += K
+        self.launches += 1
+        self.columns += K
+        self.requests_per_launch.append(len(batch))
+        for op, c0, k in zip(batch, col_start[:-1], widths):
+            blk = out[:, c0:c0 + k]
+            op.out = (blk if op.req.idx is None else blk[op.req.idx]).contiguous()
+
+
+class REMLServer:
+    """Serve single-GRM REML fits of many phenotypes over one resident matrix.
+
+    ``max_active`` bounds the fits in flight; ``hbm_budget_bytes`` bounds the
+    device memory their solver state may take (estimated per request from its
+    sample count and right-hand-side width; default half the free memory).
+    ``fit_kwargs`` go to ``fit_reml`` (defaults: 30 trace probes, 30 SLQ
+    probes x 30 Lanczos steps, PCG tol 1e-5, 20 AI iterations).
+    """
+
+    def __init__(self, streamer: GenoBlockStreamer, *, max_active: int = 8,
+                 hbm_budget_bytes: float | None = None, precision: str = "bf16x3",
+                 batch_window_s: float = 0.002, max_batch_cols: int | None = None,
+                 fit_kwargs: dict | None = None):
+        if streamer.n_components != 1:
+            raise ValueError("REMLServer serves single-GRM fits (one genotype component).")
+        if precision not in _MAX_BATCH_COLS:
+            raise ValueError(f"precision must be one of {sorted(_MAX_BATCH_COLS)}")
+        if max_active < 1:
+            raise ValueError("max_active must be >= 1")
+        self.st = streamer
+        self.max_active = int(max_active)
+        if hbm_budget_bytes is None:
+            free, _ = torch.cuda.mem_get_info(streamer.dev)
+            hbm_budget_bytes = 0.5 * free
+        self.budget = float(hbm_budget_bytes)
+        self.precision = precision
+        self._lib_lock = threading.Lock()
+        # Statistics slots 1..max_active serve subset requests; creating the
+        # highest one first sizes the handle's slot table once.
+        self._free_slots = deque(range(1, self.max_active + 1))
+        with self._lib_lock:
+            _lib.check(_lib.load().coherit_geno_compute_stats(
+                streamer.handle, self.max_active, None, None, None, None, _lib.stream_ptr()),
+                "reserve stats slots")
+        cols = _MAX_BATCH_COLS[precision] if max_batch_cols is None else int(max_batch_cols)
+        self.batcher = _Batcher(streamer, precision, batch_window_s, cols, self._lib_lock)
+        self.fit_kwargs = dict(n_rand_vec=30, maxiter=500, minq_iter=20, slq_samples=30,
+                               slq_m=30, pcg_tol=1e-5, verbose=False)
+        if fit_kwargs:
+            self.fit_kwargs.update(fit_kwargs)
+        self._cv = threading.Condition()
+        self._waiting: deque[_Request] = deque()
+        self._active = 0
+        self._bytes_active = 0.0
+        self._next_id = 0
+        self._closed = False
+        self.results: list[ServeResult] = []
+        self._admitter = threading.Thread(target=self._admit_loop, name="coherit-admit",
+                                          daemon=True)
+        self._admitter.start()
+
+    # -------------------------------------------------------------- requests
+    def submit(self, y, covar=None, sample_mask=None, **fit_kwargs) -> Future:
+        """Queue one fit; returns a Future resolving to a ServeResult.
+
+        ``y`` and ``covar`` have one row per selected sample (all samples of
+        the resident matrix when ``sample_mask`` is None)."""
+        if self._closed:
+            raise RuntimeError("REMLServer is closed.")
+        mask = None
+        n_sub = self.st.n
+        if sample_mask is not None:
+            mask = np.asarray(sample_mask, dtype=bool).reshape(-1)
+            if mask.size != self.st.n:
+                raise ValueError(f"sample_mask has {mask.size} entries, the matrix has "
+                                 f"{self.st.n} samples")
+            n_sub = int(mask.sum())
+            if n_sub == 0:
+                raise ValueError("sample_mask selects no samples")
+        y = np.asarray(y, dtype=np.float32).reshape(-1)
+        if y.size != n_sub:
+            raise ValueError(f"phenotype has {y.size} entries, the sample set has {n_sub}")
+        if covar is not None:
+            covar = np.asarray(covar, dtype=np.float32)
+            if covar.ndim == 1:
+                covar = covar[:, None]
+            if covar.shape[0] != n_sub:
+                raise ValueError("covariates must have one row per selected sample")
+        kw = dict(self.fit_kwargs)
+        kw.update(fit_kwargs)
+        p = 0 if covar is None else covar.shape[1]
+        width = p + 1 + int(kw.get("n_rand_vec", 30)) + int(kw.get("slq_samples", 30))
+        # Solver state: a few n x width FP32 blocks (solutions, residuals,
+        # directions, operator outputs) plus the Lanczos basis of the probes.
+        est = 4 * n_sub * (8 * width + int(kw.get("slq_m", 30)) * int(kw.get("slq_samples", 30)))
+        fut: Future = Future()
+        with self._cv:
+            rid = self._next_id
+            self._next_id += 1
+            self._waiting.append(_Request(rid=rid, y=y, covar=covar, mask=mask,
+                                          arrival=time.perf_counter(), future=fut,
+                                          fit_kwargs=kw, n_sub=n_sub, bytes_estimate=est))
+            self._cv.notify_all()
+        return fut
+
+    def map(self, requests) -> list[ServeResult]:
+        """Submit (y, covar, sample_mask) tuples and wait for all results."""
+        futs = [self.submit(*r) for r in requests]
+        return [f.result() for f in futs]
+
+    def stats(self) -> dict:
+        lat = np.asarray([r.latency for r in self.results], dtype=np.float64)
+        out = {"completed": int(lat.size), "launches": self.batcher.launches,
+               "columns": self.batcher.columns,
+               "mean_requests_per_launch": float(np.mean(self.batcher.requests_per_launch))
+               if self.batcher.requests_per_launch else 0.0}
+        if lat.size:
+            out.update(p50_s=float(np.percentile(lat, 50)), p99_s=float(np.percentile(lat, 99)))
+        return out
+
+    def close(self) -> None:
+        with self._cv:
+            self._closed = True
+            self._cv.notify_all()
+        self._admitter.join(timeout=30)
+        self.batcher.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------- admission
+    def _can_admit(self, req: _Request) -> bool:
+        if self._active >= self.max_active:
+            return False
+        if req.mask is not None and not self._free_slots:
+            return False
+        return self._active == 0 or self._bytes_active + req.bytes_estimate <= self.budget
+
+    def _admit_loop(self) -> None:
+        while True:
+            with self._cv:
+                while not self._closed and not (self._waiting and
+                                                self._can_admit(self._waiting[0])):
+                    self._cv.wait()
+                if self._closed:
+                    for req in self._waiting:
+                        req.future.set_exception(RuntimeError("REMLServer is closed."))
+                    self._waiting.clear()
+                    return
+                req = self._waiting.popleft()
+                self._active += 1
+                self._bytes_active += req.bytes_estimate
+                if req.mask is not None:
+                    req.slot = self._free_slots.popleft()
+            self.batcher.set_active(+1)
+            threading.Thread(target=self._run, args=(req,), name=f"coherit-fit-{req.rid}",
+                             daemon=True).start()
+
+    def _release(self, req: _Request) -> None:
+        self.batcher.set_active(-1)
+        with self._cv:
+            self._active -= 1
+            self._bytes_active -= req.bytes_estimate
+            if req.slot > 0:
+                self._free_slots.append(req.slot)
+            self._cv.notify_all()
+
+    # ------------------------------------------------------------------- fit
+    def _prepare(self, req: _Request) -> None:
+        st = self.st
+        if req.mask is None:
+            req.eff = st._eff_m_host
+            req.atom = st._mean_diag_atom_host
+            return
+        lib = _lib.load()
+        mask_u8 = np.ascontiguousarray(req.mask, dtype=np.uint8)
+        ce = np.zeros(st.n_components)
+        ca = np.zeros(st.n_components)
+        et, at = C.c_double(), C.c_double()
+        with self._lib_lock:
+            _lib.check(lib.coherit_geno_compute_stats(
+                st.handle, req.slot, mask_u8.ctypes.data, None, None, None, _lib.stream_ptr()),
+                "request stats")
+            _lib.check(lib.coherit_geno_stats_summary(st.handle, req.slot, ce.ctypes.data,
+                                                      ca.ctypes.data, C.byref(et), C.byref(at)),
+                       "request stats summary")
+        req.eff, req.atom = float(et.value), float(at.value)
+        req.idx = torch.as_tensor(np.flatnonzero(req.mask), dtype=torch.long, device=st.dev)
+
+    def _run(self, req: _Request) -> None:
+        start = time.perf_counter()
+        try:
+            torch.cuda.set_device(self.st.dev)
+            self._prepare(req)
+            b = self.batcher
+            inv_eff = 1.0 / req.eff if req.eff > 0 else 1.0
+
+            def K(V):
+                return b.apply(req, V, inv_eff, None)
+
+            def whv(theta_g, theta_e, V):
+                tg = float(np.asarray(theta_g, dtype=np.float64).reshape(-1)[0])
+                return b.apply(req, V, tg * inv_eff, float(theta_e))
+
+            diag = torch.tensor(req.atom, dtype=torch.float32, device=self.st.dev)
+            param, hist, d = fit_reml(req.y, [K], [diag], req.covar, weighted_hv=whv,
+                                      device=self.st.dev, return_diagnostics=True,
+                                      **req.fit_kwargs)
+            gen = float(np.dot(param[:1], np.asarray(d.get("genetic_trace_atoms", [1.0]))))
+            res = float(np.dot(param[1:], np.asarray(d.get("residual_trace_atoms", [1.0]))))
+            out = ServeResult(request_id=req.rid, var_components=np.asarray(param),
+                              heritability=gen / max(gen + res, 1e-12),
+                              loglik=float(d["loglik"]), n_samples=req.n_sub,
+                              arrival=req.arrival, start=start, finish=time.perf_counter(),
+                              history=hist)
+            with self._cv:
+                self.results.append(out)
+            req.future.set_result(out)
+        except BaseException as err:
+            req.future.set_exception(err)
+        finally:
+            self._release(req)
+
+
+__all__ = ["REMLServer", "ServeResult"]
