@@ -3,29 +3,33 @@
 
 Workload (default ``--config c2``): single-GRM REML, n=50,000 samples x
 m=500,000 SNPs from the MAF~U(0.05,0.5)/HWE generator (synthetic; genotypes
-generated on the device), phenotype with h2=0.3 from 5,000 causal SNPs,
-10 N(0,1) covariates + intercept, 64 Rademacher SLQ probes (30-step
-Lanczos), projected-core preconditioner.  A step is one complete REML fit
-(operator applications, block PCG, SLQ, AI/NNLS line search).
+generated on the device); each phenotype has h2=0.3 from 5,000 causal SNPs,
+10 N(0,1) covariates + intercept; 64 Rademacher SLQ probes, 30-step Lanczos,
+PCG tol 1e-5.  A step is one serving batch: R (``--requests``, default 8)
+phenotypes submitted together to the REMLServer, each fitted completely
+(operator applications, block PCG, affine SLQ, AI/NNLS line search), their
+operator applications batched into shared launches.
 
 Arms:
-  ours       (default) the mixed-precision tensor-core form (BF16 genotypes,
-             BF16x3 right-hand sides, FP32 PCG, FP64 small solves).  The same
-             line reports the plain FP32 single-fit GPU form (CUDA-core FP32
-             operator) as ``plain_fp32``, the operator roofline, and the CPU
-             baseline (the oracle's FP32 restatement of kv_impl_streamed,
-             timed on a bounded sample and scaled by the operator work the GPU
-             fit performed).
+  ours       (default) the mixed-precision batched serving form (BF16
+             genotypes, BF16x3 right-hand sides, FP32 PCG, FP64 small
+             solves).  The same line reports the same fits run one at a time
+             through the single-fit model API (``single_fit_mixed``), the
+             plain FP32 single-fit GPU form (CUDA-core FP32 operator,
+             ``plain_fp32_single_fit``), the operator roofline at the batched
+             width, and the CPU baseline (the oracle's FP32 restatement of
+             kv_impl_streamed, timed on a bounded sample and scaled by the
+             operator work of one fit).
   reference  ``--impl reference``: the CPU restatement of the reference path
              (the reference itself needs jax/numba, absent on these machines)
              on all host cores, on bounded samples of the same workload.
 
-Timing: W warm-up fits, then K timed fits bracketed by barrier +
+Timing: W warm-up steps, then K timed steps bracketed by barrier +
 synchronize; inputs (6.25 GB of packed genotypes per copy) exceed the 129 MB
 L2, so no explicit flush is needed.  ``value`` is device-timed with the
-phenotype and covariates already resident; ``e2e`` times the public API call
-with the phenotype/covariates copied from pinned host memory each step and
-the variance components read back.
+phenotypes and covariates already resident; ``e2e`` times the same serving
+steps through the public API with phenotypes/covariates taken from pinned
+host memory and the variance components returned to the host.
 """
 from __future__ import annotations
 
@@ -156,17 +160,41 @@ def cpu_fit_estimate(wl, apps: int, cols: int, budget_s: float = 20.0):
 # ----------------------------------------------------------------- our arm
 
 def build_problem(wl, device):
-    import torch
-
-    from coherit_gb300 import synth
     from coherit_gb300.geno_stream import GenoBlockStreamer, SyntheticSource
 
-    st = GenoBlockStreamer(SyntheticSource(wl.n, wl.m, seed=wl.seed),
-                           component_block_sizes=list(wl.components) if wl.components else None,
-                           device=device, precision="bf16x3")
-    y, X, _, _ = synth.phenotype(wl.seed, wl.n, wl.m, h2=wl.h2, n_causal=wl.n_causal,
-                                 n_covar=wl.n_covar)
-    return st, y, X
+    return GenoBlockStreamer(SyntheticSource(wl.n, wl.m, seed=wl.seed),
+                             component_block_sizes=list(wl.components) if wl.components else None,
+                             device=device, precision="bf16x3")
+
+
+def make_phenotypes(st, wl, R: int, seed: int):
+    """R phenotypes over the resident genotypes: for each, wl.n_causal causal
+    SNPs with N(0,1) effects on standardised genotypes (one Z B product on the
+    device for all R), scaled to variance wl.h2, plus N(0, 1 - wl.h2) noise;
+    covariates [1, wl.n_covar x N(0,1)].  Returns device tensors."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    B = np.zeros((st.m, R), dtype=np.float32)
+    for r in range(R):
+        causal = rng.choice(st.m, size=min(wl.n_causal, st.m), replace=False)
+        B[causal, r] = rng.normal(size=causal.size)
+    g = st.zxb(torch.as_tensor(B, device=st.dev)).double()
+    g = g * torch.sqrt(wl.h2 / g.var(dim=0, unbiased=False))
+    gen = torch.Generator(device=st.dev).manual_seed(seed)
+    noise = torch.randn((st.n, R), generator=gen, device=st.dev, dtype=torch.float64)
+    ys = (g + noise * math.sqrt(1.0 - wl.h2)).float()
+    Xs = []
+    for r in range(R):
+        X = torch.randn((st.n, wl.n_covar + 1), generator=gen, device=st.dev)
+        X[:, 0] = 1.0
+        Xs.append(X)
+    return [ys[:, r].contiguous() for r in range(R)], Xs
+
+
+def fit_kwargs(wl):
+    return dict(n_rand_vec=30, maxiter=1000, minq_iter=wl.minq_iter, slq_samples=wl.slq_samples,
+                slq_m=wl.slq_m, pcg_tol=wl.pcg_tol, verbose=False, seed=wl.seed)
 
 
 def make_fitter(st, wl, precision):
@@ -179,10 +207,16 @@ def make_fitter(st, wl, precision):
     return InfinitesimalREMLFitter(cfg, [st])
 
 
-def operator_roofline(st, k, hbm_peak, reps=10):
-    import torch
+def _percentile(xs, q):
+    xs = sorted(xs)
+    return xs[min(len(xs) - 1, max(0, int(math.ceil(q * len(xs))) - 1))]
 
-    from coherit_gb300 import _lib
+
+def operator_roofline(st, k, hbm_peak, tensor_peak, reps=10):
+    """Device time of one batched-width operator application, its HBM and
+    tensor fractions (algorithmic bytes n*ceil(m/4) + 8nk + 8m and flops
+    4nmk), timed with CUDA events on the launching stream."""
+    import torch
 
     V = torch.randn(st.n, k, device=st.dev)
     for _ in range(3):
@@ -198,24 +232,44 @@ def operator_roofline(st, k, hbm_peak, reps=10):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
     alg_bytes = st.n * ((st.m + 3) // 4) + 8 * st.n * k + 8 * st.m
-    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    alg_flops = 4.0 * st.n * st.m * k
+    gbs = alg_bytes / (ms * 1e-3) / 1e9
+    tfs = alg_flops / (ms * 1e-3) / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "operator_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            tr = json.load(f)
-        key = f"{st.n}x{st.m}x{k}"
-        traffic = tr.get(key)
-    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
-            "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
-            "kernel": "genotype operator application (K1 + K2 + prep), k=%d" % k,
-            "ms_per_application": round(ms, 4), "algorithmic_bytes": alg_bytes}
+            traffic = json.load(f).get(f"{st.n}x{st.m}x{k}")
+    hbm_frac, ten_frac = gbs / hbm_peak, tfs / tensor_peak
+    if ten_frac >= hbm_frac:
+        roof = {"bound": "tensor", "achieved": round(tfs, 1), "peak": tensor_peak,
+                "unit": "TFLOP/s", "frac": round(ten_frac, 4)}
+    else:
+        roof = {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(hbm_frac, 4)}
+    roof.update({"traffic": traffic,
+                 "kernel": f"genotype operator application (prep + K1 + K2), k={k}, bf16x3",
+                 "ms_per_application": round(ms, 4), "algorithmic_bytes": alg_bytes,
+                 "algorithmic_flops": alg_flops, "hbm_gbs": round(gbs, 1),
+                 "hbm_frac": round(hbm_frac, 4), "tensor_tflops": round(tfs, 1),
+                 "tensor_frac": round(ten_frac, 4)})
+    return roof
+
+
+def serve_step(srv, ys, Xs, host: bool):
+    """One step: all R requests submitted at once; returns their results."""
+    if host:
+        futs = [srv.submit(y.cpu().numpy(), X.cpu().numpy()) for y, X in zip(ys, Xs)]
+    else:
+        futs = [srv.submit(y, X) for y, X in zip(ys, Xs)]
+    return [f.result() for f in futs]
 
 
 def run_ours(args, wl):
     import torch
 
     from coherit_gb300 import _lib
+    from coherit_gb300.serving import REMLServer
 
     ws, rank, local = _dist()
     dev = torch.device("cuda", local)
@@ -227,31 +281,21 @@ def run_ours(args, wl):
         tdist.init_process_group("nccl", device_id=dev)
         dist = tdist
     lib = _lib.load()
-    hbm_peak, _, peak_src = _peaks()
-    st, y, X = build_problem(wl, dev)
-    fitter = make_fitter(st, wl, args.precision)
-    y_pin = torch.as_tensor(y).pin_memory()
-    X_pin = torch.as_tensor(X).pin_memory()
-    y_dev = y_pin.to(dev)
-    X_dev = X_pin.to(dev)
-    h2s = []
-
-    def one_fit(host: bool):
-        if host:
-            yd = y_pin.to(dev, non_blocking=True)
-            Xd = X_pin.to(dev, non_blocking=True)
-        else:
-            yd, Xd = y_dev, X_dev
-        res = fitter.fit_infinitesimal(yd, Xd)
-        vc = np.asarray(res.var_components, dtype=np.float64)  # host copy of the result
-        h2s.append(res.heritability)
-        return res, vc
+    hbm_peak, tensor_peak, peak_src = _peaks()
+    st = build_problem(wl, dev)
+    R = args.requests
+    ys, Xs = make_phenotypes(st, wl, R, seed=wl.seed + 17 * rank)
+    # Host copies for the end-to-end leg (pinned, as a serving front end holds them).
+    ys_host = [y.cpu().pin_memory() for y in ys]
+    Xs_host = [X.cpu().pin_memory() for X in Xs]
+    srv = REMLServer(st, max_active=R, precision=args.precision, fit_kwargs=fit_kwargs(wl))
 
     for _ in range(args.warmup):
-        one_fit(False)
+        serve_step(srv, ys, Xs, host=False)
     torch.cuda.synchronize()
-    apps0, cols0 = st.op_stats["apps"], st.op_stats["cols"]
     launches0 = lib.coherit_launch_count()
+    b0, c0 = srv.batcher.launches, srv.batcher.columns
+    n_res0 = len(srv.results)
     sampler = ClockSampler(local)
     sampler.start()
     if dist is not None:
@@ -260,12 +304,10 @@ def run_ours(args, wl):
     stream = torch.cuda.current_stream()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    lat = []
     e0.record(stream)
+    timed = []
     for _ in range(args.steps):
-        t0 = time.perf_counter()
-        one_fit(False)
-        lat.append(time.perf_counter() - t0)
+        timed.extend(serve_step(srv, ys, Xs, host=False))
     e1.record(stream)
     torch.cuda.synchronize()
     if dist is not None:
@@ -273,44 +315,77 @@ def run_ours(args, wl):
     clocks = sampler.stop()
     dev_s = e0.elapsed_time(e1) / 1e3
     launches = lib.coherit_launch_count() - launches0
-    apps = (st.op_stats["apps"] - apps0) / args.steps
-    cols = (st.op_stats["cols"] - cols0) / args.steps
-    # end to end through the public API with host inputs
+    op_launches = srv.batcher.launches - b0
+    op_cols = srv.batcher.columns - c0
+    lat = [r.latency for r in timed]
+
+    # End to end through the public API: phenotypes/covariates from pinned
+    # host memory each step, variance components back on the host.
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        one_fit(True)
+        futs = [srv.submit(y.numpy(), X.numpy()) for y, X in zip(ys_host, Xs_host)]
+        e2e_res = [f.result() for f in futs]
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    srv.close()
     if dist is not None:
         t = torch.tensor([dev_s, e2e_s], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dev_s, e2e_s = float(t[0]), float(t[1])
-    total_fits = args.steps * ws
+    total_fits = args.steps * R * ws
     value = total_fits / (dev_s / 3600.0)
     e2e_val = total_fits / (e2e_s / 3600.0)
     result = None
     if rank == 0:
-        roof = operator_roofline(st, wl.n_covar + 2, hbm_peak)
+        k_typ = max(16, int(round(op_cols / max(op_launches, 1))))
+        roof = operator_roofline(st, k_typ, hbm_peak, tensor_peak)
         roof["peak_source"] = peak_src
+        single = None
         plain = None
-        if not args.no_plain:
-            pf = make_fitter(st, wl, "fp32")
+        if not args.no_single:
+            # The same fits one at a time through the single-fit model API
+            # (mixed precision, projected-core preconditioner, shared setup).
+            fitter = make_fitter(st, wl, args.precision)
+            fitter.fit_infinitesimal(ys[0], Xs[0])
+            torch.cuda.synchronize()
+            a0, k0 = st.op_stats["apps"], st.op_stats["cols"]
             t0 = time.perf_counter()
-            pres = pf.fit_infinitesimal(y_dev, X_dev)
+            sh2 = []
+            for r in range(min(R, args.single_fits)):
+                sh2.append(fitter.fit_infinitesimal(ys[r], Xs[r]).heritability)
+            torch.cuda.synchronize()
+            ts = (time.perf_counter() - t0) / len(sh2)
+            fit_apps = (st.op_stats["apps"] - a0) / len(sh2)
+            fit_cols = (st.op_stats["cols"] - k0) / len(sh2)
+            single = {"fits_per_hr": round(3600.0 / ts, 3), "fit_s": round(ts, 4),
+                      "operator_apps_per_fit": fit_apps, "rhs_columns_per_fit": fit_cols,
+                      "max_abs_dh2_vs_served": round(max(
+                          abs(a - b.heritability) for a, b in zip(sh2, timed)), 6)}
+        else:
+            fit_apps, fit_cols = args.ref_apps, args.ref_cols
+        if not args.no_plain:
+            # Plain FP32 single-fit form, warm (its shared setup built by a
+            # first fit), timed on the second phenotype.
+            pf = make_fitter(st, wl, "fp32")
+            pf.fit_infinitesimal(ys[0], Xs[0])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pres = pf.fit_infinitesimal(ys[1 % R], Xs[1 % R])
             torch.cuda.synchronize()
             tp = time.perf_counter() - t0
             plain = {"fits_per_hr": round(3600.0 / tp, 3), "fit_s": round(tp, 3),
                      "h2": round(pres.heritability, 6),
-                     "abs_dh2_vs_mixed": round(abs(pres.heritability - h2s[-1]), 6)}
+                     "abs_dh2_vs_served": round(
+                         abs(pres.heritability - timed[1 % R].heritability), 6)}
         cpu = None
         if not args.no_cpu:
-            t_fit, cores, sample = cpu_fit_estimate(wl, apps, cols)
+            t_fit, cores, sample = cpu_fit_estimate(wl, fit_apps, fit_cols)
             cpu = {"value": round(3600.0 / t_fit, 4), "unit": "fits/hr", "cores": cores,
                    "kind": "port", "sample": sample, "fit_s_extrapolated": round(t_fit, 1)}
-        lat_sorted = sorted(lat)
         result = {
-            "metric": "REML fits/hr (mixed-precision BF16x3 tensor-core form; plain FP32 form and p50/p99 fit latency alongside)",
+            "metric": "REML fits/hr, p50/p99 latency: mixed-precision batched serving form "
+                      "(plain FP32 single-fit form alongside), 1 GB300, |dh2|<1e-3",
             "value": round(value, 3),
             "unit": "fits/hr",
             "n_gpus": ws,
@@ -321,23 +396,26 @@ def run_ours(args, wl):
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": "bf16x3 genotype operator, fp32 PCG, fp64 small solves",
-            "data": "synthetic (device-generated MAF~U(0.05,0.5) HWE genotypes; phenotype h2=%.2f)" % wl.h2,
-            "config": {"workload": wl.name, "n": wl.n, "m": wl.m, "slq_probes": wl.slq_samples,
+            "data": "synthetic (device-generated MAF~U(0.05,0.5) HWE genotypes; "
+                    f"{R} phenotypes with h2={wl.h2}, {wl.n_causal} causal SNPs each)",
+            "config": {"workload": wl.name, "n": wl.n, "m": wl.m,
+                       "requests_per_step": R, "slq_probes": wl.slq_samples,
                        "lanczos_steps": wl.slq_m, "covariates": wl.n_covar,
-                       "precond_rank": wl.precond_rank, "pcg_tol": wl.pcg_tol,
-                       "parallelism": f"replicas x{ws}",
+                       "pcg_tol": wl.pcg_tol, "parallelism": f"replicas x{ws}",
                        "l2_policy": "inputs larger than L2 (2 x 6.25 GB packed genotypes)"},
             "latency_s": {"p50": round(statistics.median(lat), 3),
-                          "p99": round(lat_sorted[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)], 3)},
-            "h2": round(h2s[-1], 6),
-            "operator_apps_per_fit": apps,
-            "rhs_columns_per_fit": cols,
+                          "p99": round(_percentile(lat, 0.99), 3)},
+            "h2": [round(r.heritability, 4) for r in timed[:R]],
+            "operator_launches_per_step": op_launches / args.steps,
+            "rhs_columns_per_launch": round(op_cols / max(op_launches, 1), 1),
             "e2e": {"value": round(e2e_val, 3), "unit": "fits/hr",
-                    "h2d_bytes_per_step": int(y_pin.numel() * 4 + X_pin.numel() * 4),
-                    "d2h_bytes_per_step": 8 * 2},
+                    "h2d_bytes_per_step": int(sum(y.numel() * 4 + X.numel() * 4
+                                                  for y, X in zip(ys_host, Xs_host))),
+                    "d2h_bytes_per_step": int(sum(r.var_components.size * 8 for r in e2e_res))},
             "gpu_launches": int(launches),
             "roofline": roof,
-            "plain_fp32": plain,
+            "single_fit_mixed": single,
+            "plain_fp32_single_fit": plain,
             "cpu_baseline": cpu,
             "clocks": clocks,
         }
@@ -393,11 +471,18 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="c2")
     ap.add_argument("--precision", default="bf16x3")
+    ap.add_argument("--requests", type=int, default=8,
+                    help="concurrent fit requests per step (the serving batch)")
+    ap.add_argument("--single-fits", type=int, default=3,
+                    help="fits timed one at a time for the single-fit comparison")
+    ap.add_argument("--no-single", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--ref-apps", type=float, default=200.0,
+    # Operator work of one warm c2 fit, as counted on the GPU path (same
+    # algorithm and probe settings as the reference's single fit).
+    ap.add_argument("--ref-apps", type=float, default=52.0,
                     help="operator applications per fit assumed by the reference arm")
-    ap.add_argument("--ref-cols", type=float, default=4000.0,
+    ap.add_argument("--ref-cols", type=float, default=368.0,
                     help="right-hand-side columns per fit assumed by the reference arm")
     args = ap.parse_args()
     from coherit_gb300.configs import WORKLOADS

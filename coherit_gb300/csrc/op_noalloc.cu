@@ -14,7 +14,8 @@
 //
 // Limits: single request, tensor-core precisions; the workspace of one
 // launch (about 2*nsplit*kp*(n_pad + m_pad) bytes, plus 8*kp*m_pad with
-// missing genotypes) must fit kScratchBytes, else COHERIT_E_SHAPE.
+// missing genotypes, plus the split-K partials) must fit kScratchBytes, else
+// COHERIT_E_SHAPE.
 //
 // What must start at zero: only the FP64 rank-one accumulators, cleared by
 // the launch sequence on every call; every other region is written before it

@@ -83,6 +83,10 @@ struct TcParams {
   uint32_t tmem_cols;
   uint32_t acc_cols;
   int* err;
+  int ksplit;           // CTAs along K (gridDim.z); > 1 writes partials
+  float* part;          // ksplit x part_stride FP32 partials (ksplit > 1)
+  int64_t part_stride;  // floats per K share: rows x kp
+  int64_t part_rows;    // K2: rows per component block (n_pad)
   EpiParams e;
 };
 
@@ -200,6 +204,50 @@ __device__ __forceinline__ void epilogue_k2(const EpiParams& e, int64_t i, int c
 }
 
 #include "tc_kernel.cuh"
+
+// Split-K finish: T = sum of the ksplit FP32 partials of (row, 16 columns) in
+// fixed order, then the K1 or K2 epilogue.  Block (32, 4): x = row within a
+// 32-row group (a full warp, as epilogue_k1's reductions need), y = column
+// chunk.
+__global__ void __launch_bounds__(128) k_k1_finish(const float* __restrict__ part, int ksplit,
+                                                    int64_t stride, EpiParams e) {
+  const int64_t j = static_cast<int64_t>(blockIdx.x) * 32 + threadIdx.x;
+  const int c0 = 16 * static_cast<int>(blockIdx.y * 4 + threadIdx.y);
+  if (c0 >= e.kp) return;  // uniform per warp
+  float T[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) T[i] = 0.f;
+  for (int z = 0; z < ksplit; ++z) {
+    const float4* src = reinterpret_cast<const float4*>(part + z * stride + j * e.kp + c0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 v = src[q];
+      T[4 * q] += v.x; T[4 * q + 1] += v.y; T[4 * q + 2] += v.z; T[4 * q + 3] += v.w;
+    }
+  }
+  epilogue_k1(e, j, c0, T, static_cast<int>(threadIdx.x));
+}
+
+__global__ void __launch_bounds__(128) k_k2_finish(const float* __restrict__ part, int ksplit,
+                                                    int64_t stride, int64_t rows, EpiParams e) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * 32 + threadIdx.x;
+  const int c0 = 16 * static_cast<int>(blockIdx.y * 4 + threadIdx.y);
+  const int comp = blockIdx.z;
+  if (c0 >= e.kp || i >= e.n) return;
+  float T[16];
+#pragma unroll
+  for (int t = 0; t < 16; ++t) T[t] = 0.f;
+  for (int z = 0; z < ksplit; ++z) {
+    const float4* src = reinterpret_cast<const float4*>(
+        part + z * stride + (static_cast<int64_t>(comp) * rows + i) * e.kp + c0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 v = src[q];
+      T[4 * q] += v.x; T[4 * q + 1] += v.y; T[4 * q + 2] += v.z; T[4 * q + 3] += v.w;
+    }
+  }
+  epilogue_k2(e, i, comp, c0, T);
+}
 
 // ------------------------------------------------------------ helper kernels
 
@@ -327,17 +375,72 @@ __global__ void k_prep_s_from_b(const float* __restrict__ b, int64_t ldb,
 // Widest right-hand-side block of one launch: two B ring slots (one stage of
 // all split terms each) next to the genotype ring must fit the 227 KB of
 // dynamic shared memory, and N <= 256.
+// The split terms always sit side by side in N (nsplit * kp <= 256):
+// accumulating them one after another into one accumulator loses accuracy
+// on long chains (measured 6.5e-4 relative at n = 50,000, m = 500,000).
 static inline int max_kp_for(const coherit_geno* h, int nsplit) {
   const int budget = h->smem_optin - 4096 - kBarrierBytes - kRG * kStageBlocks * kBlockBytes;
   const int per_col = 2 * kStageBlocks * nsplit * kPanel * 2;
-  return std::min(256, (budget / per_col) / 16 * 16);
+  return std::min((256 / nsplit) / 16 * 16, (budget / per_col) / 16 * 16);
 }
 
+// Split K.  Longest chain one accumulator takes: 512 stages (65,536 K values,
+// 4,096 MMAs of K = 16).  Measured on GB300 at n = 50,000: K2 chains over
+// 62,500 SNPs stay within 2e-6 relative of FP64, over 500,000 SNPs 4.5e-5.
+// Short problems are split further, down to 16 stages a share, until the
+// grid holds about two waves.
+constexpr int64_t kMaxChainStages = 512;
+constexpr int64_t kMinShareStages = 16;
+
+static int split_count(int64_t stages, int64_t ctas, int64_t target_ctas) {
+  int64_t P = std::max<int64_t>(1, (stages + kMaxChainStages - 1) / kMaxChainStages);
+  if (ctas * P < target_ctas) {
+    const int64_t want = (target_ctas + ctas - 1) / ctas;
+    P = std::max(P, std::min(want, stages / kMinShareStages));
+  }
+  return static_cast<int>(std::min<int64_t>(P, 1024));
+}
+
+struct SplitPlan {
+  int k1, k2;     // K shares of K1 and of K2
+  int64_t nr;     // K2 component blocks (G when stacked, else 1)
+};
+
+static SplitPlan split_plan(const coherit_geno* h, bool stacked, int64_t target_ctas) {
+  SplitPlan s;
+  s.nr = stacked ? h->G : 1;
+  s.k1 = split_count(h->n_chunks / kStageBlocks, h->n_ttiles, target_ctas);
+  int64_t stages2 = h->n_panels / kStageBlocks;
+  if (stacked) {
+    stages2 = 0;
+    for (int g = 0; g < h->G; ++g)
+      stages2 = std::max<int64_t>(
+          stages2, (h->comp_slot_start[g + 1] - h->comp_slot_start[g]) / kPanel / kStageBlocks);
+  }
+  s.k2 = split_count(stages2, h->n_stiles * s.nr, target_ctas);
+  return s;
+}
+
+// Grid size that fills about two waves of the operator kernel.
+static int64_t target_ctas(const coherit_geno* h) { return 4LL * std::max(h->sm_count, 1); }
+
 struct WsLayout {
-  size_t vt, sbuf, cs_part, cs, rbuf, vmiss, sf32, total;
+  size_t vt, sbuf, cs_part, cs, rbuf, vmiss, sf32, part, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+// Split-K partial buffer (floats per column): the larger of K1's and K2's,
+// over both output modes.  K1's partials are consumed before K2 runs.
+static int64_t part_rows_needed(const coherit_geno* h) {
+  int64_t rows = 0;
+  for (int stacked = 0; stacked < 2; ++stacked) {
+    const SplitPlan s = split_plan(h, stacked != 0, target_ctas(h));
+    if (s.k1 > 1) rows = std::max<int64_t>(rows, s.k1 * h->m_pad);
+    if (s.k2 > 1) rows = std::max<int64_t>(rows, s.k2 * s.nr * h->n_pad);
+  }
+  return rows;
+}
 
 static WsLayout ws_layout(const coherit_geno* h, int kp, int nsplit) {
   WsLayout L;
@@ -359,6 +462,8 @@ static WsLayout ws_layout(const coherit_geno* h, int kp, int nsplit) {
     L.sf32 = off;
     off = align256(off + static_cast<size_t>(h->m_pad) * kp * 4);
   }
+  L.part = off;
+  off = align256(off + static_cast<size_t>(part_rows_needed(h)) * kp * 4);
   L.total = off;
   return L;
 }
@@ -428,9 +533,9 @@ struct TcLaunchCfg {
   size_t smem;
 };
 
-// Accumulator: NSPLIT*kp columns when the split terms sit side by side in N
-// (one MMA per K step, N <= 256), kp columns otherwise.  The A ring takes the
-// remaining tensor-memory columns (3..8 slots of 32 * kStageBlocks).
+// Accumulator: NSPLIT*kp columns, the split terms side by side in N (one MMA
+// per K step, N <= 256).  The A ring takes the remaining tensor-memory
+// columns (3..6 slots of 32 * kStageBlocks).
 static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
   TcLaunchCfg c;
   c.side = nsplit > 1 && nsplit * kp <= 256;
@@ -471,8 +576,9 @@ static int launch_tc(int nsplit, bool side, dim3 grid, size_t smem, cudaStream_t
     return COHERIT_OK;
   };
   if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false>);
-  if (nsplit == 2) return side ? go(k_tc_op<IS_K1, 2, true>) : go(k_tc_op<IS_K1, 2, false>);
-  return side ? go(k_tc_op<IS_K1, 3, true>) : go(k_tc_op<IS_K1, 3, false>);
+  CO_CHECK(side, COHERIT_E_SHAPE, "split terms must fit side by side (nsplit * kp <= 256)");
+  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true>);
+  return go(k_tc_op<IS_K1, 3, true>);
 }
 
 // Column-block width when k exceeds what one launch holds (each block
@@ -562,6 +668,9 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   e.rbuf = rbuf;
   const int nr = e.stacked ? h->G : 1;
   CO_CUDA(cudaMemsetAsync(rbuf, 0, sizeof(double) * nr * kp, st));
+  const SplitPlan sp = split_plan(h, e.stacked != 0, target_ctas(h));
+  float* part = reinterpret_cast<float*>(ws + L.part);
+  const unsigned col_blocks = static_cast<unsigned>((kp / 16 + 3) / 4);
 
   const TcLaunchCfg cfg = tc_config(h, kp, nsplit);
   TcParams p;
@@ -589,9 +698,19 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
     p.geno = h->geno_t;
     p.bsrc = reinterpret_cast<const uint8_t*>(vt);
     p.e = e;
-    rc = launch_tc<true>(nsplit, cfg.side, dim3(static_cast<unsigned>(h->n_ttiles), 1), cfg.smem,
-                         st, p);
+    p.ksplit = sp.k1;
+    p.part = sp.k1 > 1 ? part : nullptr;
+    p.part_stride = h->m_pad * kp;
+    p.part_rows = h->m_pad;
+    rc = launch_tc<true>(nsplit, cfg.side,
+                         dim3(static_cast<unsigned>(h->n_ttiles), 1, static_cast<unsigned>(sp.k1)),
+                         cfg.smem, st, p);
     if (rc != COHERIT_OK) return rc;
+    if (sp.k1 > 1) {
+      k_k1_finish<<<dim3(static_cast<unsigned>(h->m_pad / 32), col_blocks), dim3(32, 4), 0, st>>>(
+          part, sp.k1, p.part_stride, e); note_launch();
+      CO_CUDA(cudaGetLastError());
+    }
     if (d.xtv) return COHERIT_OK;
   } else {
     // Z b: S = inv_sd * b computed directly.
@@ -603,10 +722,20 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   p.bsrc = reinterpret_cast<const uint8_t*>(sbuf);
   p.comp_slot_start = h->d_comp_slot_start;
   p.e = e;
+  p.ksplit = sp.k2;
+  p.part = sp.k2 > 1 ? part : nullptr;
+  p.part_stride = static_cast<int64_t>(nr) * h->n_pad * kp;
+  p.part_rows = h->n_pad;
   rc = launch_tc<false>(nsplit, cfg.side,
-                        dim3(static_cast<unsigned>(h->n_stiles), static_cast<unsigned>(nr)),
+                        dim3(static_cast<unsigned>(h->n_stiles), static_cast<unsigned>(nr),
+                             static_cast<unsigned>(sp.k2)),
                         cfg.smem, st, p);
   if (rc != COHERIT_OK) return rc;
+  if (sp.k2 > 1) {
+    k_k2_finish<<<dim3(static_cast<unsigned>(h->n_pad / 32), col_blocks, static_cast<unsigned>(nr)),
+                  dim3(32, 4), 0, st>>>(part, sp.k2, p.part_stride, h->n_pad, e); note_launch();
+    CO_CUDA(cudaGetLastError());
+  }
   if (sf32 != nullptr) {
     k_rowcorr<<<static_cast<unsigned>((h->n + 7) / 8), 256, 0, st>>>(h->d_csr_off, h->d_csr_idx,
                                                                       h->n, e); note_launch();

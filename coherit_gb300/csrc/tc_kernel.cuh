@@ -16,6 +16,13 @@
 //            epilogue sums the column groups); otherwise each term is its own
 //            MMA into one accumulator.
 // Barrier arrivals from the decoders are per warp.  All waits are bounded.
+//
+// Split K: with p.ksplit > 1 the CTA at blockIdx.z walks only its share of
+// the stages and writes its FP32 partial (split terms summed) to p.part; a
+// finish kernel sums the partials and applies the epilogue.  Tensor-core FP32
+// accumulation loses precision over very long chains (relative error grows
+// with the number of MMAs into one accumulator), so the host bounds every
+// chain this way.
 
 template <bool IS_K1, int NSPLIT, bool SIDE>
 __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __grid_constant__ TcParams p) {
@@ -42,12 +49,14 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
 
   const int64_t tile = blockIdx.x;
   const int comp = blockIdx.y;
-  int64_t nch;
+  const int zsplit = blockIdx.z;
+  int64_t ntot;
   const uint8_t* gbase;
   const uint8_t* bbase;
-  // nch counts pipeline stages of kStageBlocks consecutive 2 KB blocks.
+  const int64_t stage_b_bytes = kStageBlocks * p.b_chunk_bytes;
+  // Stages of kStageBlocks consecutive 2 KB blocks along K.
   if (IS_K1) {
-    nch = p.n_chunks / kStageBlocks;
+    ntot = p.n_chunks / kStageBlocks;
     gbase = p.geno + tile * p.n_chunks * kBlockBytes;
     bbase = p.bsrc;
   } else {
@@ -56,11 +65,15 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
       p0 = p.comp_slot_start[comp] / kPanel;
       p1 = p.comp_slot_start[comp + 1] / kPanel;
     }
-    nch = (p1 - p0) / kStageBlocks;
+    ntot = (p1 - p0) / kStageBlocks;
     gbase = p.geno + (tile * p.n_panels + p0) * kBlockBytes;
     bbase = p.bsrc + p0 * p.b_chunk_bytes;
   }
-  const int64_t stage_b_bytes = kStageBlocks * p.b_chunk_bytes;
+  // This CTA's share of the K stages: [s0, s0 + nch).
+  const int64_t s0 = ntot * zsplit / p.ksplit;
+  const int64_t nch = ntot * (zsplit + 1) / p.ksplit - s0;
+  gbase += s0 * (kStageBlocks * kBlockBytes);
+  bbase += s0 * stage_b_bytes;
 
   if (threadIdx.x == 0) {
     // Each chunk is consumed and decoded by one set of 4 warps.
@@ -87,6 +100,8 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
   {
     const uint32_t acc_need = SIDE ? static_cast<uint32_t>(NSPLIT * e.kp) : static_cast<uint32_t>(e.kp);
     const bool cfg_ok = p.RA >= 1 && p.RA <= kMaxRA && p.RB >= 1 && p.RB <= kMaxRB &&
+                        p.ksplit >= 1 && static_cast<int>(gridDim.z) == p.ksplit &&
+                        (p.ksplit == 1 || p.part != nullptr) &&
                         acc_need <= p.acc_cols && (p.acc_cols & 31u) == 0 &&
                         p.acc_cols + static_cast<uint32_t>(p.RA) * 32u * kStageBlocks <= p.tmem_cols &&
                         p.tmem_cols >= 32 && p.tmem_cols <= 512 &&
@@ -262,7 +277,15 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
 #pragma unroll
           for (int i = 0; i < 16; ++i) T[i] = 0.f;
         }
-        if (IS_K1) {
+        if (p.ksplit > 1) {
+          // Partial of this K share: row (K1: slot; K2: component, sample).
+          const int64_t prow = IS_K1 ? rowid : static_cast<int64_t>(comp) * p.part_rows + rowid;
+          float4* dst = reinterpret_cast<float4*>(
+              p.part + zsplit * p.part_stride + prow * kp + c0);
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            dst[q] = make_float4(T[4 * q], T[4 * q + 1], T[4 * q + 2], T[4 * q + 3]);
+        } else if (IS_K1) {
           epilogue_k1(e, rowid, c0, T, lane);
         } else {
           epilogue_k2(e, rowid, comp, c0, T);

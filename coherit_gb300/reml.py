@@ -677,6 +677,50 @@ def _apply_projected_step(param, step_dir, alpha, *, n_genetic=None, genetic_zer
 
 # --------------------------------------------------------------------- fit
 
+def _probe_setup(probe_cache, K_mvs, n, *, seed, Vrand, slq_samples, slq_m, residual_free, E,
+                  stacked_kv, slq_probes, dev):
+    """Phenotype-independent probe work of a fit: K_i applied to the trace
+    probes and the affine SLQ cache, reused when ``probe_cache`` holds them for
+    the same operators, sample count, seed and probe shapes (reml.py:62-73)."""
+    G = len(K_mvs)
+    n_trace = 0 if Vrand is None else int(Vrand.shape[1])
+    signature = (K_mvs, n, int(seed), n_trace, int(slq_samples), int(slq_m),
+                 bool(residual_free), str(dev))
+    hit = probe_cache is not None and probe_cache.signature == signature
+    KVrand = probe_cache.kvrand_stack if (hit and Vrand is not None) else None
+    if Vrand is not None and KVrand is None:
+        KVrand = stacked_kv(Vrand) if stacked_kv is not None else torch.stack(
+            [_as_col(mv(Vrand)) for mv in K_mvs])
+    affine = probe_cache.affine_slq if hit else None
+    if G == 1 and E == 1 and residual_free and affine is None:
+        probes = None if slq_probes is None else torch.as_tensor(
+            slq_probes, dtype=torch.float32).to(dev)
+        key_slq = (int(seed) + 2026) * 3 + 2
+        affine = _build_affine_slq_cache(K_mvs[0], n, key_slq, nsamples=slq_samples, m=slq_m,
+                                         probes=probes, device=dev)
+    if probe_cache is not None:
+        probe_cache.signature = signature
+        probe_cache.kvrand_stack = KVrand
+        probe_cache.affine_slq = affine
+    return KVrand, affine
+
+
+def prime_probe_cache(probe_cache: REMLProbeCache, K_mv: Callable, n: int, *, seed: int = 0,
+                      slq_samples: int = 30, slq_m: int = 30, slq_probes=None, device=None):
+    """Fill ``probe_cache`` for single-GRM strict fits on ``(K_mv,)``.
+
+    A later ``fit_reml(y, K_mvs, ...)`` with the same tuple object
+    ``K_mvs == (K_mv,)``, ``n``, ``seed`` and probe shapes reuses the cached
+    affine SLQ data instead of rebuilding it; returns that tuple."""
+    dev = torch.device(device) if device is not None else torch.device(
+        "cuda", torch.cuda.current_device())
+    K_mvs = (K_mv,)
+    _probe_setup(probe_cache, K_mvs, int(n), seed=seed, Vrand=None, slq_samples=slq_samples,
+                 slq_m=slq_m, residual_free=True, E=1, stacked_kv=None, slq_probes=slq_probes,
+                 dev=dev)
+    return K_mvs
+
+
 def fit_reml(
     y,
     K_mvs: Sequence[Callable],
@@ -864,22 +908,11 @@ def fit_reml(
                 if torch.as_tensor(d).ndim == 0 else torch.as_tensor(d, dtype=torch.float32).to(dev)
                 for d in diag_list])
 
-    signature = (K_mvs, n, int(seed), int(n_trace), int(slq_samples), int(slq_m),
-                 residual_diag_stack is None, str(dev))
-    hit = probe_cache is not None and probe_cache.signature == signature
-    KVrand = probe_cache.kvrand_stack if (hit and use_trace_probes) else None
-    if use_trace_probes and KVrand is None:
-        KVrand = stacked_kv(Vrand) if stacked_kv is not None else torch.stack(
-            [_as_col(mv(Vrand)) for mv in K_mvs])
-    affine = probe_cache.affine_slq if hit else None
+    KVrand, affine = _probe_setup(probe_cache, K_mvs, n, seed=seed, Vrand=Vrand,
+                                  slq_samples=slq_samples, slq_m=slq_m,
+                                  residual_free=residual_diag_stack is None, E=E,
+                                  stacked_kv=stacked_kv, slq_probes=slq_probes, dev=dev)
     slq_probes_t = None if slq_probes is None else torch.as_tensor(slq_probes, dtype=torch.float32).to(dev)
-    if G == 1 and E == 1 and residual_diag_stack is None and affine is None:
-        affine = _build_affine_slq_cache(K_mvs[0], n, key_slq, nsamples=slq_samples, m=slq_m,
-                                         probes=slq_probes_t, device=dev)
-    if probe_cache is not None:
-        probe_cache.signature = signature
-        probe_cache.kvrand_stack = KVrand
-        probe_cache.affine_slq = affine
 
     if slq_precond_conf is None:
         slq_precond_conf = precond_conf
@@ -1068,4 +1101,5 @@ def fit_reml(
     return param, history
 
 
-__all__ = ["fit_reml", "standardize_response", "REMLProbeCache", "AffineSLQCache"]
+__all__ = ["fit_reml", "standardize_response", "REMLProbeCache", "AffineSLQCache",
+           "prime_probe_cache"]

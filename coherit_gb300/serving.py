@@ -37,12 +37,11 @@ import torch
 
 from . import _lib
 from .geno_stream import GenoBlockStreamer
-from .reml import fit_reml
+from .reml import REMLProbeCache, fit_reml, prime_probe_cache
 
 # Widest right-hand-side block one batched launch takes per precision: the
-# B-operand ring of the tensor-core operator must hold two pipeline stages of
-# all split terms in shared memory (227 KB per CTA on GB300).
-_MAX_BATCH_COLS = {"bf16x3": 112, "bf16x2": 176, "bf16x1": 256}
+# split terms of all columns sit side by side in one MMA (N <= 256).
+_MAX_BATCH_COLS = {"bf16x3": 80, "bf16x2": 128, "bf16x1": 256}
 
 
 @dataclasses.dataclass
@@ -77,6 +76,14 @@ class _Request:
     idx: Optional[torch.Tensor] = None
     eff: float = 0.0
     atom: float = 0.0
+
+
+@dataclasses.dataclass
+class _Target:
+    """Where an operator application goes: stats slot, subset rows, row count."""
+    slot: int
+    idx: Optional[torch.Tensor]
+    n_sub: int
 
 
 class _Op:
@@ -121,7 +128,7 @@ class _Batcher:
             self.n_active += delta
             self.cv.notify_all()
 
-    def apply(self, req: _Request, V: torch.Tensor, scale: float, theta_e) -> torch.Tensor:
+    def apply(self, req, V: torch.Tensor, scale: float, theta_e) -> torch.Tensor:
         vec = V.ndim == 1
         V2 = (V[:, None] if vec else V).to(torch.float32).contiguous()
         if V2.shape[0] != req.n_sub:
@@ -211,6 +218,23 @@ class _Batcher:
             op.out = (blk if op.req.idx is None else blk[op.req.idx]).contiguous()
 
 
+def _init_device_linalg(dev) -> None:
+    """Run each device linear-algebra routine a fit uses once on this thread.
+
+    PyTorch loads its CUDA linear-algebra backend lazily on first use, and
+    that first use is not safe to race from several threads ("lazy wrapper
+    should be called at most once"); the worker threads start only after
+    this has run."""
+    for dt in (torch.float32, torch.float64):
+        A = torch.eye(4, dtype=dt, device=dev) * 2.0
+        L, _ = torch.linalg.cholesky_ex(A)
+        torch.linalg.cholesky(A)
+        torch.cholesky_solve(torch.ones((4, 1), dtype=dt, device=dev), L)
+        torch.linalg.eigh(A)
+        torch.linalg.qr(A)
+    torch.cuda.synchronize(dev)
+
+
 class REMLServer:
     """Serve single-GRM REML fits of many phenotypes over one resident matrix.
 
@@ -246,12 +270,23 @@ class REMLServer:
             _lib.check(_lib.load().coherit_geno_compute_stats(
                 streamer.handle, self.max_active, None, None, None, None, _lib.stream_ptr()),
                 "reserve stats slots")
+        _init_device_linalg(streamer.dev)
         cols = _MAX_BATCH_COLS[precision] if max_batch_cols is None else int(max_batch_cols)
         self.batcher = _Batcher(streamer, precision, batch_window_s, cols, self._lib_lock)
         self.fit_kwargs = dict(n_rand_vec=30, maxiter=500, minq_iter=20, slq_samples=30,
                                slq_m=30, pcg_tol=1e-5, verbose=False)
         if fit_kwargs:
             self.fit_kwargs.update(fit_kwargs)
+        # Full-cohort requests share one operator (slot 0) and so one set of
+        # phenotype-independent probe work (the affine SLQ Lanczos data),
+        # built by the first such request and reused by the rest, as the
+        # single-fit path reuses it across phenotypes (reml.py:62-73).
+        self._full = _Target(slot=0, idx=None, n_sub=streamer.n)
+        inv_full = 1.0 / streamer._eff_m_host if streamer._eff_m_host > 0 else 1.0
+        self._full_K = lambda V: self.batcher.apply(self._full, V, inv_full, None)
+        self._full_cache = REMLProbeCache()
+        self._full_cache_key = None
+        self._full_cache_lock = threading.Lock()
         self._cv = threading.Condition()
         self._waiting: deque[_Request] = deque()
         self._active = 0
@@ -281,11 +316,18 @@ class REMLServer:
             n_sub = int(mask.sum())
             if n_sub == 0:
                 raise ValueError("sample_mask selects no samples")
-        y = np.asarray(y, dtype=np.float32).reshape(-1)
-        if y.size != n_sub:
-            raise ValueError(f"phenotype has {y.size} entries, the sample set has {n_sub}")
+        # Host arrays are copied to the device by the fit; device tensors stay.
+        if isinstance(y, torch.Tensor):
+            y = y.detach().to(self.st.dev, torch.float32).reshape(-1)
+        else:
+            y = np.asarray(y, dtype=np.float32).reshape(-1)
+        if y.shape[0] != n_sub:
+            raise ValueError(f"phenotype has {y.shape[0]} entries, the sample set has {n_sub}")
         if covar is not None:
-            covar = np.asarray(covar, dtype=np.float32)
+            if isinstance(covar, torch.Tensor):
+                covar = covar.detach().to(self.st.dev, torch.float32)
+            else:
+                covar = np.asarray(covar, dtype=np.float32)
             if covar.ndim == 1:
                 covar = covar[:, None]
             if covar.shape[0] != n_sub:
@@ -394,6 +436,17 @@ class REMLServer:
         req.eff, req.atom = float(et.value), float(at.value)
         req.idx = torch.as_tensor(np.flatnonzero(req.mask), dtype=torch.long, device=st.dev)
 
+    def _shared_cache_key(self, req: _Request):
+        """(seed, slq_samples, slq_m) when the request may use the shared
+        full-cohort probe cache, else None (subset requests, caller-supplied
+        probes or cache, other optimizers)."""
+        kw = req.fit_kwargs
+        if req.mask is not None or kw.get("slq_probes") is not None or "probe_cache" in kw:
+            return None
+        if kw.get("optimizer", "strict") != "strict" or kw.get("slq_mode", "raw") != "raw":
+            return None
+        return (int(kw.get("seed", 0)), int(kw.get("slq_samples", 30)), int(kw.get("slq_m", 30)))
+
     def _run(self, req: _Request) -> None:
         start = time.perf_counter()
         try:
@@ -402,17 +455,32 @@ class REMLServer:
             b = self.batcher
             inv_eff = 1.0 / req.eff if req.eff > 0 else 1.0
 
-            def K(V):
-                return b.apply(req, V, inv_eff, None)
-
             def whv(theta_g, theta_e, V):
                 tg = float(np.asarray(theta_g, dtype=np.float64).reshape(-1)[0])
                 return b.apply(req, V, tg * inv_eff, float(theta_e))
 
+            kw = dict(req.fit_kwargs)
+            cache_key = self._shared_cache_key(req)
+            shared = False
+            if cache_key is not None:
+                # The first full-cohort request builds the cache (its
+                # applications batch with the other fits); later ones wait
+                # here and reuse it.  Another probe setting keeps its own.
+                with self._full_cache_lock:
+                    if self._full_cache_key is None:
+                        prime_probe_cache(self._full_cache, self._full_K, req.n_sub,
+                                          seed=cache_key[0], slq_samples=cache_key[1],
+                                          slq_m=cache_key[2], device=self.st.dev)
+                        self._full_cache_key = cache_key
+                    shared = self._full_cache_key == cache_key
+            if shared:
+                K_mvs = [self._full_K]
+                kw["probe_cache"] = self._full_cache
+            else:
+                K_mvs = [lambda V: b.apply(req, V, inv_eff, None)]
             diag = torch.tensor(req.atom, dtype=torch.float32, device=self.st.dev)
-            param, hist, d = fit_reml(req.y, [K], [diag], req.covar, weighted_hv=whv,
-                                      device=self.st.dev, return_diagnostics=True,
-                                      **req.fit_kwargs)
+            param, hist, d = fit_reml(req.y, K_mvs, [diag], req.covar, weighted_hv=whv,
+                                      device=self.st.dev, return_diagnostics=True, **kw)
             gen = float(np.dot(param[:1], np.asarray(d.get("genetic_trace_atoms", [1.0]))))
             res = float(np.dot(param[1:], np.asarray(d.get("residual_trace_atoms", [1.0]))))
             out = ServeResult(request_id=req.rid, var_components=np.asarray(param),

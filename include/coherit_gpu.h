@@ -175,8 +175,9 @@ int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t preci
  * stream of a process that runs several solves at once.
  *   - tensor-core precisions only (COHERIT_PREC_FP32 -> COHERIT_E_UNSUPPORTED);
  *   - the workspace of one launch, about 2*nsplit*kp*(n_pad + m_pad) bytes
- *     (+ 8*kp*m_pad with missing genotypes; kp = columns per launch rounded
- *     up to 16), must fit 64 MiB, else COHERIT_E_SHAPE;
+ *     (+ 8*kp*m_pad with missing genotypes, + the split-K partials; kp =
+ *     columns per launch rounded up to 16), must fit 64 MiB, else
+ *     COHERIT_E_SHAPE;
  *   - the handle's device must be current; the first call on a device
  *     resolves the array's address (cudaGetSymbolAddress), so make it before
  *     any stream capture;
