@@ -288,7 +288,8 @@ def run_ours(args, wl):
     # Host copies for the end-to-end leg (pinned, as a serving front end holds them).
     ys_host = [y.cpu().pin_memory() for y in ys]
     Xs_host = [X.cpu().pin_memory() for X in Xs]
-    srv = REMLServer(st, max_active=R, precision=args.precision, fit_kwargs=fit_kwargs(wl))
+    srv = REMLServer(st, max_active=R, precision=args.precision, fit_kwargs=fit_kwargs(wl),
+                     batch_window_s=args.batch_window)
 
     for _ in range(args.warmup):
         serve_step(srv, ys, Xs, host=False)
@@ -463,6 +464,51 @@ def run_reference(args, wl):
     }
 
 
+def run_operator_only(args, wl):
+    """Operator micro-benchmark: W + K applications of K V at width
+    ``--operator`` on the workload's genotypes (or --n/--m), CUDA-event timed
+    on the launching stream.  Used for kernel profiles."""
+    import dataclasses
+
+    import torch
+
+    from coherit_gb300 import _lib
+
+    if args.n or args.m:
+        wl = dataclasses.replace(wl, name=f"n{args.n or wl.n}_m{args.m or wl.m}",
+                                 n=args.n or wl.n, m=args.m or wl.m, components=None)
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    hbm_peak, tensor_peak, peak_src = _peaks()
+    st = build_problem(wl, dev)
+    k = args.operator
+    V = torch.randn(st.n, k, device=dev)
+    for _ in range(args.warmup):
+        st.kv(V, precision=args.precision)
+    torch.cuda.synchronize()
+    l0 = _lib.load().coherit_launch_count()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        st.kv(V, precision=args.precision)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = _lib.load().coherit_launch_count() - l0
+    alg_bytes = st.n * ((st.m + 3) // 4) + 8 * st.n * k + 8 * st.m
+    st.check()
+    st.close()
+    return {"metric": "genotype operator application time", "value": round(ms, 4), "unit": "ms",
+            "higher_is_better": False, "steps": args.steps, "warmup": args.warmup,
+            "precision": args.precision,
+            "config": {"workload": wl.name, "n": wl.n, "m": wl.m, "k": k},
+            "hbm_gbs": round(alg_bytes / (ms * 1e-3) / 1e9, 1),
+            "tensor_tflops": round(4.0 * wl.n * wl.m * k / (ms * 1e-3) / 1e12, 1),
+            "gpu_launches": int(launches), "peak_source": peak_src}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -473,6 +519,8 @@ def main():
     ap.add_argument("--precision", default="bf16x3")
     ap.add_argument("--requests", type=int, default=8,
                     help="concurrent fit requests per step (the serving batch)")
+    ap.add_argument("--batch-window", type=float, default=0.01,
+                    help="seconds the batcher waits for the other active fits")
     ap.add_argument("--single-fits", type=int, default=3,
                     help="fits timed one at a time for the single-fit comparison")
     ap.add_argument("--no-single", action="store_true")
@@ -484,11 +532,20 @@ def main():
                     help="operator applications per fit assumed by the reference arm")
     ap.add_argument("--ref-cols", type=float, default=368.0,
                     help="right-hand-side columns per fit assumed by the reference arm")
+    ap.add_argument("--operator", type=int, default=0, metavar="K",
+                    help="time bare operator applications of width K instead of fits")
+    ap.add_argument("--n", type=int, default=0, help="with --operator: samples")
+    ap.add_argument("--m", type=int, default=0, help="with --operator: SNPs")
     args = ap.parse_args()
     from coherit_gb300.configs import WORKLOADS
 
     wl = WORKLOADS[args.config]
-    out = run_reference(args, wl) if args.impl == "reference" else run_ours(args, wl)
+    if args.operator > 0:
+        out = run_operator_only(args, wl)
+    elif args.impl == "reference":
+        out = run_reference(args, wl)
+    else:
+        out = run_ours(args, wl)
     if out is not None:
         print(json.dumps(out), flush=True)
 

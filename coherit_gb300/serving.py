@@ -247,7 +247,7 @@ class REMLServer:
 
     def __init__(self, streamer: GenoBlockStreamer, *, max_active: int = 8,
                  hbm_budget_bytes: float | None = None, precision: str = "bf16x3",
-                 batch_window_s: float = 0.002, max_batch_cols: int | None = None,
+                 batch_window_s: float = 0.01, max_batch_cols: int | None = None,
                  fit_kwargs: dict | None = None):
         if streamer.n_components != 1:
             raise ValueError("REMLServer serves single-GRM fits (one genotype component).")
