@@ -28,17 +28,17 @@
 
 namespace coherit {
 
-// Decoder warp sets.  Two sets let a 32-column bf16x3 block (96-column
-// accumulator + 2-slot A ring) fit 256 tensor-memory columns, i.e. two CTAs
-// per SM; measured at n = 50,000, m = 500,000: 10.8 ms per application at
-// k = 32 (17.6 ms with three sets, which need a third slot and 512 columns),
-// unchanged at k <= 16 and k >= 48.
+// Decoder warp sets (stages decoded concurrently).
 #ifndef COHERIT_SETS
-#define COHERIT_SETS 2
+#define COHERIT_SETS 3
 #endif
-// A-ring depth floor: at least one slot per decoder set.
+// A-ring depth floor: at least one slot per decoder set, and never fewer
+// than 3.  A 2-slot ring with two CTAs per SM (two decoder sets, 32-column
+// bf16x3 blocks) gave results 5e-3 off at n = 50,000, m = 500,000, while the
+// same ring with one CTA per SM and 3-slot rings with two CTAs per SM were
+// exact; the cause was not found, so no launch uses fewer than 3 slots.
 #ifndef COHERIT_TMEM_MIN_SLOTS
-#define COHERIT_TMEM_MIN_SLOTS COHERIT_SETS
+#define COHERIT_TMEM_MIN_SLOTS (COHERIT_SETS > 3 ? COHERIT_SETS : 3)
 #endif
 constexpr int kSets = COHERIT_SETS;  // decoder warp sets (stages in flight through the A ring)
 constexpr int kThreads = 32 * (3 + 4 * kSets);

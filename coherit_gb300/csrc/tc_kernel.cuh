@@ -102,7 +102,8 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
     // RA >= kSets: a decoder set never waits on an A slot whose previous use
     // is more than one barrier phase behind (parity waits are ambiguous
     // beyond one phase).
-    const bool cfg_ok = p.RA >= kSets && p.RA <= kMaxRA && p.RB >= 1 && p.RB <= kMaxRB &&
+    const bool cfg_ok = p.RA >= kSets && p.RA >= 3 && p.RA <= kMaxRA && p.RB >= 1 &&
+                        p.RB <= kMaxRB &&
                         p.ksplit >= 1 && static_cast<int>(gridDim.z) == p.ksplit &&
                         (p.ksplit == 1 || p.part != nullptr) &&
                         acc_need <= p.acc_cols && (p.acc_cols & 31u) == 0 &&

@@ -282,3 +282,9 @@ def test_accuracy_at_scale_vs_dense_fp64(cuda):
     # to the order of FP64 atomic additions in the rank-one term).
     wide = torch.cat([V, torch.randn((n, 74), generator=gen, device=dev)], dim=1)
     assert col_rel(st.kv(wide)[:, :6].cpu().numpy(), out) < 1e-6
+    # Every launch width (its own tensor-memory layout, two CTAs per SM at this
+    # size) agrees with 16-column launches.
+    ref16 = torch.cat([st.kv(wide[:, i:i + 16].contiguous()) for i in range(0, 80, 16)], dim=1)
+    for k in (20, 32, 48, 64, 80):
+        got = st.kv(wide[:, :k].contiguous())
+        assert col_rel(got.cpu().numpy(), ref16[:, :k].cpu().numpy()) < 1e-6, k
