@@ -238,8 +238,9 @@ def operator_roofline(st, k, hbm_peak, tensor_peak, reps=10):
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "operator_traffic.json")
     if os.path.exists(tpath):
+        kp = (k + 15) // 16 * 16
         with open(tpath) as f:
-            traffic = json.load(f).get(f"{st.n}x{st.m}x{k}")
+            traffic = json.load(f).get(f"{st.n}x{st.m}x{kp}")
     hbm_frac, ten_frac = gbs / hbm_peak, tfs / tensor_peak
     if ten_frac >= hbm_frac:
         roof = {"bound": "tensor", "achieved": round(tfs, 1), "peak": tensor_peak,
