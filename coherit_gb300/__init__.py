@@ -37,6 +37,8 @@ _EXPORTS: dict[str, str] = {
     "REMLServer": ".serving",
     "SmileBlockWeight": ".smile_block_w",
     "SmileBlockWeightedOperator": ".smile_block_w",
+    "SmileMultiBlockWeightedOperator": ".smile_block_w",
+    "ServeResult": ".serving",
 }
 
 __all__ = list(_EXPORTS)

@@ -77,6 +77,7 @@ _SIGNATURES = {
         C.c_int,
         [_p, _i32, _i32, _i32, _p, _i64, _i32, _p, _i32, _f32, _p, _p, _i64, _p],
     ),
+    "coherit_geno_extract_columns": (C.c_int, [_p, _i32, _p, _i32, _p, _i64, _p]),
     "coherit_geno_kv_noalloc": (
         C.c_int,
         [_p, _i32, _i32, _i32, _p, _i64, _i32, _p, _i32, _f32, _p, _p, _i64, _p],

@@ -149,6 +149,34 @@ __global__ void k_read_packed(uint8_t* __restrict__ out, const uint8_t* __restri
   out[idx] = static_cast<uint8_t>(byte);
 }
 
+// Standardised genotype columns: out[i, c] = (g - mean) * inv_sd of SNP
+// snp_idx[c] (cache order) for sample i, 0 for a missing genotype (mean
+// imputation), in FP32 with the reference's operation order
+// (geno_stream.py:2498-2501).  Threads of a warp take consecutive columns so
+// the writes of a row are coalesced.  An index outside [0, m) yields NaN.
+__global__ void k_extract_std(float* __restrict__ out, int64_t ldo, const int64_t* __restrict__ snp_idx,
+                              int32_t count, const uint8_t* __restrict__ geno_t, int64_t n,
+                              int64_t m, int64_t n_chunks, const int64_t* __restrict__ slot_of_snp,
+                              const float* __restrict__ mean, const float* __restrict__ inv) {
+  const int32_t c = static_cast<int32_t>(blockIdx.x) * 32 + threadIdx.x;
+  if (c >= count) return;
+  const int64_t snp = snp_idx[c];
+  const bool valid = snp >= 0 && snp < m;
+  const int64_t slot = valid ? slot_of_snp[snp] : 0;
+  const float mu = mean[slot];
+  const float iv = inv[slot];
+  const uint8_t* tile = geno_t + (slot / kTile) * n_chunks * kBlockBytes + (slot % kTile) * kRowBytes;
+  for (int64_t i = static_cast<int64_t>(blockIdx.y) * blockDim.y + threadIdx.y; i < n;
+       i += static_cast<int64_t>(gridDim.y) * blockDim.y) {
+    const uint32_t* row = reinterpret_cast<const uint32_t*>(tile + (i / kPanel) * kBlockBytes);
+    const int e = static_cast<int>(i % kPanel);
+    const uint32_t code = (row[row_word(e)] >> row_shift(e)) & 3u;
+    float z = code == 3u ? 0.f : __fmul_rn(__fsub_rn(static_cast<float>(code), mu), iv);
+    if (!valid) z = __int_as_float(0x7fc00000);
+    out[i * ldo + c] = z;
+  }
+}
+
 // ------------------------------------------------------------ statistics
 
 __device__ __forceinline__ void count_codes(uint32_t w, uint32_t mask, int& n1, int& n2,
@@ -801,6 +829,23 @@ int coherit_geno_read_packed(coherit_geno_t* h, int64_t snp_start, int32_t width
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaFree(d);
   if (e != cudaSuccess) return cuda_status(e, "read_packed");
+  return COHERIT_OK;
+}
+
+int coherit_geno_extract_columns(coherit_geno_t* h, int32_t slot, const int64_t* snp_idx,
+                                 int32_t count, float* out, int64_t ldo, void* stream) {
+  CO_CHECK(h != nullptr, COHERIT_E_CLOSED, "genotype handle is closed");
+  CO_CHECK(slot >= 0 && slot < static_cast<int32_t>(h->slots.size()) && h->slots[slot].used,
+           COHERIT_E_INDEX, "stats slot %d is not initialised", slot);
+  CO_CHECK(count >= 0 && ldo >= count, COHERIT_E_SHAPE, "need 0 <= count <= ldo");
+  if (count == 0) return COHERIT_OK;
+  CO_CHECK(snp_idx != nullptr && out != nullptr, COHERIT_E_SHAPE, "snp_idx and out are required");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned gy = static_cast<unsigned>(std::min<int64_t>((h->n + 7) / 8, 8192));
+  k_extract_std<<<dim3(static_cast<unsigned>((count + 31) / 32), gy), dim3(32, 8), 0, st>>>(
+      out, ldo, snp_idx, count, h->geno_t, h->n, h->m, h->n_chunks, h->d_slot_of_snp,
+      h->slots[slot].mean, h->slots[slot].inv); note_launch();
+  CO_CUDA(cudaGetLastError());
   return COHERIT_OK;
 }
 

@@ -568,6 +568,41 @@ class GenoBlockStreamer:
         return [torch.tensor(float(a), dtype=torch.float32, device=self.dev)
                 for a in self._component_mean_diag_atoms_host]
 
+    def set_standardization(self, means, inv_sds) -> None:
+        """Install externally supplied per-SNP means and inverse sds (cache
+        order), e.g. the training set's on a test streamer before prediction
+        (reml_model.py:275-279)."""
+        mo = np.ascontiguousarray(means, dtype=np.float32).reshape(-1)
+        io = np.ascontiguousarray(inv_sds, dtype=np.float32).reshape(-1)
+        if mo.size != self.m or io.size != self.m:
+            raise ValueError(f"standardization length mismatch: expected m={self.m}, "
+                             f"got means={mo.size}, inv={io.size}.")
+        self._standardization_override = (mo, io)
+        with torch.cuda.device(self.dev):
+            _lib.check(self._lib.coherit_geno_set_stats(
+                self._h(), 0, None, mo.ctypes.data, io.ctypes.data, _lib.stream_ptr()), "set stats")
+            self._refresh_stats()
+
+    def standardized_columns(self, snp_indices) -> torch.Tensor:
+        """Device FP32 (n, len(snp_indices)) standardised genotype columns
+        (cache SNP order; missing -> 0), computed from the resident matrix."""
+        idx = np.asarray(snp_indices, dtype=np.int64).reshape(-1)
+        if idx.size and (idx.min() < 0 or idx.max() >= self.m):
+            raise IndexError(f"SNP indices must lie in [0, {self.m}).")
+        out = torch.empty((self.n, idx.size), dtype=torch.float32, device=self.dev)
+        if idx.size == 0:
+            return out
+        idx_dev = torch.as_tensor(idx, device=self.dev)
+        _lib.check(self._lib.coherit_geno_extract_columns(
+            self._h(), 0, idx_dev.data_ptr(), int(idx.size), out.data_ptr(), int(idx.size),
+            _lib.stream_ptr()), "extract columns")
+        return out
+
+    def extract_standardized_columns(self, snp_indices: np.ndarray) -> np.ndarray:
+        """Host FP32 (n, len(snp_indices)) standardised columns
+        (geno_stream.py:2748-2760)."""
+        return self.standardized_columns(snp_indices).cpu().numpy()
+
     def exact_diag(self, *, target_block_bytes: int = 256 * 1024 * 1024) -> torch.Tensor:
         """Sample-wise diagonal of the GRM, cached (geno_stream.py:2780-2821)."""
         if self._exact_diag_dev is not None:

@@ -19,7 +19,8 @@ import numpy as np
 import torch
 
 from .geno_stream import GenoBlockStreamer
-from .precond import ProjectedCorePrecondConf, build_lowrank_basis
+from .precond import (ProjectedCorePrecondConf, build_lowrank_basis, make_precond,
+                      scalar_diag_from_precond_conf)
 from .reml import REMLProbeCache, fit_reml
 from .slq import default_workspace_bytes
 
@@ -56,6 +57,20 @@ class FitConfig:
     optimizer: str = "strict"
     precision: str = "bf16x3"
     sketch_precision: str = "bf16x1"
+    # SMILE block-weighted GRMs (reml_model.py:42-53): exactly one W mode.
+    smile_w_files: Sequence[str] | None = None
+    smile_w_file_groups: Sequence[Sequence[str]] | None = None
+    smile_weight_matrices: Sequence[np.ndarray] | None = None
+    smile_weight_matrix_groups: Sequence[Sequence[np.ndarray]] | None = None
+    smile_identity: bool = False
+    smile_identity_block_size: int | None = None
+    smile_normalization: str = "kernel_trace"
+    smile_diag_mode: str = "mean"
+    smile_strict_coverage: bool = True
+    smile_w_device_cache_bytes: float | None = None
+    smile_optimizer: str = "strict"
+    smile_scoring_step_tol: float = 1e-4
+    effect_pcg_tol: float = 1e-3
 
 
 @dataclasses.dataclass
@@ -68,6 +83,72 @@ class FitResult:
     diagnostics: dict | None = None
     final_loglik: float | None = None
     elapsed_sec: float = 0.0
+
+
+@dataclasses.dataclass
+class EffectEstimates:
+    """Post-REML effects on the standardised phenotype scale (reml_model.py:87-97)."""
+
+    fixed_effects: torch.Tensor
+    random_effect: torch.Tensor
+    random_effect_components: tuple
+    snp_effects: tuple
+    pcg_rel_res: float
+    pcg_iters: int
+    y_mean: float
+    y_scale: float
+
+
+@dataclasses.dataclass
+class PredictionEstimates:
+    """Test-set predictions from effect estimates (reml_model.py:100-109)."""
+
+    fixed_effect: torch.Tensor
+    random_effect: torch.Tensor
+    random_effect_components: tuple
+    y_pred_std: torch.Tensor
+    y_pred: torch.Tensor
+
+
+def _validate_dense_prediction_streamers(train, test) -> None:
+    """Train/test streamers must share the SNP set and call geometry
+    (reml_model.py:223-272)."""
+    if len(train) != len(test):
+        raise ValueError(
+            f"Prediction component count mismatch: expected {len(train)}, got {len(test)}.")
+    for idx, (a, b) in enumerate(zip(train, test)):
+        if int(a.m) != int(b.m):
+            raise ValueError(f"Prediction SNP count mismatch for component {idx}: "
+                             f"expected {int(a.m)}, got {int(b.m)}.")
+        if int(a._n_calls) != int(b._n_calls):
+            raise ValueError(f"Prediction call geometry mismatch for component {idx}: "
+                             f"expected {int(a._n_calls)} calls, got {int(b._n_calls)}.")
+        if not np.array_equal(a._call_snp_starts, b._call_snp_starts):
+            raise ValueError(f"Prediction SNP call starts mismatch for component {idx}.")
+        if not np.array_equal(a._call_true_widths, b._call_true_widths):
+            raise ValueError(f"Prediction SNP call widths mismatch for component {idx}.")
+        if a.n_components != b.n_components:
+            raise ValueError(f"Prediction component partition mismatch for component {idx}.")
+
+
+def _solve_small_spd(A: torch.Tensor, b: torch.Tensor, *, base_jitter=1e-6, max_tries=8):
+    """Host FP64 SPD solve with geometric jitter (reml_model.py:296-330)."""
+    A_np = np.asarray(0.5 * (A + A.T).double().cpu().numpy())
+    b_np = b.double().cpu().numpy().reshape(-1)
+    p = A_np.shape[0]
+    if p == 0:
+        raise ValueError("solve_small_spd requires a non-empty square matrix.")
+    scale = float(np.mean(np.abs(np.diag(A_np))))
+    if not np.isfinite(scale) or scale <= 0.0:
+        scale = 1.0
+    for k in range(max_tries):
+        try:
+            L = np.linalg.cholesky(A_np + base_jitter * scale * (10.0 ** k) * np.eye(p))
+        except np.linalg.LinAlgError:
+            continue
+        x = np.linalg.solve(L.T, np.linalg.solve(L, b_np))
+        return torch.as_tensor(x, dtype=torch.float32, device=A.device)
+    raise FloatingPointError("GLS system is not positive definite.")
 
 
 @dataclasses.dataclass(frozen=True)
@@ -104,10 +185,71 @@ class InfinitesimalREMLFitter:
         self.precond_conf: ProjectedCorePrecondConf | None = None
         self._probe_cache = REMLProbeCache() if cfg.cache_reml_setup else None
         self._ops: _OperatorBundle | None = None
+        self._smile_operators = self._build_smile_operators()
+
+    def _build_smile_operators(self) -> tuple:
+        """SMILE W modes and their checks (reml_model.py:429-485)."""
+        cfg = self.cfg
+        present = {
+            "identity": bool(cfg.smile_identity),
+            "w_files": bool(cfg.smile_w_files),
+            "w_file_groups": bool(cfg.smile_w_file_groups),
+            "matrices": bool(cfg.smile_weight_matrices),
+            "matrix_groups": bool(cfg.smile_weight_matrix_groups),
+        }
+        if present["w_files"] and present["matrices"]:
+            raise ValueError("Use either smile_w_files or smile_weight_matrices, not both.")
+        if sum(present.values()) > 1:
+            raise ValueError(
+                "Use only one SMILE W mode: identity, single W list, W file groups, "
+                "single matrix list, or matrix groups.")
+        if not any(present.values()):
+            return ()
+        if cfg.smile_normalization not in ("kernel_trace", "effective_rank"):
+            raise ValueError("SMILE normalization must be 'kernel_trace' or 'effective_rank'.")
+        if cfg.smile_diag_mode not in ("full", "mean"):
+            raise ValueError("SMILE diag mode must be 'full' or 'mean'.")
+        if cfg.vc_block_sizes is not None or cfg.component_variant_indices is not None:
+            raise ValueError("SMILE block-W mode cannot be combined with component partitioning.")
+        if len(self.streamers) != 1:
+            raise ValueError("SMILE block-W mode needs exactly one dense streamer.")
+        from .smile_block_w import SmileBlockWeightedOperator, SmileMultiBlockWeightedOperator
+
+        st = self.streamers[0]
+        kw = dict(normalization=cfg.smile_normalization, strict_coverage=cfg.smile_strict_coverage,
+                  diag_mode=cfg.smile_diag_mode)
+        if present["identity"]:
+            return (SmileBlockWeightedOperator.identity(
+                st, block_size=cfg.smile_identity_block_size, **kw),)
+        if present["matrices"]:
+            return (SmileBlockWeightedOperator(st, list(cfg.smile_weight_matrices), **kw),)
+        if present["w_files"]:
+            return (SmileBlockWeightedOperator.from_weight_files(st, list(cfg.smile_w_files), **kw),)
+        if present["matrix_groups"]:
+            return SmileMultiBlockWeightedOperator.from_weight_matrix_groups(
+                st, cfg.smile_weight_matrix_groups, **kw).operators
+        return SmileMultiBlockWeightedOperator.from_weight_file_groups(
+            st, cfg.smile_w_file_groups, **kw).operators
 
     # ------------------------------------------------------------ operators
     def _assemble_reml_operators(self) -> _OperatorBundle:
         prec = self.cfg.precision
+        if self._smile_operators:
+            # One X^T V pass shared by all SMILE GRMs (reml_model.py:1069-1164).
+            from .smile_block_w import SmileMultiBlockWeightedOperator
+
+            multi = SmileMultiBlockWeightedOperator(self._smile_operators)
+
+            def atoms(U):
+                KU = multi.stacked_kv(U)
+                raw = torch.einsum("nr,gns->grs", U.to(KU.dtype), KU)
+                return 0.5 * (raw + raw.transpose(-1, -2))
+
+            return _OperatorBundle(
+                K_mvs=tuple((lambda V, op=op: op.kv(V)) for op in self._smile_operators),
+                diag_list=tuple(op.diag() for op in self._smile_operators),
+                weighted_hv=multi.weighted_hv, stacked_kv=multi.stacked_kv,
+                projected_core_atoms=atoms)
         if len(self.streamers) == 1 and self.streamers[0].n_components > 1:
             st = self.streamers[0]
             G = st.n_components
@@ -150,12 +292,30 @@ class InfinitesimalREMLFitter:
             return lambda V: ops.weighted_hv(tg, te, V)
         return lambda V: sum(float(tg[i]) * mv(V) for i, mv in enumerate(ops.K_mvs)) + te * V
 
+    def _make_effect_precond(self, ops: _OperatorBundle, theta_g, theta_e):
+        """M^{-1} at the given variance components (reml_model.py:1443-1457)."""
+        if self.precond_conf is None:
+            return None
+        dev = self.streamers[0].dev
+        tg = torch.as_tensor(np.asarray(theta_g, float).reshape(-1), dtype=torch.float32, device=dev)
+        te = torch.as_tensor(np.asarray(theta_e, float).reshape(-1), dtype=torch.float32, device=dev)
+        diag_H = scalar_diag_from_precond_conf(self.precond_conf, tg, te)
+        if diag_H is None:
+            stack = torch.stack([torch.as_tensor(d, dtype=torch.float32, device=dev).expand(self.n)
+                                 for d in ops.diag_list])
+            diag_H = te[0] + torch.tensordot(tg, stack, dims=1)
+        return make_precond(self.precond_conf, tg, diag_H, eps=self.cfg.pcg_ridge)
+
+    def _ensure_projected_core_precond_ready(self, ops: _OperatorBundle, var_components_init=None):
+        if self.precond_conf is None and self.cfg.precond_rank > 0:
+            self._build_projected_core_precond(ops, var_components_init)
+
     def _build_projected_core_precond(self, ops: _OperatorBundle, var_components_init=None,
                                       theta_ref=None) -> ProjectedCorePrecondConf:
         """Nystrom basis of the reference kernel + projected cores (reml_model.py:863-960)."""
         cfg = self.cfg
         G = len(ops.K_mvs)
-        atoms = np.asarray([float(d) for d in ops.diag_list])
+        atoms = np.asarray([float(torch.as_tensor(d).double().mean()) for d in ops.diag_list])
         if theta_ref is None:
             if var_components_init is not None:
                 theta_ref = np.asarray(var_components_init, float)[:G]
@@ -163,7 +323,10 @@ class InfinitesimalREMLFitter:
                 theta_ref = np.where(atoms > 0, 1.0 / max(float(np.sum(atoms)), 1e-12), 0.0)
         theta_ref = np.asarray(theta_ref, float)
         sk = cfg.sketch_precision
-        if len(self.streamers) == 1:
+        if self._smile_operators:
+            def K_ref(V):
+                return ops.weighted_hv(theta_ref, None, V)
+        elif len(self.streamers) == 1:
             st = self.streamers[0]
             eff = st._component_eff_m_host.astype(np.float64)
 
@@ -221,7 +384,9 @@ class InfinitesimalREMLFitter:
             slq_workspace_bytes=default_workspace_bytes(cfg.gpu_budget_bytes),
             precond_conf=conf, slq_precond_conf=conf, precond_refresh_fn=refresh,
             precond_eps=cfg.pcg_ridge, weighted_hv=ops.weighted_hv, stacked_kv=ops.stacked_kv,
-            optimizer=cfg.optimizer, pcg_tol=cfg.reml_pcg_tol,
+            optimizer=cfg.smile_optimizer if self._smile_operators else cfg.optimizer,
+            scoring_step_tol=(cfg.smile_scoring_step_tol if self._smile_operators else 1e-4),
+            pcg_tol=cfg.reml_pcg_tol,
             response_is_standardized=cfg.response_is_standardized,
             unit_variance_components=cfg.unit_variance_components,
             max_linesearch_trials=cfg.strict_max_linesearch_trials, return_diagnostics=True,
@@ -242,4 +407,161 @@ class InfinitesimalREMLFitter:
                          final_loglik=float(diag["loglik"]), elapsed_sec=time.time() - t0)
 
 
-__all__ = ["FitConfig", "FitResult", "InfinitesimalREMLFitter"]
+    # ------------------------------------------------------------ effects
+    def _estimate_snp_effects(self, alpha: torch.Tensor, theta_g) -> tuple:
+        """Per-component SNP effects beta_g with Z_g beta_g = theta_g K_g alpha
+        (reml_model.py:1459-1540): theta_g/m_eff,g Z_g^T alpha."""
+        tg = np.asarray(theta_g, float).reshape(-1)
+        if self._smile_operators:
+            if tg.size != len(self._smile_operators):
+                raise ValueError(
+                    f"theta_g must have length {len(self._smile_operators)} for SMILE effects.")
+            return tuple(op.snp_effects(alpha, tg[i]) for i, op in enumerate(self._smile_operators))
+        if len(self.streamers) == 1 and self.streamers[0].n_components > 1:
+            st = self.streamers[0]
+            xt = st.xtv(alpha, normalize=False)
+            out = []
+            for g in range(st.n_components):
+                a, b = int(st._component_snp_offsets[g]), int(st._component_snp_offsets[g + 1])
+                eff = float(st._component_eff_m_host[g])
+                out.append(xt[a:b] * (tg[g] / eff) if eff > 0 else torch.zeros_like(xt[a:b]))
+            return tuple(out)
+        return tuple(float(tg[g]) * st.xtv(alpha, normalize=True)
+                     for g, st in enumerate(self.streamers))
+
+    def estimate_effects(self, y, *, var_components, covar=None) -> EffectEstimates:
+        """Fixed effects, BLUP random effect and SNP effects at the given
+        variance components (reml_model.py:1543-1644)."""
+        if not self.streamers:
+            raise RuntimeError("estimate_effects requires initialized streamers.")
+        from .pcg import pcg_solve
+        from .reml import standardize_response
+
+        ops = self._assemble_reml_operators()
+        G = len(ops.K_mvs)
+        theta = np.asarray(var_components, dtype=np.float64).reshape(-1)
+        if theta.size != G + 1:
+            raise ValueError(f"var_components length mismatch: expected {G + 1}, got {theta.size}.")
+        theta_g, theta_e = theta[:-1], theta[-1]
+        self._ensure_projected_core_precond_ready(ops, var_components_init=theta)
+        dev = self.streamers[0].dev
+        y_t = torch.as_tensor(y, dtype=torch.float32).reshape(-1).to(dev)
+        if self.cfg.response_is_standardized:
+            if not bool(torch.all(torch.isfinite(y_t))):
+                raise ValueError("Phenotype contains non-finite values.")
+            y_std, y_mean, y_scale = y_t, 0.0, 1.0
+        else:
+            y_std, y_mean, y_scale = standardize_response(y_t)
+        xmat = None
+        if covar is not None:
+            xmat = torch.as_tensor(covar, dtype=torch.float32).to(dev)
+            if xmat.ndim == 1:
+                xmat = xmat[:, None]
+            if xmat.numel() == 0:
+                xmat = None
+        Hv = self._make_hv(ops, theta_g, theta_e)
+        M = self._make_effect_precond(ops, theta_g, theta_e)
+        rhs = y_std[:, None] if xmat is None else torch.cat([y_std[:, None], xmat], dim=1)
+        rhs = rhs.contiguous()
+        X0 = M(rhs) if M is not None else torch.zeros_like(rhs)
+        tol = float(self.cfg.effect_pcg_tol)
+        sol, rel, iters = pcg_solve(Hv, rhs, M=M, tol=tol, maxiter=self.cfg.max_pcg_iters, X0=X0)
+        if not bool(torch.all(torch.isfinite(sol))):
+            raise FloatingPointError("Non-finite PCG solution encountered in estimate_effects.")
+        rel_host = float(torch.as_tensor(rel).double().max())
+        if not np.isfinite(rel_host) or rel_host > tol * 1.05:
+            raise FloatingPointError(
+                f"Effect-estimation PCG did not converge: relative residual={rel_host:.3e}, "
+                f"tolerance={tol:.3e}, iterations={int(iters)}/{int(self.cfg.max_pcg_iters)}.")
+        Hinv_y = sol[:, 0]
+        if xmat is not None:
+            Hinv_x = sol[:, 1:]
+            fixed = _solve_small_spd(xmat.T @ Hinv_x, xmat.T @ Hinv_y)
+            alpha = Hinv_y - Hinv_x @ fixed
+        else:
+            fixed = torch.empty(0, dtype=torch.float32, device=dev)
+            alpha = Hinv_y
+        alpha = alpha.contiguous()
+        if ops.stacked_kv is not None:
+            Ka = ops.stacked_kv(alpha[:, None])[..., 0]
+        else:
+            Ka = torch.stack([mv(alpha) for mv in ops.K_mvs], dim=0)
+        tg_t = torch.as_tensor(theta_g, dtype=torch.float32, device=dev)
+        comps = tuple(float(theta_g[g]) * Ka[g] for g in range(G))
+        return EffectEstimates(
+            fixed_effects=fixed, random_effect=torch.sum(tg_t[:, None] * Ka, dim=0),
+            random_effect_components=comps, snp_effects=self._estimate_snp_effects(alpha, theta_g),
+            pcg_rel_res=rel_host, pcg_iters=int(iters), y_mean=float(y_mean),
+            y_scale=float(y_scale))
+
+    def predict(self, effects: EffectEstimates, *, test_fitter: "InfinitesimalREMLFitter",
+                test_covar=None) -> PredictionEstimates:
+        """X_test b + Z_test beta on the test samples with the training
+        standardisation (reml_model.py:1646-1818): one Z b pass per test
+        streamer, the components as columns of b."""
+        if not self.streamers or not test_fitter.streamers:
+            raise RuntimeError("Prediction requires initialized training and test streamers.")
+        _validate_dense_prediction_streamers(self.streamers, test_fitter.streamers)
+        if len(self.streamers) == 1 and self.streamers[0].n_components > 1:
+            expected = self.streamers[0].n_components
+        elif self._smile_operators:
+            expected = len(self._smile_operators)
+        else:
+            expected = len(self.streamers)
+        if len(effects.snp_effects) != expected:
+            raise ValueError("Prediction SNP-effect component count mismatch: "
+                             f"expected {expected}, got {len(effects.snp_effects)}.")
+        for a, b in zip(self.streamers, test_fitter.streamers):
+            b.set_standardization(a._means_host, a._inv_sds_host)
+        st_test0 = test_fitter.streamers[0]
+        dev = st_test0.dev
+        n_test = int(st_test0.n)
+        beta = torch.as_tensor(effects.fixed_effects, dtype=torch.float32).reshape(-1).to(dev)
+        X_test = None
+        if test_covar is not None:
+            X_test = torch.as_tensor(test_covar, dtype=torch.float32).to(dev)
+            if X_test.ndim == 1:
+                X_test = X_test[:, None]
+            if X_test.ndim != 2 or X_test.shape[0] != n_test:
+                raise ValueError("Prediction covariates must be a 2D matrix with one row per test sample.")
+            if not bool(torch.all(torch.isfinite(X_test))):
+                raise ValueError("Prediction covariates contain non-finite values.")
+        if beta.numel() > 0:
+            if X_test is None:
+                raise ValueError("Prediction requires test covariates aligned to the training design matrix.")
+            if X_test.shape[1] != beta.numel():
+                raise ValueError(f"Prediction covariate width mismatch: expected {beta.numel()}, "
+                                 f"got {X_test.shape[1]}.")
+            fixed_effect = X_test @ beta
+        else:
+            fixed_effect = torch.zeros(n_test, dtype=torch.float32, device=dev)
+        if len(self.streamers) == 1:
+            st_tr = self.streamers[0]
+            B = torch.zeros((int(st_tr.m), expected), dtype=torch.float32, device=dev)
+            if st_tr.n_components > 1 and not self._smile_operators:
+                for g in range(expected):
+                    a, b = int(st_tr._component_snp_offsets[g]), int(st_tr._component_snp_offsets[g + 1])
+                    B[a:b, g] = torch.as_tensor(effects.snp_effects[g], dtype=torch.float32).to(dev).reshape(-1)
+            else:
+                for g in range(expected):
+                    bg = torch.as_tensor(effects.snp_effects[g], dtype=torch.float32).to(dev).reshape(-1)
+                    if bg.numel() != int(st_tr.m):
+                        raise ValueError(f"SNP-effect length mismatch: expected {int(st_tr.m)}, "
+                                         f"got {bg.numel()}.")
+                    B[:, g] = bg
+            comp = st_test0.zxb(B)
+            components = tuple(comp[:, g] for g in range(expected))
+        else:
+            components = tuple(
+                st.zxb(torch.as_tensor(b, dtype=torch.float32).to(dev).reshape(-1))
+                for st, b in zip(test_fitter.streamers, effects.snp_effects))
+        random_effect = torch.stack(components, dim=0).sum(0)
+        y_pred_std = fixed_effect + random_effect
+        return PredictionEstimates(
+            fixed_effect=fixed_effect, random_effect=random_effect,
+            random_effect_components=components, y_pred_std=y_pred_std,
+            y_pred=float(effects.y_mean) + float(effects.y_scale) * y_pred_std)
+
+
+__all__ = ["FitConfig", "FitResult", "InfinitesimalREMLFitter", "EffectEstimates",
+           "PredictionEstimates"]

@@ -111,6 +111,16 @@ int coherit_geno_info(const coherit_geno_t* h, int64_t* n, int64_t* m, int64_t* 
 int coherit_geno_read_packed(coherit_geno_t* h, int64_t snp_start, int32_t width,
                              uint8_t* out_host, void* stream);
 
+/* Standardised genotype columns of stats slot `slot`: out[i*ldo + c] =
+ * (g_ic - mean) * inv_sd of cache SNP snp_idx[c] (device int64 array of
+ * `count` indices) for every sample i, 0 where the genotype is missing,
+ * evaluated in FP32 in the reference's order.  out: device, n x ldo.
+ * Replaces GenoBlockStreamer.extract_standardized_columns
+ * (geno_stream.py:2748-2760, :2472-2502), here on the device.  An index
+ * outside [0, m) yields a NaN column.                                        */
+int coherit_geno_extract_columns(coherit_geno_t* h, int32_t slot, const int64_t* snp_idx,
+                                 int32_t count, float* out, int64_t ldo, void* stream);
+
 /* ------------------------------------------------------------ standardisation */
 
 /* Compute per-SNP statistics of stats slot `slot` over the samples selected by
