@@ -43,7 +43,14 @@ namespace coherit {
 constexpr int kSets = COHERIT_SETS;  // decoder warp sets (stages in flight through the A ring)
 constexpr int kThreads = 32 * (3 + 4 * kSets);
 constexpr int kWarpG = 0, kWarpMMA = 1, kWarpB = 2, kWarpDec0 = 3;
-constexpr int kRG = 12;        // genotype ring depth (stages of kStageBlocks 2 KB blocks)
+// Genotype ring depth (stages of kStageBlocks 2 KB blocks).  It must be a
+// multiple of the number of decoder sets: then every ring slot is only ever
+// consumed by one set, in stage order, so a set never waits on a slot whose
+// previous fill is still in flight (parity waits see one phase only).  Nine
+// stages keep the decoders' waits on genotype data short and leave shared
+// memory for a deeper B ring.
+constexpr int kRG = 9;
+static_assert(kRG % kSets == 0, "genotype ring depth must be a multiple of the decoder sets");
 // Tensor-memory A ring depth limit (slots of 32 * kStageBlocks columns).  Depths
 // up to 6 are the configurations exercised on GB300; a 7-slot ring with a
 // 64-column accumulator raised an illegal-instruction fault whose cause was

@@ -69,9 +69,10 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
     gbase = p.geno + (tile * p.n_panels + p0) * kBlockBytes;
     bbase = p.bsrc + p0 * p.b_chunk_bytes;
   }
-  // This CTA's share of the K stages: [s0, s0 + nch).
+  // This CTA's share of the K stages: [s0, s0 + nch).  The host keeps a
+  // share at most 512 stages long (split K), so 32-bit stage counters hold.
   const int64_t s0 = ntot * zsplit / p.ksplit;
-  const int64_t nch = ntot * (zsplit + 1) / p.ksplit - s0;
+  const int nch = static_cast<int>(ntot * (zsplit + 1) / p.ksplit - s0);
   gbase += s0 * (kStageBlocks * kBlockBytes);
   bbase += s0 * stage_b_bytes;
 
@@ -124,18 +125,22 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
   if (warp == kWarpG) {
     // ---------------------------------------------- genotype block producer
     if (lane == 0) {
-      int64_t issued = 0;
-      for (int64_t c = 0; c < nch; ++c) {
-        const int s = static_cast<int>(c % kRG);
-        const uint32_t u = static_cast<uint32_t>(c / kRG);
-        if (u > 0 && !ptx::mbar_wait(&emptyG[s], (u - 1) & 1, p.err, 11, abort_flag)) break;
+      // Ring slot and phase parity are carried as counters: no division in
+      // the per-stage loops of the single-thread roles.
+      int issued = 0;
+      int s = 0;
+      uint32_t ph = 0;
+      for (int c = 0; c < nch; ++c) {
+        if (c >= kRG && !ptx::mbar_wait(&emptyG[s], ph ^ 1u, p.err, 11, abort_flag)) break;
         ptx::mbar_arrive_expect_tx(&fullG[s], kStageBytes);
-        ptx::bulk_g2s(gring + s * kStageBytes, gbase + c * kStageBytes, kStageBytes, &fullG[s]);
+        ptx::bulk_g2s(gring + s * kStageBytes, gbase + static_cast<int64_t>(c) * kStageBytes,
+                      kStageBytes, &fullG[s]);
         issued = c + 1;
+        if (++s == kRG) { s = 0; ph ^= 1u; }
       }
       if (*abort_flag) {
         // Let copies still in flight land before the CTA exits.
-        for (int64_t c = (issued > kRG ? issued - kRG : 0); c < issued; ++c) {
+        for (int c = (issued > kRG ? issued - kRG : 0); c < issued; ++c) {
           volatile int no_abort = 0;
           ptx::mbar_wait(&fullG[c % kRG], static_cast<uint32_t>(c / kRG) & 1, p.err, 18,
                          &no_abort);
@@ -145,18 +150,19 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
   } else if (warp == kWarpB) {
     // ---------------------------------------------------- B tile producer
     if (lane == 0) {
-      int64_t issued = 0;
-      for (int64_t c = 0; c < nch; ++c) {
-        const int s = static_cast<int>(c % RB);
-        const uint32_t u = static_cast<uint32_t>(c / RB);
-        if (u > 0 && !ptx::mbar_wait(&emptyB[s], (u - 1) & 1, p.err, 12, abort_flag)) break;
+      int issued = 0;
+      int s = 0;
+      uint32_t ph = 0;
+      for (int c = 0; c < nch; ++c) {
+        if (c >= RB && !ptx::mbar_wait(&emptyB[s], ph ^ 1u, p.err, 12, abort_flag)) break;
         ptx::mbar_arrive_expect_tx(&fullB[s], p.bslot_bytes);
-        ptx::bulk_g2s(bring + static_cast<size_t>(s) * p.bslot_bytes, bbase + c * stage_b_bytes,
-                      p.bslot_bytes, &fullB[s]);
+        ptx::bulk_g2s(bring + static_cast<size_t>(s) * p.bslot_bytes,
+                      bbase + static_cast<int64_t>(c) * stage_b_bytes, p.bslot_bytes, &fullB[s]);
         issued = c + 1;
+        if (++s == RB) { s = 0; ph ^= 1u; }
       }
       if (*abort_flag) {
-        for (int64_t c = (issued > RB ? issued - RB : 0); c < issued; ++c) {
+        for (int c = (issued > RB ? issued - RB : 0); c < issued; ++c) {
           volatile int no_abort = 0;
           ptx::mbar_wait(&fullB[c % RB], static_cast<uint32_t>(c / RB) & 1, p.err, 19, &no_abort);
         }
@@ -168,14 +174,11 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
       const uint32_t idesc = ptx::idesc_bf16_f32(128, SIDE ? NSPLIT * kp : kp);
       const uint64_t bdesc0 = ptx::smem_desc(ptx::smem_addr(bring), 128u, 1024u);
       const uint32_t term_off = static_cast<uint32_t>(kp * 128) >> 4;
-      for (int64_t c = 0; c < nch; ++c) {
-        const int as = static_cast<int>(c % RA);
-        const int bs = static_cast<int>(c % RB);
-        if (!ptx::mbar_wait(&decoded[as], static_cast<uint32_t>(c / RA) & 1, p.err, 13,
-                            abort_flag))
-          break;
-        if (!ptx::mbar_wait(&fullB[bs], static_cast<uint32_t>(c / RB) & 1, p.err, 14, abort_flag))
-          break;
+      int as = 0, bs = 0;
+      uint32_t pa = 0, pb = 0;
+      for (int c = 0; c < nch; ++c) {
+        if (!ptx::mbar_wait(&decoded[as], pa, p.err, 13, abort_flag)) break;
+        if (!ptx::mbar_wait(&fullB[bs], pb, p.err, 14, abort_flag)) break;
         ptx::tc_fence_after();
         const uint64_t bslot = bdesc0 + ((static_cast<uint64_t>(bs) * p.bslot_bytes) >> 4);
         const uint32_t a_slot = tmem + p.acc_cols + static_cast<uint32_t>(as) * (32u * kStageBlocks);
@@ -199,6 +202,8 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
         }
         ptx::mma_commit(&emptyA[as]);
         ptx::mma_commit(&emptyB[bs]);
+        if (++as == RA) { as = 0; pa ^= 1u; }
+        if (++bs == RB) { bs = 0; pb ^= 1u; }
       }
       if (nch == 0) {
         ptx::mbar_arrive(done);
@@ -221,10 +226,12 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
     const int row = quarter * 32 + lane;
     const uint32_t lane_base = static_cast<uint32_t>(quarter * 32) << 16;
     bool ok = true;
-    for (int64_t c = set; c < nch; c += kSets) {
-      const int gs = static_cast<int>(c % kRG);
-      bool w_ok = ptx::mbar_wait(&fullG[gs], static_cast<uint32_t>(c / kRG) & 1, p.err, 15,
-                                 abort_flag);
+    // Stage c = set + i * kSets: its G slot/phase and A slot/round advance by
+    // kSets per step (kSets <= kRG and kSets <= RA, so one wrap at most).
+    int gs = set, as = set;
+    uint32_t gph = 0, around = 0;
+    for (int c = set; c < nch; c += kSets) {
+      bool w_ok = ptx::mbar_wait(&fullG[gs], gph, p.err, 15, abort_flag);
       if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
       uint4 raw[kStageBlocks];
 #pragma unroll
@@ -233,10 +240,8 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
                                                  row * kRowBytes);
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&emptyG[gs]);
-      const int as = static_cast<int>(c % RA);
       if (c >= RA) {
-        w_ok = ptx::mbar_wait(&emptyA[as], static_cast<uint32_t>(c / RA - 1) & 1, p.err, 16,
-                              abort_flag);
+        w_ok = ptx::mbar_wait(&emptyA[as], (around - 1u) & 1u, p.err, 16, abort_flag);
         if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
       }
       ptx::tc_fence_after();
@@ -251,6 +256,10 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
       ptx::tc_fence_before();
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&decoded[as]);
+      gs += kSets;
+      if (gs >= kRG) { gs -= kRG; gph ^= 1u; }
+      as += kSets;
+      if (as >= RA) { as -= RA; ++around; }
     }
     if (ok) {
       const bool w_ok = ptx::mbar_wait(done, 0, p.err, 17, abort_flag);
