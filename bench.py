@@ -266,6 +266,59 @@ def serve_step(srv, ys, Xs, host: bool):
     return [f.result() for f in futs]
 
 
+def serving_stream(st, wl, n_requests: int, rate_per_s: float, seed: int, max_active: int):
+    """A bounded stream of heterogeneous requests with Poisson arrivals over
+    the resident genotypes (the serving workload's request mix on this
+    matrix): each request a random sample subset (size log-uniform in
+    [n/5, n]), 1-20 N(0,1) covariates + intercept, h2 ~ U(0.05, 0.8) from
+    wl.n_causal causal SNPs.  Requests arrive while earlier ones are on the
+    GPU and join their batched launches.  Returns the stream's summary."""
+    import torch
+
+    from coherit_gb300.serving import REMLServer
+
+    rng = np.random.default_rng(seed)
+    n = st.n
+    B = np.zeros((st.m, n_requests), dtype=np.float32)
+    for r in range(n_requests):
+        causal = rng.choice(st.m, size=min(wl.n_causal, st.m), replace=False)
+        B[causal, r] = rng.normal(size=causal.size)
+    G = st.zxb(torch.as_tensor(B, device=st.dev)).double().cpu().numpy()
+    reqs = []
+    for r in range(n_requests):
+        size = int(np.exp(rng.uniform(np.log(n / 5), np.log(n))))
+        mask = np.zeros(n, dtype=bool)
+        mask[rng.choice(n, size=size, replace=False)] = True
+        h2 = rng.uniform(0.05, 0.8)
+        g = G[mask, r]
+        g = g * np.sqrt(h2 / g.var())
+        y = (g + rng.normal(scale=np.sqrt(1 - h2), size=size)).astype(np.float32)
+        p = int(rng.integers(1, 21))
+        X = np.column_stack([np.ones(size), rng.normal(size=(size, p))]).astype(np.float32)
+        reqs.append((y, X, mask))
+    gaps = rng.exponential(1.0 / rate_per_s, size=n_requests)
+    srv = REMLServer(st, max_active=max_active, fit_kwargs=fit_kwargs(wl))
+    b0 = srv.batcher.launches
+    t0 = time.perf_counter()
+    futs = []
+    for (y, X, mask), gap in zip(reqs, gaps):
+        time.sleep(float(gap))
+        futs.append(srv.submit(y, X, sample_mask=mask))
+    res = [f.result() for f in futs]
+    wall = time.perf_counter() - t0
+    per_launch = srv.batcher.requests_per_launch
+    srv.close()
+    lat = [r.latency for r in res]
+    return {"requests": n_requests, "arrival_rate_per_s": round(rate_per_s, 3),
+            "fits_per_hr": round(n_requests / (wall / 3600.0), 1),
+            "latency_s": {"p50": round(statistics.median(lat), 3),
+                          "p99": round(_percentile(lat, 0.99), 3)},
+            "subset_sizes": [int(m.sum()) for _, _, m in reqs][:8],
+            "operator_launches": srv.batcher.launches - b0,
+            "mean_requests_per_launch": round(float(np.mean(per_launch)), 2) if per_launch else 0.0,
+            "max_active": max_active, "seed": seed}
+
+
 def run_ours(args, wl):
     import torch
 
@@ -380,6 +433,11 @@ def run_ours(args, wl):
                      "h2": round(pres.heritability, 6),
                      "abs_dh2_vs_served": round(
                          abs(pres.heritability - timed[1 % R].heritability), 6)}
+        stream = None
+        if args.stream > 0:
+            rate = args.stream_rate
+            stream = serving_stream(st, wl, args.stream, rate, seed=wl.seed + 99,
+                                    max_active=R)
         cpu = None
         if not args.no_cpu:
             t_fit, cores, sample = cpu_fit_estimate(wl, fit_apps, fit_cols)
@@ -415,6 +473,7 @@ def run_ours(args, wl):
                     "d2h_bytes_per_step": int(sum(r.var_components.size * 8 for r in e2e_res))},
             "gpu_launches": int(launches),
             "roofline": roof,
+            "serving_stream": stream,
             "single_fit_mixed": single,
             "plain_fp32_single_fit": plain,
             "cpu_baseline": cpu,
@@ -526,6 +585,10 @@ def main():
     ap.add_argument("--precision", default="bf16x3")
     ap.add_argument("--requests", type=int, default=8,
                     help="concurrent fit requests per step (the serving batch)")
+    ap.add_argument("--stream", type=int, default=24,
+                    help="requests in the Poisson-arrival subset stream (0 = skip)")
+    ap.add_argument("--stream-rate", type=float, default=2.0,
+                    help="stream arrivals per second (Poisson)")
     ap.add_argument("--batch-window", type=float, default=0.01,
                     help="seconds the batcher waits for the other active fits")
     ap.add_argument("--single-fits", type=int, default=3,
