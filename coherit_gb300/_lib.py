@@ -64,6 +64,10 @@ _SIGNATURES = {
         C.c_int,
         [_i64, _i64, _p, _i32, _u64, _u32, C.c_int, _p, _p],
     ),
+    "coherit_geno_create_bed": (
+        C.c_int,
+        [_p, _i64, _i64, _i64, _p, _i64, _p, _i32, C.c_int, _p, _p],
+    ),
     "coherit_geno_destroy": (C.c_int, [_p]),
     "coherit_geno_info": (C.c_int, [_p, _p, _p, _p, _p, _p, _p, _p]),
     "coherit_geno_read_packed": (C.c_int, [_p, _i64, _i32, _p, _p]),

@@ -40,6 +40,10 @@ class BedSource:
         lut = np.asarray([2, MISSING_VAL, 1, 0], dtype=np.int8)
         self._lut = lut
 
+    def raw_bytes(self) -> np.ndarray:
+        """The whole .bed file (header + SNP-major records), memory-mapped."""
+        return self._mm
+
     def read_block_variant_major(self, start: int, count: int) -> np.ndarray:
         bps = self._bytes_per_snp
         raw = np.asarray(self._mm[3 + start * bps: 3 + (start + count) * bps]).reshape(count, bps)

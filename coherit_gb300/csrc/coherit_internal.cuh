@@ -152,6 +152,9 @@ int build_layout_from_ref(coherit_geno* h, const uint8_t* d_packed, const int64_
                           const int32_t* d_call_pw, const int32_t* d_snp_call,
                           const int32_t* d_snp_col, cudaStream_t st);
 int build_layout_synthetic(coherit_geno* h, uint64_t seed, uint32_t miss_q24, cudaStream_t st);
+int build_layout_from_bed(coherit_geno* h, const uint8_t* bed_body, int64_t bps,
+                          const int32_t* d_keep, const std::vector<int32_t>& slot_of_snp_host,
+                          cudaStream_t st);
 int build_copy_t(coherit_geno* h, cudaStream_t st);
 int build_missing_lists(coherit_geno* h, cudaStream_t st);
 int compute_slot_stats(coherit_geno* h, StatsSlot& s, const float* override_mean,

@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <algorithm>
 #include <cmath>
 
@@ -63,6 +64,42 @@ __global__ void k_build_s_from_ref(uint8_t* __restrict__ geno_s, int64_t n, int6
   uint4* dst = reinterpret_cast<uint4*>(geno_s + ((st * n_panels + p) * kTile + (i % kTile)) *
                                                      kRowBytes);
   *dst = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// copy S from SNP-major PLINK BED records of cache SNPs [s_lo, s_hi) (one
+// record of `bps` bytes per SNP, sample k at bits 2*(k%4) of byte k/4; BED
+// codes 0,1,2,3 -> allele count 2, missing, 1, 0 as the reference's BED
+// transcode, geno_stream.py:709-745).  keep: source sample of each row
+// (nullptr = identity).  Rows of panels [p_lo, p_hi) are OR-ed into copy S
+// (zeroed beforehand), so a panel may be filled by consecutive chunks.
+__global__ void k_build_s_from_bed(uint8_t* __restrict__ geno_s, int64_t n, int64_t n_pad,
+                                   int64_t n_panels, const uint8_t* __restrict__ bed, int64_t bps,
+                                   int64_t s_lo, int64_t s_hi, const int32_t* __restrict__ keep,
+                                   const int32_t* __restrict__ snp_of_slot, int64_t p_lo,
+                                   int64_t p_hi) {
+  const int64_t np = p_hi - p_lo;
+  const int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (idx >= n * np) return;
+  // Consecutive threads take consecutive samples of one panel, so a warp
+  // reads 8 neighbouring bytes of each SNP record.
+  const int64_t i = idx % n;
+  const int64_t p = p_lo + idx / n;
+  const int64_t ks = keep ? keep[i] : i;
+  const int64_t byte_off = ks >> 2;
+  const int shift = static_cast<int>(2 * (ks & 3));
+  uint32_t w[4] = {0u, 0u, 0u, 0u};
+  for (int e = 0; e < kPanel; ++e) {
+    const int32_t snp = snp_of_slot[p * kPanel + e];
+    if (snp < s_lo || snp >= s_hi) continue;
+    const uint32_t b = (bed[(snp - s_lo) * bps + byte_off] >> shift) & 3u;
+    const uint32_t code = (0x1Eu >> (2 * b)) & 3u;  // BED 0,1,2,3 -> 2, 3 (missing), 1, 0
+    w[row_word(e)] |= code << row_shift(e);
+  }
+  const int64_t st = i / kTile;
+  uint4* dst = reinterpret_cast<uint4*>(geno_s + ((st * n_panels + p) * kTile + (i % kTile)) *
+                                                     kRowBytes);
+  const uint4 old = *dst;
+  *dst = make_uint4(old.x | w[0], old.y | w[1], old.z | w[2], old.w | w[3]);
 }
 
 // copy S from the synthetic generator.
@@ -357,6 +394,43 @@ int build_layout_from_ref(coherit_geno* h, const uint8_t* d_packed, const int64_
         h->geno_s, h->n, h->n_pad, h->n_panels, d_packed, d_call_off, d_call_pw, d_snp_call,
         d_snp_col, h->d_snp_of_slot); note_launch();
   CO_CUDA(cudaGetLastError());
+  return build_copy_t(h, st);
+}
+
+// copy S from a host PLINK BED file (bytes after the 3-byte header), uploaded
+// and transcoded in chunks of whole SNP records; then copy T.
+int build_layout_from_bed(coherit_geno* h, const uint8_t* bed_body, int64_t bps,
+                          const int32_t* d_keep, const std::vector<int32_t>& slot_of_snp_host,
+                          cudaStream_t st) {
+  CO_CUDA(cudaMemsetAsync(h->geno_s, 0, static_cast<size_t>(h->n_pad) * h->m_pad / 4, st));
+  // Device staging per chunk: COHERIT_BED_CHUNK_BYTES (default 256 MB) of
+  // whole SNP records.
+  int64_t chunk_bytes = int64_t(256) << 20;
+  if (const char* env = getenv("COHERIT_BED_CHUNK_BYTES")) {
+    const long long v = atoll(env);
+    if (v > 0) chunk_bytes = v;
+  }
+  const int64_t chunk = std::max<int64_t>(1, chunk_bytes / std::max<int64_t>(bps, 1));
+  uint8_t* d_chunk = nullptr;
+  CO_CUDA(cudaMalloc(&d_chunk, static_cast<size_t>(std::min<int64_t>(chunk, h->m)) * bps));
+  cudaError_t e = cudaSuccess;
+  for (int64_t s_lo = 0; s_lo < h->m && e == cudaSuccess; s_lo += chunk) {
+    const int64_t s_hi = std::min<int64_t>(s_lo + chunk, h->m);
+    e = cudaMemcpyAsync(d_chunk, bed_body + s_lo * bps, static_cast<size_t>(s_hi - s_lo) * bps,
+                        cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) break;
+    const int64_t p_lo = slot_of_snp_host[s_lo] / kPanel;
+    const int64_t p_hi = slot_of_snp_host[s_hi - 1] / kPanel + 1;
+    const int64_t work = h->n * (p_hi - p_lo);
+    k_build_s_from_bed<<<grid_of(work, 256), 256, 0, st>>>(
+        h->geno_s, h->n, h->n_pad, h->n_panels, d_chunk, bps, s_lo, s_hi, d_keep,
+        h->d_snp_of_slot, p_lo, p_hi); note_launch();
+    e = cudaGetLastError();
+  }
+  // The chunk buffer is reused by queued work until the stream drains.
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_chunk);
+  if (e != cudaSuccess) return cuda_status(e, "BED transcode");
   return build_copy_t(h, st);
 }
 
@@ -786,6 +860,67 @@ int coherit_geno_create_synthetic(int64_t n, int64_t m, const int32_t* component
   if (rc == COHERIT_OK) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = cuda_status(e, "synthetic genotypes");
+  }
+  if (rc == COHERIT_OK) rc = finish_create(h, st);
+  if (rc != COHERIT_OK) { free_handle(h); return rc; }
+  *out = h;
+  return COHERIT_OK;
+}
+
+int coherit_geno_create_bed(const uint8_t* bed, int64_t bed_bytes, int64_t n_full, int64_t m,
+                            const int32_t* keep, int64_t n_keep, const int32_t* component_sizes,
+                            int32_t n_components, int device, void* stream,
+                            coherit_geno_t** out) {
+  CO_CHECK(out != nullptr, COHERIT_E_SHAPE, "out handle pointer is NULL");
+  *out = nullptr;
+  CO_CHECK(bed != nullptr && n_full > 0 && m > 0, COHERIT_E_SHAPE,
+           "BED input needs a buffer, n > 0 and m > 0");
+  const int64_t bps = (n_full + 3) / 4;
+  CO_CHECK(bed_bytes >= 3 + bps * m, COHERIT_E_SHAPE,
+           "BED buffer holds %lld bytes, expected %lld for n=%lld, m=%lld",
+           (long long)bed_bytes, (long long)(3 + bps * m), (long long)n_full, (long long)m);
+  CO_CHECK(bed[0] == 0x6C && bed[1] == 0x1B && bed[2] == 0x01, COHERIT_E_SHAPE,
+           "Not a valid SNP-major BED file");
+  const int64_t n = keep ? n_keep : n_full;
+  CO_CHECK(n > 0 && n < (int64_t(1) << 31), COHERIT_E_SHAPE, "sample count %lld out of range",
+           (long long)n);
+  if (keep)
+    for (int64_t i = 0; i < n; ++i)
+      CO_CHECK(keep[i] >= 0 && keep[i] < n_full, COHERIT_E_INDEX, "kept sample %lld out of range",
+               (long long)i);
+  std::vector<int64_t> comp_m;
+  if (component_sizes == nullptr || n_components <= 1) {
+    comp_m.push_back(m);
+  } else {
+    int64_t tot = 0;
+    for (int g = 0; g < n_components; ++g) {
+      CO_CHECK(component_sizes[g] > 0, COHERIT_E_SHAPE, "component %d has no SNPs", g);
+      comp_m.push_back(component_sizes[g]);
+      tot += component_sizes[g];
+    }
+    CO_CHECK(tot <= m, COHERIT_E_SHAPE, "components cover %lld SNPs, the BED has %lld",
+             (long long)tot, (long long)m);
+  }
+  coherit_geno* h = new coherit_geno();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = alloc_common(h, n, comp_m, device);
+  if (rc != COHERIT_OK) { free_handle(h); return rc; }
+  // Cache SNP s of component g sits at slot comp_slot_start[g] + (s - comp_snp_start[g]).
+  std::vector<int32_t> slot_of_snp(h->m);
+  for (int g = 0; g < h->G; ++g)
+    for (int64_t s = h->comp_snp_start[g]; s < h->comp_snp_start[g + 1]; ++s)
+      slot_of_snp[s] = static_cast<int32_t>(h->comp_slot_start[g] + (s - h->comp_snp_start[g]));
+  int32_t* d_keep = nullptr;
+  if (keep) {
+    cudaError_t e = cudaMalloc(&d_keep, sizeof(int32_t) * n);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_keep, keep, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { cudaFree(d_keep); free_handle(h); return cuda_status(e, "keep list"); }
+  }
+  rc = build_layout_from_bed(h, bed + 3, bps, d_keep, slot_of_snp, st);
+  if (d_keep) {
+    cudaStreamSynchronize(st);
+    cudaFree(d_keep);
   }
   if (rc == COHERIT_OK) rc = finish_create(h, st);
   if (rc != COHERIT_OK) { free_handle(h); return rc; }

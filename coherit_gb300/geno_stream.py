@@ -258,8 +258,27 @@ class GenoBlockStreamer:
             and self._sample_mask is None
             and cache_to_source is None
         )
+        from .bed import BedSource
+
+        bed_direct = isinstance(source, BedSource) and cache_to_source is None
         with torch.cuda.device(self.dev):
-            if synthetic:
+            if bed_direct:
+                # PLINK BED bytes go to the device as they are and are
+                # transcoded there (no host repacking).
+                sizes_arr = np.asarray(sizes, dtype=np.int32)
+                keep = (None if self._sample_mask is None
+                        else np.ascontiguousarray(np.flatnonzero(self._sample_mask), dtype=np.int32))
+                raw = source.raw_bytes()
+                _lib.check(
+                    self._lib.coherit_geno_create_bed(
+                        raw.ctypes.data, int(raw.size), self._source_n, self.source_m,
+                        None if keep is None else keep.ctypes.data,
+                        0 if keep is None else int(keep.size), sizes_arr.ctypes.data, len(sizes),
+                        self.dev.index, stream, C.byref(self._handle),
+                    ),
+                    "create genotypes from BED",
+                )
+            elif synthetic:
                 sizes_arr = np.asarray(sizes, dtype=np.int32)
                 _lib.check(
                     self._lib.coherit_geno_create_synthetic(

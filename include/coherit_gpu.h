@@ -88,6 +88,19 @@ int coherit_geno_create_packed(const uint8_t* packed, int64_t n, int32_t n_calls
                                int32_t n_components, int packed_on_device, int device,
                                void* stream, coherit_geno_t** out);
 
+/* Build the resident matrix directly from a PLINK 1 SNP-major .bed file held
+ * in host memory (`bed`, `bed_bytes` bytes including the 3-byte header; n_full
+ * samples, m SNP records), transcoding BED codes 0,1,2,3 to allele counts
+ * 2, missing, 1, 0 on the device in chunks of whole SNP records.  keep: host
+ * list of n_keep source sample indices to retain (NULL = all).  Components as
+ * in coherit_geno_create_synthetic (contiguous SNP ranges).  Replaces the
+ * host transcode of the reference's cache build (geno_stream.py:709-745,
+ * :1594-1846).  Synchronises `stream`.                                       */
+int coherit_geno_create_bed(const uint8_t* bed, int64_t bed_bytes, int64_t n_full, int64_t m,
+                            const int32_t* keep, int64_t n_keep, const int32_t* component_sizes,
+                            int32_t n_components, int device, void* stream,
+                            coherit_geno_t** out);
+
 /* Build a synthetic resident matrix (no host copy): per-SNP MAF ~ U(0.05, 0.5)
  * and genotypes ~ Binomial(2, MAF) drawn from a counter-based hash of
  * (seed, snp, sample); `missing_q24` = missing rate * 2^24 (0 = none).  The
