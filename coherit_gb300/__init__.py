@@ -39,6 +39,10 @@ _EXPORTS: dict[str, str] = {
     "SmileBlockWeightedOperator": ".smile_block_w",
     "SmileMultiBlockWeightedOperator": ".smile_block_w",
     "ServeResult": ".serving",
+    "run_continuous_gwas": ".gwas",
+    "marginal_scan": ".gwas",
+    "solve_hinv_columns_batched": ".hinv",
+    "compute_projected_hinv_vector": ".hinv",
 }
 
 __all__ = list(_EXPORTS)
