@@ -19,7 +19,9 @@ Arms:
              ``plain_fp32_single_fit``), the operator roofline at the batched
              width, and the CPU baseline (the oracle's FP32 restatement of
              kv_impl_streamed, timed on a bounded sample and scaled by the
-             operator work of one fit).
+             operator work of one fit).  ``sparse12`` times the rare-variant
+             operator (per-SNP entry lists, MAF~U(0.0005,0.01)) at the same
+             n x m and width as the roofline.
   reference  ``--impl reference``: the CPU restatement of the reference path
              (the reference itself needs jax/numba, absent on these machines)
              on all host cores, on bounded samples of the same workload.
@@ -257,6 +259,55 @@ def operator_roofline(st, k, hbm_peak, tensor_peak, reps=10):
     return roof
 
 
+def sparse12_operator(n, m, k, hbm_peak, dense_ms, seed, reps=10):
+    """The rare-variant (sparse12) operator at the headline shape: n samples x
+    m SNPs with MAF ~ U(0.0005, 0.01) held as per-SNP entry lists in HBM
+    (built on the device by the generator), K V and Z^T V at width k timed
+    with CUDA events on the launching stream.  Algorithmic bytes of K V:
+    4 per stored entry + 16 per SNP (offsets, mean, inv) + 8nk (V read, out
+    written); the gathers / scatter-adds of 2 x 4k bytes per entry run out of
+    L2 (V and out are L2-resident), so the L2 rate is reported beside the HBM
+    fraction."""
+    import torch
+
+    from coherit_gb300.sparse_stream import SparseGenoBlockStreamer, SyntheticRareSource
+
+    t0 = time.perf_counter()
+    sp = SparseGenoBlockStreamer(SyntheticRareSource(n, m, seed=seed, maf_range=(0.0005, 0.01)))
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    nnz = sp.info()["nnz"]
+    V = torch.randn(n, k, device=sp.dev)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    kv_ms = timed(lambda: sp.kv(V))
+    xtv_ms = timed(lambda: sp.xtv(V))
+    alg = 4 * nnz + 16 * m + 8 * n * k
+    gbs = alg / (kv_ms * 1e-3) / 1e9
+    l2_tbs = 2 * 4 * nnz * k / (kv_ms * 1e-3) / 1e12
+    sp.close()
+    return {"workload": f"n{n}_m{m}_rare_maf0.0005-0.01", "n": n, "m": m, "entries": nnz,
+            "k": k, "build_s": round(build_s, 3), "kv_ms": round(kv_ms, 3),
+            "xtv_ms": round(xtv_ms, 3), "dense_kv_ms_same_shape": round(dense_ms, 3),
+            "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm_peak,
+                         "unit": "GB/s", "frac": round(gbs / hbm_peak, 4), "traffic": None,
+                         "kernel": "sparse K V (prep + fused gather/scatter + finish)",
+                         "algorithmic_bytes": alg, "l2_gather_scatter_TBps": round(l2_tbs, 2)}}
+
+
 def serve_step(srv, ys, Xs, host: bool):
     """One step: all R requests submitted at once; returns their results."""
     if host:
@@ -438,6 +489,10 @@ def run_ours(args, wl):
             rate = args.stream_rate
             stream = serving_stream(st, wl, args.stream, rate, seed=wl.seed + 99,
                                     max_active=R)
+        sparse = None
+        if not args.no_sparse:
+            sparse = sparse12_operator(wl.n, wl.m, k_typ, hbm_peak, roof["ms_per_application"],
+                                       seed=wl.seed + 7)
         cpu = None
         if not args.no_cpu:
             t_fit, cores, sample = cpu_fit_estimate(wl, fit_apps, fit_cols)
@@ -476,6 +531,7 @@ def run_ours(args, wl):
             "serving_stream": stream,
             "single_fit_mixed": single,
             "plain_fp32_single_fit": plain,
+            "sparse12": sparse,
             "cpu_baseline": cpu,
             "clocks": clocks,
         }
@@ -575,6 +631,22 @@ def run_operator_only(args, wl):
             "gpu_launches": int(launches), "peak_source": peak_src}
 
 
+def run_sparse_only(args, wl):
+    """Rare-variant operator micro-benchmark (``--sparse K``) at the
+    workload's n x m (or --n/--m), as reported in the ``sparse12`` object of
+    the full run.  Used for kernel profiles."""
+    import torch
+
+    torch.cuda.set_device(0)
+    n, m = args.n or wl.n, args.m or wl.m
+    hbm_peak, _, peak_src = _peaks()
+    out = sparse12_operator(n, m, args.sparse, hbm_peak, float("nan"), seed=wl.seed + 7,
+                            reps=max(1, args.steps))
+    out.pop("dense_kv_ms_same_shape")
+    out["peak_source"] = peak_src
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -596,6 +668,8 @@ def main():
     ap.add_argument("--no-single", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-sparse", action="store_true",
+                    help="skip the rare-variant (sparse12) operator measurement")
     # Operator work of one warm c2 fit, as counted on the GPU path (same
     # algorithm and probe settings as the reference's single fit).
     ap.add_argument("--ref-apps", type=float, default=52.0,
@@ -604,14 +678,18 @@ def main():
                     help="right-hand-side columns per fit assumed by the reference arm")
     ap.add_argument("--operator", type=int, default=0, metavar="K",
                     help="time bare operator applications of width K instead of fits")
-    ap.add_argument("--n", type=int, default=0, help="with --operator: samples")
-    ap.add_argument("--m", type=int, default=0, help="with --operator: SNPs")
+    ap.add_argument("--sparse", type=int, default=0, metavar="K",
+                    help="time the rare-variant operator at width K instead of fits")
+    ap.add_argument("--n", type=int, default=0, help="with --operator/--sparse: samples")
+    ap.add_argument("--m", type=int, default=0, help="with --operator/--sparse: SNPs")
     args = ap.parse_args()
     from coherit_gb300.configs import WORKLOADS
 
     wl = WORKLOADS[args.config]
     if args.operator > 0:
         out = run_operator_only(args, wl)
+    elif args.sparse > 0:
+        out = run_sparse_only(args, wl)
     elif args.impl == "reference":
         out = run_reference(args, wl)
     else:

@@ -43,6 +43,8 @@ _EXPORTS: dict[str, str] = {
     "marginal_scan": ".gwas",
     "solve_hinv_columns_batched": ".hinv",
     "compute_projected_hinv_vector": ".hinv",
+    "SparseGenoBlockStreamer": ".sparse_stream",
+    "SyntheticRareSource": ".sparse_stream",
 }
 
 __all__ = list(_EXPORTS)

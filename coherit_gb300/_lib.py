@@ -103,6 +103,23 @@ _SIGNATURES = {
         [_i64, _i32, _p, _i64, _p, _i64, _p, _p, _p, _p, _p, _p, _p],
     ),
     "coherit_selftest_mma": (C.c_int, [_i32, _p, _p]),
+    "coherit_sparse_create_bed": (
+        C.c_int,
+        [_p, _i64, _i64, _i64, _p, _i64, C.c_int, _p, _p],
+    ),
+    "coherit_sparse_create_synthetic": (
+        C.c_int,
+        [_i64, _i64, _u64, _u32, _u32, _u32, C.c_int, _p, _p],
+    ),
+    "coherit_sparse_create_csc": (C.c_int, [_i64, _i64, _p, _p, _p, C.c_int, _p, _p]),
+    "coherit_sparse_destroy": (C.c_int, [_p]),
+    "coherit_sparse_info": (C.c_int, [_p, _p, _p, _p, _p, _p]),
+    "coherit_sparse_stats": (C.c_int, [_p, _p, _p, _p, _p, _p, _p, _p]),
+    "coherit_sparse_read_csc": (C.c_int, [_p, _p, _p, _p]),
+    "coherit_sparse_kv": (C.c_int, [_p, _p, _i64, _i32, C.c_double, _f32, _p, _i64, _p]),
+    "coherit_sparse_xtv": (C.c_int, [_p, _p, _i64, _i32, C.c_double, _p, _i64, _p]),
+    "coherit_sparse_extract_columns": (C.c_int, [_p, _p, _i32, _p, _i64, _p]),
+    "coherit_sparse_exact_diag": (C.c_int, [_p, _p, _p]),
 }
 
 

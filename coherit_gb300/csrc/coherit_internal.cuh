@@ -81,16 +81,61 @@ __host__ __device__ __forceinline__ uint32_t synth_maf_q24(uint64_t seed, int64_
   return 838861u + static_cast<uint32_t>((h >> 20) % 7549747ull);
 }
 
+// MAF of SNP s on a 2^24 scale, uniform on [lo, lo + span) (rare variants).
+__host__ __device__ __forceinline__ uint32_t synth_maf_q24_range(uint64_t seed, int64_t s,
+                                                                 uint32_t lo, uint32_t span) {
+  const uint64_t h = splitmix64(seed * 0xD1B54A32D192ED03ull + static_cast<uint64_t>(s));
+  return lo + static_cast<uint32_t>((h >> 20) % static_cast<uint64_t>(span));
+}
+
+// Per-SNP key of the generator: splitmix64(seed ^ s * C).
+__host__ __device__ __forceinline__ uint64_t synth_snp_key(uint64_t seed, int64_t s) {
+  return splitmix64(seed ^ (static_cast<uint64_t>(s) * 0x8CB92BA72F3D8DD7ull));
+}
+
+// Genotype code of sample i of the SNP with key `ks`.
+__host__ __device__ __forceinline__ uint32_t synth_code_keyed(uint64_t ks, int64_t i,
+                                                              uint32_t maf_q24, uint32_t miss_q24) {
+  const uint64_t h = splitmix64(ks ^ (static_cast<uint64_t>(i) * 0x9E3779B97F4A7C15ull));
+  const uint32_t a1 = (static_cast<uint32_t>(h) & 0xFFFFFFu) < maf_q24;
+  const uint32_t a2 = (static_cast<uint32_t>(h >> 24) & 0xFFFFFFu) < maf_q24;
+  if (miss_q24 != 0u && static_cast<uint32_t>(h >> 48) * 256u < miss_q24) return 3u;
+  return a1 + a2;
+}
+
 // Genotype code of (sample i, SNP s): 0/1/2 allele count, 3 missing.
 __host__ __device__ __forceinline__ uint32_t synth_code(uint64_t seed, int64_t s, int64_t i,
                                                         uint32_t maf_q24, uint32_t miss_q24) {
-  const uint64_t key = splitmix64(seed ^ (static_cast<uint64_t>(s) * 0x8CB92BA72F3D8DD7ull)) ^
-                       (static_cast<uint64_t>(i) * 0x9E3779B97F4A7C15ull);
+  const uint64_t key = synth_snp_key(seed, s) ^ (static_cast<uint64_t>(i) * 0x9E3779B97F4A7C15ull);
   const uint64_t h = splitmix64(key);
   const uint32_t a1 = (static_cast<uint32_t>(h) & 0xFFFFFFu) < maf_q24;
   const uint32_t a2 = (static_cast<uint32_t>(h >> 24) & 0xFFFFFFu) < maf_q24;
   if (miss_q24 != 0u && static_cast<uint32_t>(h >> 48) * 256u < miss_q24) return 3u;
   return a1 + a2;
+}
+
+// ------------------------------------------- FP32 per-SNP standardisation
+// Reference FP32 standardisation from genotype counts over n_sub samples
+// (geno_stream.py:1780-1792, sparse_stream.py:726-735), evaluated with
+// explicitly rounded operations so that no multiply-add contraction changes
+// the rounding.  n1 / n2 / n3 = het, hom-alt and missing counts.
+__device__ __forceinline__ void ref_fp32_standardize(int64_t n_sub, int64_t n1, int64_t n2,
+                                                     int64_t n3, float& mean, float& inv) {
+  const long long cnt = static_cast<long long>(n_sub - n3);
+  const long long s1 = static_cast<long long>(n1 + 2 * n2);
+  const long long s2 = static_cast<long long>(n1 + 4 * n2);
+  const float cnt_f = __ll2float_rn(cnt);
+  const float s1_f = __ll2float_rn(s1);
+  const float s2_f = __ll2float_rn(s2);
+  const float denom = fmaxf(cnt_f, 1.0f);
+  const float mu = __fdiv_rn(s1_f, denom);
+  const float t1 = __fdiv_rn(s2_f, denom);
+  const float t2 = __fmul_rn(mu, mu);
+  const float var = fmaxf(__fsub_rn(t1, t2), 0.0f);
+  const bool valid = (cnt_f > 0.0f) && (var > 0.0f);
+  const float sd = __fsqrt_rn(fmaxf(var, 1e-6f));
+  mean = mu;
+  inv = valid ? __fdiv_rn(1.0f, sd) : 0.0f;
 }
 
 // ------------------------------------------------------------- handle

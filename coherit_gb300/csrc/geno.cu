@@ -255,9 +255,7 @@ __global__ void k_slot_counts(const uint8_t* __restrict__ geno_t, int64_t m_pad,
   n3o[j] = a3;
 }
 
-// Reference FP32 standardisation (geno_stream.py:1780-1792), evaluated with
-// explicitly rounded operations so that no multiply-add contraction changes
-// the rounding.
+// Reference FP32 standardisation of every slot (padding slots get 0, 0).
 __global__ void k_slot_stats(int64_t m_pad, int64_t n_sub, const int64_t* __restrict__ n1,
                              const int64_t* __restrict__ n2, const int64_t* __restrict__ n3,
                              const int32_t* __restrict__ snp_of_slot, float* __restrict__ mean,
@@ -269,21 +267,7 @@ __global__ void k_slot_stats(int64_t m_pad, int64_t n_sub, const int64_t* __rest
     inv[j] = 0.f;
     return;
   }
-  const long long cnt = static_cast<long long>(n_sub - n3[j]);
-  const long long s1 = static_cast<long long>(n1[j] + 2 * n2[j]);
-  const long long s2 = static_cast<long long>(n1[j] + 4 * n2[j]);
-  const float cnt_f = __ll2float_rn(cnt);
-  const float s1_f = __ll2float_rn(s1);
-  const float s2_f = __ll2float_rn(s2);
-  const float denom = fmaxf(cnt_f, 1.0f);
-  const float mu = __fdiv_rn(s1_f, denom);
-  const float t1 = __fdiv_rn(s2_f, denom);
-  const float t2 = __fmul_rn(mu, mu);
-  const float var = fmaxf(__fsub_rn(t1, t2), 0.0f);
-  const bool valid = (cnt_f > 0.0f) && (var > 0.0f);
-  const float sd = __fsqrt_rn(fmaxf(var, 1e-6f));
-  mean[j] = mu;
-  inv[j] = valid ? __fdiv_rn(1.0f, sd) : 0.0f;
+  ref_fp32_standardize(n_sub, n1[j], n2[j], n3[j], mean[j], inv[j]);
 }
 
 // Missing-genotype counts per sample (copy S rows).

@@ -3,7 +3,9 @@
 Binds resident genotype streamers to ``fit_reml`` exactly as the reference
 assembles its operator bundle for dense streamers (reml_model.py:962-1390):
 one streamer (optionally partitioned into components, giving a one-pass
-weighted H.V and a stacked K_g V), or several streamers (one per GRM).  The
+weighted H.V and a stacked K_g V), or several streamers (one per GRM), with
+rare-variant sparse streamers appended after the dense ones as further GRMs
+(reml_model.py:611-666, :1196-1290).  The
 projected-core preconditioner is built from a Nystrom basis of the
 reference kernel sum_g theta_ref,g K_g and the per-component projected cores
 (reml_model.py:863-960).
@@ -31,7 +33,12 @@ logger = logging.getLogger(__name__)
 class FitConfig:
     """Subset of the reference FitConfig (reml_model.py:34-83) used by the GPU path."""
 
+    bed_prefix: str | Sequence[str] = ""
     sources: Sequence | None = None
+    # Rare-variant sparse sources, one genetic component each
+    # (reml_model.py:34-38, :611-666).
+    rare_bed_prefix: str | Sequence[str] = ""
+    rare_sources: Sequence | None = None
     vc_block_sizes: Sequence[int] | None = None
     component_variant_indices: Sequence[Sequence[int]] | None = None
     sample_mask: np.ndarray | None = None
@@ -151,6 +158,11 @@ def _solve_small_spd(A: torch.Tensor, b: torch.Tensor, *, base_jitter=1e-6, max_
     raise FloatingPointError("GLS system is not positive definite.")
 
 
+def _prefix_list(prefix) -> list:
+    items = list(prefix) if isinstance(prefix, (list, tuple)) else [prefix]
+    return [str(p) for p in items if p]
+
+
 @dataclasses.dataclass(frozen=True)
 class _OperatorBundle:
     K_mvs: tuple
@@ -165,19 +177,35 @@ class InfinitesimalREMLFitter:
 
     def __init__(self, cfg: FitConfig, streamers: Sequence[GenoBlockStreamer] | None = None):
         self.cfg = cfg
+        rare_prefixes = _prefix_list(cfg.rare_bed_prefix)
+        has_rare = cfg.rare_sources is not None or bool(rare_prefixes)
         if streamers is None:
-            if not cfg.sources:
-                raise ValueError("FitConfig.sources or explicit streamers are required.")
-            streamers = [
-                GenoBlockStreamer(
-                    src, call_width=cfg.call_width, component_block_sizes=cfg.vc_block_sizes,
-                    component_variant_indices=cfg.component_variant_indices,
-                    sample_mask=cfg.sample_mask, device=cfg.device, precision=cfg.precision)
-                for src in cfg.sources
-            ]
+            dense_kw = dict(call_width=cfg.call_width, component_block_sizes=cfg.vc_block_sizes,
+                            component_variant_indices=cfg.component_variant_indices,
+                            sample_mask=cfg.sample_mask, device=cfg.device,
+                            precision=cfg.precision)
+            streamers = [GenoBlockStreamer(src, **dense_kw) for src in (cfg.sources or ())]
+            streamers += [GenoBlockStreamer(bed_prefix=p, **dense_kw)
+                          for p in _prefix_list(cfg.bed_prefix)]
+            if has_rare:
+                from .sparse_stream import SparseGenoBlockStreamer
+
+                rare_kw = dict(call_width=cfg.call_width, sample_mask=cfg.sample_mask,
+                               device=cfg.device, gpu_budget_bytes=cfg.gpu_budget_bytes,
+                               mixed_dense_sparse=bool(streamers))
+                streamers += [SparseGenoBlockStreamer(src, **rare_kw)
+                              for src in (cfg.rare_sources or ())]
+                streamers += [SparseGenoBlockStreamer(bed_prefix=p, **rare_kw)
+                              for p in rare_prefixes]
         self.streamers = list(streamers)
         if not self.streamers:
-            raise ValueError("at least one streamer is required")
+            raise ValueError("At least one dense or sparse genotype source is required.")
+        sparse_flags = [bool(getattr(s, "has_sparse_backend", False)) for s in self.streamers]
+        self._n_dense_streamers = sparse_flags.index(True) if any(sparse_flags) else len(sparse_flags)
+        if any(not f for f in sparse_flags[self._n_dense_streamers:]):
+            raise ValueError("Sparse (rare-variant) streamers must follow the dense streamers.")
+        self._has_sparse = any(sparse_flags)
+        self._sparse_streamers = tuple(self.streamers[self._n_dense_streamers:])
         ns = {int(s.n) for s in self.streamers}
         if len(ns) != 1:
             raise ValueError("all streamers must share the sample set")
@@ -211,6 +239,8 @@ class InfinitesimalREMLFitter:
             raise ValueError("SMILE diag mode must be 'full' or 'mean'.")
         if cfg.vc_block_sizes is not None or cfg.component_variant_indices is not None:
             raise ValueError("SMILE block-W mode cannot be combined with component partitioning.")
+        if self._has_sparse:
+            raise ValueError("SMILE block-W mode is currently supported only for dense-only fits.")
         if len(self.streamers) != 1:
             raise ValueError("SMILE block-W mode needs exactly one dense streamer.")
         from .smile_block_w import SmileBlockWeightedOperator, SmileMultiBlockWeightedOperator
@@ -326,7 +356,7 @@ class InfinitesimalREMLFitter:
         if self._smile_operators:
             def K_ref(V):
                 return ops.weighted_hv(theta_ref, None, V)
-        elif len(self.streamers) == 1:
+        elif len(self.streamers) == 1 and not self._has_sparse:
             st = self.streamers[0]
             eff = st._component_eff_m_host.astype(np.float64)
 
@@ -499,6 +529,10 @@ class InfinitesimalREMLFitter:
         """X_test b + Z_test beta on the test samples with the training
         standardisation (reml_model.py:1646-1818): one Z b pass per test
         streamer, the components as columns of b."""
+        if self._has_sparse or getattr(test_fitter, "_has_sparse", False):
+            raise NotImplementedError(
+                "Prediction currently supports dense genotype paths only; sparse test prediction "
+                "is not implemented.")
         if not self.streamers or not test_fitter.streamers:
             raise RuntimeError("Prediction requires initialized training and test streamers.")
         _validate_dense_prediction_streamers(self.streamers, test_fitter.streamers)

@@ -1,0 +1,412 @@
+"""Rare-variant sparse genotype streamer with the reference's call surface.
+
+``SparseGenoBlockStreamer`` mirrors the reference's sparse streamer
+(sparse_stream.py:804-1469): same constructor arguments, per-SNP statistics,
+call-block descriptors, ``sparse_block_metadata`` and operator methods.  The
+reference keeps host CSC shards and ``device_put``s them for every operator
+application (sparse_stream.py:1147-1222, :1344-1388).  Here the non-zero
+genotypes are built once into per-SNP entry lists resident in HBM (from
+PLINK BED bytes on the device, or from any variant-major source on the
+host), and ``kv`` / ``xtv`` are a fused gather / scatter pass over them on
+the caller's current CUDA stream.
+
+Every streamer is one genetic component (its own m_eff), exactly as the
+reference appends sparse streamers after the dense ones
+(reml_model.py:611-666, :1196-1290).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .block_backend import Sparse12BlockDescriptor
+from .geno_stream import _build_call_geometry, _device_of, _pack_lut, as_rhs
+
+_MISSING = 3
+
+
+class SyntheticRareSource:
+    """Generator-backed rare-variant source: MAF ~ U(maf_lo, maf_hi) per SNP,
+    Binomial(2, MAF) genotypes from the counter-based hash of
+    ``coherit_gb300.synth``.  The streamer builds its entries directly on the
+    device from the same hash (no host copy of the genotypes)."""
+
+    def __init__(self, n: int, m: int, seed: int = 0, maf_range=(0.0005, 0.01),
+                 missing_rate: float = 0.0):
+        from .synth import maf_range_q24, missing_rate_q24
+
+        self.n = int(n)
+        self.m = int(m)
+        self.seed = int(seed)
+        self.maf_range_q24 = maf_range_q24(*maf_range)
+        self.missing_q24 = missing_rate_q24(missing_rate)
+        self.missing_val = -127
+        self.sample_ids = None
+
+    def read_block_variant_major(self, start: int, count: int) -> np.ndarray:
+        from .synth import genotype_codes
+
+        codes = genotype_codes(self.seed, self.n, np.arange(start, start + count),
+                               self.missing_q24, self.maf_range_q24)
+        out = codes.T.astype(np.int8)
+        out[codes.T == _MISSING] = self.missing_val
+        return out
+
+
+def _entries_from_block(block_vm: np.ndarray, lut: np.ndarray):
+    """(w, n) variant-major block -> per-SNP counts, sample rows and values
+    (1 het, 2 hom-alt, 3 missing) in SNP-then-sample order
+    (sparse_stream.py:336-411, :447-469)."""
+    codes = lut[np.asarray(block_vm).view(np.uint8)]
+    snp, row = np.nonzero(codes)
+    counts = np.bincount(snp, minlength=codes.shape[0]).astype(np.int64)
+    return counts, row.astype(np.int32), codes[snp, row].astype(np.int8)
+
+
+class SparseGenoBlockStreamer:
+    """HBM-resident rare-variant operator with the reference's interface."""
+
+    def __init__(
+        self,
+        source=None,
+        *,
+        bed_prefix: str | None = None,
+        call_width: int = 131072,
+        device=None,
+        keep_host_stats: bool = True,
+        build_threads: int | None = None,
+        sample_mask: np.ndarray | None = None,
+        ring_depth: int | None = None,
+        gpu_budget_bytes: float | None = None,
+        mixed_dense_sparse: bool = False,
+        source_build_chunk_width: int | None = None,
+    ):
+        if source is not None and bed_prefix is not None:
+            raise ValueError("Provide either source or bed_prefix, not both.")
+        if source is None:
+            if bed_prefix is None:
+                raise ValueError("Either source or bed_prefix must be provided.")
+            from .bed import BedSource
+
+            source = BedSource(bed_prefix)
+        self._lib = _lib.load()
+        self.dev = _device_of(device)
+        self.keep_host_stats = bool(keep_host_stats)
+        self.bed_prefix = bed_prefix
+        self._gpu_budget_bytes = gpu_budget_bytes
+        self._mixed_dense_sparse = bool(mixed_dense_sparse)
+        self._source_n = int(source.n)
+        self.source_m = int(source.m)
+        self._sample_mask = None if sample_mask is None else np.asarray(sample_mask, dtype=bool)
+        if self._sample_mask is not None and self._sample_mask.shape != (self._source_n,):
+            raise ValueError(
+                "sample_mask is incompatible with the supplied source: "
+                f"mask length={self._sample_mask.size}, source.n={self._source_n}."
+            )
+        self.n = int(self._sample_mask.sum()) if self._sample_mask is not None else self._source_n
+        if self.n <= 0:
+            raise ValueError("Genotype source must contain at least one selected sample.")
+        if self.source_m <= 0:
+            raise ValueError("Genotype source must contain at least one variant.")
+        sample_ids = getattr(source, "sample_ids", None)
+        self.sample_ids = (
+            None if sample_ids is None else
+            tuple(s for s, k in zip(sample_ids, self._sample_mask) if k)
+            if self._sample_mask is not None else tuple(sample_ids)
+        )
+        self._missing_val = np.uint8(_MISSING)
+        self.m = self.source_m
+        self.call_width = max(1, int(call_width))
+        self.block_size = self.call_width
+        (self._block_starts, self._block_sizes, self._call_component_ids,
+         self._component_call_offsets) = _build_call_geometry(self.m, self.call_width, [self.m])
+        self._n_calls = int(self._block_starts.size)
+        self._call_true_widths = self._block_sizes.copy()
+        self._call_snp_starts = self._block_starts.astype(np.int32)
+        self._component_block_sizes = [self.m]
+        self._component_snp_offsets = np.asarray([0, self.m], dtype=np.int32)
+
+        self._handle = C.c_void_p()
+        self._closed = False
+        stream = _lib.stream_ptr()
+        from .bed import BedSource
+
+        with torch.cuda.device(self.dev):
+            if isinstance(source, SyntheticRareSource) and self._sample_mask is None:
+                lo, hi = source.maf_range_q24
+                _lib.check(
+                    self._lib.coherit_sparse_create_synthetic(
+                        self.n, self.m, source.seed, lo, hi, source.missing_q24, self.dev.index,
+                        stream, C.byref(self._handle)),
+                    "create synthetic sparse genotypes")
+            elif isinstance(source, BedSource):
+                keep = (None if self._sample_mask is None
+                        else np.ascontiguousarray(np.flatnonzero(self._sample_mask), dtype=np.int32))
+                raw = source.raw_bytes()
+                _lib.check(
+                    self._lib.coherit_sparse_create_bed(
+                        raw.ctypes.data, int(raw.size), self._source_n, self.source_m,
+                        None if keep is None else keep.ctypes.data,
+                        0 if keep is None else int(keep.size), self.dev.index, stream,
+                        C.byref(self._handle)),
+                    "create sparse genotypes from BED")
+            else:
+                col_off, rows, vals = self._entries_from_source(source)
+                _lib.check(
+                    self._lib.coherit_sparse_create_csc(
+                        self.n, self.m, col_off.ctypes.data, rows.ctypes.data, vals.ctypes.data,
+                        self.dev.index, stream, C.byref(self._handle)),
+                    "create sparse genotypes")
+            self._refresh_stats()
+        self._exact_diag_dev = None
+        self.op_stats = {"apps": 0, "cols": 0}
+
+    # ------------------------------------------------------------ building
+    def _entries_from_source(self, source):
+        lut = _pack_lut(int(source.missing_val))
+        counts, rows, vals = [], [], []
+        for c in range(self._n_calls):
+            s0 = int(self._call_snp_starts[c])
+            w = int(self._call_true_widths[c])
+            blk = np.asarray(source.read_block_variant_major(s0, w))
+            if self._sample_mask is not None:
+                blk = blk[:, self._sample_mask]
+            cnt, r, v = _entries_from_block(np.ascontiguousarray(blk), lut)
+            counts.append(cnt)
+            rows.append(r)
+            vals.append(v)
+        col_off = np.zeros(self.m + 1, dtype=np.int64)
+        np.cumsum(np.concatenate(counts), out=col_off[1:])
+        return (col_off, np.ascontiguousarray(np.concatenate(rows), dtype=np.int32),
+                np.ascontiguousarray(np.concatenate(vals), dtype=np.int8))
+
+    def _refresh_stats(self) -> None:
+        m = self.m
+        mean = np.zeros(m, dtype=np.float32)
+        inv = np.zeros(m, dtype=np.float32)
+        het = np.zeros(m, dtype=np.int64)
+        hom = np.zeros(m, dtype=np.int64)
+        miss = np.zeros(m, dtype=np.int64)
+        eff = C.c_double()
+        atom = C.c_double()
+        _lib.check(self._lib.coherit_sparse_stats(
+            self._h(), mean.ctypes.data, inv.ctypes.data, het.ctypes.data, hom.ctypes.data,
+            miss.ctypes.data, C.byref(eff), C.byref(atom)), "sparse stats")
+        cnt = (self.n - miss).astype(np.int32)
+        self._means_host = mean if self.keep_host_stats else None
+        self._inv_sds_host = inv if self.keep_host_stats else None
+        self._count_host = cnt if self.keep_host_stats else None
+        self._nnz_het_by_snp, self._nnz_hom_by_snp, self._nnz_miss_by_snp = het, hom, miss
+        self._eff_m_host = float(eff.value)
+        self._mean_diag_atom_host = float(atom.value)
+        self._component_eff_m_host = np.asarray([self._eff_m_host], dtype=np.float32)
+        self._component_mean_diag_atoms_host = np.asarray([self._mean_diag_atom_host],
+                                                          dtype=np.float32)
+        self._eff_m_const = torch.tensor(self._eff_m_host, dtype=torch.float32, device=self.dev)
+        self._component_eff_m_const = torch.as_tensor(self._component_eff_m_host, device=self.dev)
+        # Per-call summaries (sparse_stream.py:885-898) and descriptors (:845-880).
+        summary = []
+        for c in range(self._n_calls):
+            s0 = int(self._call_snp_starts[c])
+            s1 = s0 + int(self._call_true_widths[c])
+            nh, nd = int(het[s0:s1].sum()), int(hom[s0:s1].sum())
+            nm = int(miss[s0:s1].sum())
+            summary.append({"nnz_het": nh, "nnz_hom": nd, "nnz_miss": nm, "has_missing": nm > 0,
+                            "skip_kv": bool(nh == 0 and nd == 0 and not np.any(inv[s0:s1]))})
+        self._sparse_block_summary = summary
+        self._block_backend_plan = tuple(
+            Sparse12BlockDescriptor(
+                call_idx=c, snp_start=int(self._call_snp_starts[c]),
+                true_width=int(self._call_true_widths[c]), nnz_het=summary[c]["nnz_het"],
+                nnz_hom=summary[c]["nnz_hom"], has_csc=True, has_csr=False, idx_dtype="int32",
+                storage="hbm_resident_entries")
+            for c in range(self._n_calls))
+        self._sparse_total_nnz_het = int(het.sum())
+        self._sparse_total_nnz_hom = int(hom.sum())
+
+    # ------------------------------------------------------------ helpers
+    def _h(self):
+        if self._closed or not self._handle:
+            raise RuntimeError("SparseGenoBlockStreamer is closed.")
+        return self._handle
+
+    def close(self) -> None:
+        if not self._closed and self._handle:
+            self._lib.coherit_sparse_destroy(self._handle)
+        self._closed = True
+        self._handle = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h()
+
+    @property
+    def n_components(self) -> int:
+        return 1
+
+    @property
+    def has_component_partition(self) -> bool:
+        return False
+
+    @property
+    def has_arbitrary_component_partition(self) -> bool:
+        return False
+
+    @property
+    def has_sparse_backend(self) -> bool:
+        return True
+
+    def block_backend_plan(self):
+        return self._block_backend_plan
+
+    def sparse_block_metadata(self):
+        """Per-call het / hom / missing entry counts (sparse_stream.py:963-964)."""
+        return self._sparse_block_summary
+
+    def info(self) -> dict:
+        vals = [C.c_int64() for _ in range(5)]
+        _lib.check(self._lib.coherit_sparse_info(self._h(), *(C.byref(v) for v in vals)))
+        return dict(n=vals[0].value, m=vals[1].value, nnz=vals[2].value,
+                    n_missing=vals[3].value, device_bytes=vals[4].value)
+
+    def read_entries(self):
+        """Host copy of the resident entries: (col_off, rows, vals)."""
+        nnz = self.info()["nnz"]
+        col_off = np.empty(self.m + 1, dtype=np.int64)
+        rows = np.empty(nnz, dtype=np.int32)
+        vals = np.empty(nnz, dtype=np.int8)
+        _lib.check(self._lib.coherit_sparse_read_csc(
+            self._h(), col_off.ctypes.data, rows.ctypes.data, vals.ctypes.data), "read entries")
+        return col_off, rows, vals
+
+    def _inv_eff(self) -> float:
+        return 1.0 / self._eff_m_host if self._eff_m_host > 0 else 1.0
+
+    def _apply_kv(self, V, scale: float, theta_e: float | None):
+        V, squeeze = as_rhs(V, self.dev)
+        if V.shape[0] != self.n:
+            raise ValueError(f"V has {V.shape[0]} rows, expected n={self.n}")
+        k = int(V.shape[1])
+        out = torch.empty((self.n, k), dtype=torch.float32, device=self.dev)
+        self.op_stats["apps"] += 1
+        self.op_stats["cols"] += k
+        _lib.check(self._lib.coherit_sparse_kv(
+            self._h(), V.data_ptr(), k, k, float(scale),
+            0.0 if theta_e is None else float(theta_e), out.data_ptr(), k, _lib.stream_ptr()),
+            "sparse kv")
+        return out[:, 0] if squeeze else out
+
+    # ------------------------------------------------------------ operators
+    def kv(self, V, normalize: bool = True, *, sum_v=None, precision=None):
+        """K V = Z Z^T V / m_eff (sparse_stream.py:1344-1388).  ``sum_v`` is
+        accepted for call compatibility; the column sums are formed on the
+        device in the same launch sequence.  ``precision`` is ignored (the
+        sparse path computes in FP32 with FP64 per-SNP terms)."""
+        return self._apply_kv(V, self._inv_eff() if normalize else 1.0, None)
+
+    def component_kv(self, V, component_idx: int, normalize: bool = True, *, precision=None):
+        if component_idx != 0:
+            raise IndexError(f"component_idx={component_idx} out of range for 1 component.")
+        return self.kv(V, normalize)
+
+    def stacked_component_kv(self, V, normalize: bool = True, *, precision=None):
+        return self.kv(V, normalize)[None]
+
+    def weighted_component_hv(self, theta_g, theta_e, V, *, precision=None):
+        """theta_g K V (+ theta_e V) in one pass over the entries."""
+        tg = np.asarray(theta_g.detach().cpu() if isinstance(theta_g, torch.Tensor) else theta_g,
+                        dtype=np.float64).reshape(-1)
+        if tg.size != 1:
+            raise ValueError(f"theta_g length mismatch: expected 1, got {tg.size}.")
+        te = None
+        if theta_e is not None:
+            te = float(theta_e.detach().cpu().reshape(-1)[0]) if isinstance(theta_e, torch.Tensor) \
+                else float(np.asarray(theta_e).reshape(-1)[0])
+        scale = float(tg[0]) / self._eff_m_host if self._eff_m_host > 0 else 0.0
+        return self._apply_kv(V, scale, te)
+
+    def xtv(self, V, normalize: bool = False, *, precision=None):
+        """Standardised Z^T V (m x k) (sparse_stream.py:1390-1421)."""
+        V, squeeze = as_rhs(V, self.dev)
+        if V.shape[0] != self.n:
+            raise ValueError(f"V has {V.shape[0]} rows, expected n={self.n}")
+        k = int(V.shape[1])
+        out = torch.empty((self.m, k), dtype=torch.float32, device=self.dev)
+        s = self._inv_eff() if normalize else 1.0
+        _lib.check(self._lib.coherit_sparse_xtv(
+            self._h(), V.data_ptr(), k, k, float(s), out.data_ptr(), k, _lib.stream_ptr()),
+            "sparse xtv")
+        return out[:, 0] if squeeze else out
+
+    def diag(self) -> torch.Tensor:
+        """Mean diagonal atom tr(K)/n (geno_stream.py:2773-2778)."""
+        return torch.tensor(self._mean_diag_atom_host, dtype=torch.float32, device=self.dev)
+
+    def component_diag_list(self) -> list:
+        return [self.diag()]
+
+    def standardized_columns(self, snp_indices) -> torch.Tensor:
+        """Device FP32 (n, len(snp_indices)) standardised columns (missing -> 0)."""
+        idx = np.asarray(snp_indices, dtype=np.int64).reshape(-1)
+        if idx.size and (idx.min() < 0 or idx.max() >= self.m):
+            raise IndexError(f"SNP indices must lie in [0, {self.m}).")
+        out = torch.empty((self.n, idx.size), dtype=torch.float32, device=self.dev)
+        if idx.size == 0:
+            return out
+        idx_dev = torch.as_tensor(idx, device=self.dev)
+        _lib.check(self._lib.coherit_sparse_extract_columns(
+            self._h(), idx_dev.data_ptr(), int(idx.size), out.data_ptr(), int(idx.size),
+            _lib.stream_ptr()), "sparse extract columns")
+        return out
+
+    def extract_standardized_columns(self, snp_indices: np.ndarray) -> np.ndarray:
+        """Host FP32 standardised columns (sparse_stream.py:893-961)."""
+        return self.standardized_columns(snp_indices).cpu().numpy()
+
+    def exact_diag(self, *, target_block_bytes: int = 256 * 1024 * 1024) -> torch.Tensor:
+        """Sample-wise diagonal of the GRM, cached (geno_stream.py:2780-2821)."""
+        if self._exact_diag_dev is not None:
+            return self._exact_diag_dev
+        out = torch.empty(self.n, dtype=torch.float32, device=self.dev)
+        _lib.check(self._lib.coherit_sparse_exact_diag(self._h(), out.data_ptr(),
+                                                       _lib.stream_ptr()), "sparse exact_diag")
+        self._exact_diag_dev = out
+        return out
+
+    def build_projected_core_atom(self, U, *, subtract_identity: bool = True):
+        """U^T K U (- I) (sparse_stream.py:1423-1461, kv_impl.py:829-849)."""
+        U = torch.as_tensor(U, dtype=torch.float32, device=self.dev)
+        if U.ndim != 2:
+            raise ValueError("build_projected_core_atom expects U with shape (n, k).")
+        blk = self.xtv(U)
+        core = blk.T @ blk
+        if self._eff_m_host <= 0:
+            return torch.zeros_like(core)
+        core = core / self._eff_m_host
+        if subtract_identity:
+            core = core - torch.eye(core.shape[0], device=core.device, dtype=core.dtype)
+        return core
+
+    def build_projected_core_atoms(self, U, *, subtract_identity: bool = True):
+        return self.build_projected_core_atom(U, subtract_identity=subtract_identity)[None]
+
+    def _prepare_kv_pass(self) -> None:
+        self._h()
+
+
+__all__ = ["SparseGenoBlockStreamer", "SyntheticRareSource"]

@@ -21,14 +21,27 @@ def _splitmix64(x: np.ndarray) -> np.ndarray:
     return x ^ (x >> _U(31))
 
 
-def maf_q24(seed: int, snps) -> np.ndarray:
+COMMON_MAF_Q24 = (838861, 838861 + 7549747)  # [0.05, 0.5)
+
+
+def maf_q24(seed: int, snps, maf_range_q24=COMMON_MAF_Q24) -> np.ndarray:
+    """Per-SNP MAF on a 2^24 scale, uniform on [lo, hi) of ``maf_range_q24``."""
+    lo, hi = (int(x) for x in maf_range_q24)
     s = np.asarray(snps, dtype=np.uint64)
     with np.errstate(over="ignore"):
         h = _splitmix64(np.full(s.shape, seed, dtype=np.uint64) * _U(0xD1B54A32D192ED03) + s)
-    return (_U(838861) + (h >> _U(20)) % _U(7549747)).astype(np.uint32)
+    return (_U(lo) + (h >> _U(20)) % _U(hi - lo)).astype(np.uint32)
 
 
-def genotype_codes(seed: int, n: int, snps, missing_q24: int = 0) -> np.ndarray:
+def maf_range_q24(lo: float, hi: float) -> tuple:
+    """MAF interval [lo, hi) on the generator's 2^24 scale."""
+    if not 0.0 <= lo < hi <= 0.5:
+        raise ValueError("MAF range must satisfy 0 <= lo < hi <= 0.5")
+    return int(round(lo * (1 << 24))), int(round(hi * (1 << 24)))
+
+
+def genotype_codes(seed: int, n: int, snps, missing_q24: int = 0,
+                   maf_range_q24=COMMON_MAF_Q24) -> np.ndarray:
     """Codes (n x len(snps), uint8; 3 = missing) of the given SNP indices."""
     s = np.asarray(snps, dtype=np.uint64).reshape(-1)
     i = np.arange(n, dtype=np.uint64)
@@ -36,7 +49,7 @@ def genotype_codes(seed: int, n: int, snps, missing_q24: int = 0) -> np.ndarray:
         key_s = _splitmix64(np.full(s.shape, seed, dtype=np.uint64) ^ (s * _U(0x8CB92BA72F3D8DD7)))
         key = key_s[None, :] ^ (i[:, None] * _U(0x9E3779B97F4A7C15))
     h = _splitmix64(key)
-    maf = maf_q24(seed, s).astype(np.uint64)[None, :]
+    maf = maf_q24(seed, s, maf_range_q24).astype(np.uint64)[None, :]
     codes = ((h & _U(0xFFFFFF)) < maf).astype(np.uint8) + (
         ((h >> _U(24)) & _U(0xFFFFFF)) < maf
     ).astype(np.uint8)

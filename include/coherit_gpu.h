@@ -264,6 +264,75 @@ int coherit_pcg_direction_update(int64_t n, int32_t k, float* P, int64_t ldp,
                                  const double* rnorm2, double* rs_old, const double* threshold,
                                  uint8_t* active, double* rnorm_out, void* stream);
 
+/* ------------------------------------------- rare-variant sparse operator */
+
+/* Rare-variant ("sparse12") genotype matrix: per-SNP lists of the non-zero
+ * genotypes (het = 1, hom-alt = 2, missing = 3, samples ascending) resident
+ * in HBM, replacing SparseGenoBlockStreamer's host CSC shards and their
+ * per-pass device_put (sparse_stream.py:804-1222).                          */
+typedef struct coherit_sparse coherit_sparse_t;
+
+/* Build from a PLINK 1 SNP-major .bed held in host memory (layout and keep
+ * list as coherit_geno_create_bed), counting and then filling the entries on
+ * the device in chunks of whole SNP records (the single-pass raw-BED build of
+ * sparse_stream.py:518-606, :711-801).  Synchronises `stream`.              */
+int coherit_sparse_create_bed(const uint8_t* bed, int64_t bed_bytes, int64_t n_full, int64_t m,
+                              const int32_t* keep, int64_t n_keep, int device, void* stream,
+                              coherit_sparse_t** out);
+
+/* Build a synthetic rare-variant matrix on the device (no host copy): per-SNP
+ * MAF ~ U[maf_lo_q24, maf_hi_q24) / 2^24 and genotypes ~ Binomial(2, MAF)
+ * from the counter-based hash of coherit_geno_create_synthetic (same key per
+ * (seed, snp, sample)), `missing_q24` = missing rate * 2^24.  The generator
+ * is restated in the oracle.  Synchronises `stream`.                        */
+int coherit_sparse_create_synthetic(int64_t n, int64_t m, uint64_t seed, uint32_t maf_lo_q24,
+                                    uint32_t maf_hi_q24, uint32_t missing_q24, int device,
+                                    void* stream, coherit_sparse_t** out);
+
+/* Build from host entry lists (any other genotype source): col_off[m+1]
+ * offsets, rows[nnz] sample indices < n, vals[nnz] in {1, 2, 3}
+ * (the packed het/hom/missing orders of sparse_stream.py:671-708).          */
+int coherit_sparse_create_csc(int64_t n, int64_t m, const int64_t* col_off, const int32_t* rows,
+                              const int8_t* vals, int device, void* stream,
+                              coherit_sparse_t** out);
+
+int coherit_sparse_destroy(coherit_sparse_t* h);
+
+/* Samples, SNPs, stored entries, missing entries, bytes held on the device. */
+int coherit_sparse_info(const coherit_sparse_t* h, int64_t* n, int64_t* m, int64_t* nnz,
+                        int64_t* n_missing, int64_t* device_bytes);
+
+/* Host copies of the FP32 mean / inverse sd and the het / hom / missing
+ * counts (m each, any may be NULL), m_eff (SNPs with inv > 0) and the mean
+ * diagonal atom (sparse_stream.py:726-742, geno_stream.py:1409-1420).      */
+int coherit_sparse_stats(const coherit_sparse_t* h, float* mean, float* inv, int64_t* n_het,
+                         int64_t* n_hom, int64_t* n_miss, double* eff_m, double* mean_diag_atom);
+
+/* Host copy of the entries: col_off[m+1], rows[nnz], vals[nnz].            */
+int coherit_sparse_read_csc(const coherit_sparse_t* h, int64_t* col_off, int32_t* rows,
+                            int8_t* vals);
+
+/* out (n x k, ldo) = scale * Z Z^T V + theta_e * V for device V (n x k, ldv)
+ * (kv_impl.py:777-905, sparse_stream.py:1344-1388 with scale = theta/m_eff).
+ * out must not alias V.  Asynchronous on `stream`.                         */
+int coherit_sparse_kv(coherit_sparse_t* h, const float* V, int64_t ldv, int32_t k, double scale,
+                      float theta_e, float* out, int64_t ldo, void* stream);
+
+/* out (m x k, ldo) = scale * Z^T V (kv_impl.py:752-827,
+ * sparse_stream.py:1390-1421).  Asynchronous on `stream`.                  */
+int coherit_sparse_xtv(coherit_sparse_t* h, const float* V, int64_t ldv, int32_t k, double scale,
+                       float* out, int64_t ldo, void* stream);
+
+/* Standardised FP32 columns (n x count, ldo) of the SNPs in device array
+ * snp_idx; missing genotypes give 0, an index outside [0, m) gives a NaN
+ * column (sparse_stream.py:893-961).                                        */
+int coherit_sparse_extract_columns(coherit_sparse_t* h, const int64_t* snp_idx, int32_t count,
+                                   float* out, int64_t ldo, void* stream);
+
+/* Exact diagonal of Z Z^T / m_eff into device out[n], accumulated in FP64
+ * (geno_stream.py:2780-2821).                                               */
+int coherit_sparse_exact_diag(coherit_sparse_t* h, float* out, void* stream);
+
 /* One-tile tensor-core self-test (no counterpart in the reference): computes
  * D(128x16) = A(128x16) B(16x16)^T for fixed small integers with A taken from
  * tensor memory (variant 0) or shared memory (variant 1) and copies D to
