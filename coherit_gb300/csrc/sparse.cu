@@ -38,6 +38,8 @@ struct coherit_sparse {
   double* d_ws = nullptr;  // sum(V)[k_cap] then c[k_cap]
   int32_t k_cap = 0;
   double* d_diag = nullptr;  // n, exact diagonal accumulator
+  float* d_stage = nullptr;  // padded copies of V and out for k % 4 != 0 / unaligned rows
+  size_t stage_bytes = 0;
   int sm_count = 0;
   int64_t device_bytes = 0;
 };
@@ -197,38 +199,6 @@ __global__ void k_prep(const float* __restrict__ V, int64_t ldv, int64_t n, int3
   }
 }
 
-__device__ __forceinline__ float4 ld4(const float* p, int nv, bool vec) {
-  if (vec && nv == 4) return __ldg(reinterpret_cast<const float4*>(p));
-  float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (nv > 0) r.x = __ldg(p);
-  if (nv > 1) r.y = __ldg(p + 1);
-  if (nv > 2) r.z = __ldg(p + 2);
-  if (nv > 3) r.w = __ldg(p + 3);
-  return r;
-}
-
-__device__ __forceinline__ void st4(float* p, float4 v, int nv, bool vec) {
-  if (vec && nv == 4) {
-    *reinterpret_cast<float4*>(p) = v;
-    return;
-  }
-  if (nv > 0) p[0] = v.x;
-  if (nv > 1) p[1] = v.y;
-  if (nv > 2) p[2] = v.z;
-  if (nv > 3) p[3] = v.w;
-}
-
-__device__ __forceinline__ void red4(float* p, float4 v, int nv, bool vec) {
-  if (vec && nv == 4) {
-    atomicAdd(reinterpret_cast<float4*>(p), v);
-    return;
-  }
-  if (nv > 0) atomicAdd(p, v.x);
-  if (nv > 1) atomicAdd(p + 1, v.y);
-  if (nv > 2) atomicAdd(p + 2, v.z);
-  if (nv > 3) atomicAdd(p + 3, v.w);
-}
-
 __device__ __forceinline__ float entry_x(uint32_t e, float mu) {
   const uint32_t v = e & 3u;
   return v == 3u ? mu : static_cast<float>(v);
@@ -255,30 +225,24 @@ struct ApplyArgs {
   float* out;
   int64_t ldo;
   double* corr;
-  int vec_in;
-  int vec_out;
 };
 
-// Gather / scatter of the 4 columns [col, col + nv) of one row.  VEC: all
-// four columns exist (k % 4 == 0) and rows are 16-byte aligned, so one vector
-// access; otherwise per-column accesses.
-template <bool VEC>
-__device__ __forceinline__ float4 gather4(const float* p, int nv) {
-  if constexpr (VEC) return __ldg(reinterpret_cast<const float4*>(p));
-  return ld4(p, nv, false);
+__device__ __forceinline__ float4 gather4(const float* p) {
+  return __ldg(reinterpret_cast<const float4*>(p));
 }
 
-template <bool VEC>
-__device__ __forceinline__ void scatter4(float* p, float4 v, int nv) {
-  if constexpr (VEC) atomicAdd(reinterpret_cast<float4*>(p), v);
-  else red4(p, v, nv, false);
+__device__ __forceinline__ void scatter4(float* p, float4 v) {
+  atomicAdd(reinterpret_cast<float4*>(p), v);
 }
 
 // KV = false: out (m x k) = scale Z^T V.  KV = true: out (n x k) += scale Z Z^T V
 // without the rank-one term, whose vector c is accumulated into corr.
-// Lanes whose 4 columns lie beyond k skip the entry loops entirely, so the
-// loops of the active lanes stay branch-free with 4 gathers in flight.
-template <int L, bool KV, bool VEC>
+// Requires k % 4 == 0 and 16-byte aligned rows of V and out (the host
+// stages other blocks through padded buffers), so every access is one
+// 128-bit gather / store / atomic add.  Lanes whose 4 columns lie beyond k
+// skip the entry loops entirely, so the loops of the active lanes stay
+// branch-free with 4 gathers in flight.
+template <int L, bool KV>
 __global__ void __launch_bounds__(256) k_apply(const ApplyArgs a) {
   constexpr int E = 32 / L;  // entries in flight per warp step
   const int lane = threadIdx.x & 31;
@@ -287,17 +251,16 @@ __global__ void __launch_bounds__(256) k_apply(const ApplyArgs a) {
   const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   for (int c0 = 0; c0 < a.k; c0 += 4 * L) {
     const int col = c0 + 4 * q;
-    const int nv = max(0, min(4, a.k - col));
-    const bool active = nv > 0;
+    const bool active = col < a.k;
     double sv[4];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) sv[t] = t < nv ? a.sumv[col + t] : 0.0;
+    for (int t = 0; t < 4; ++t) sv[t] = active ? a.sumv[col + t] : 0.0;
     double cacc[4] = {0.0, 0.0, 0.0, 0.0};
     for (int64_t j = w0; j < a.m; j += nw) {
       const float iv = a.inv[j];
       if (!(iv != 0.f)) {
         if (!KV && g == 0 && active)
-          st4(a.out + j * a.ldo + col, make_float4(0.f, 0.f, 0.f, 0.f), nv, VEC);
+          *reinterpret_cast<float4*>(a.out + j * a.ldo + col) = make_float4(0.f, 0.f, 0.f, 0.f);
         continue;
       }
       const float mu = a.mean[j];
@@ -309,10 +272,10 @@ __global__ void __launch_bounds__(256) k_apply(const ApplyArgs a) {
         for (; p + 3 * E < p1; p += 4 * E) {
           const uint32_t e0 = __ldg(a.entry + p), e1 = __ldg(a.entry + p + E);
           const uint32_t e2 = __ldg(a.entry + p + 2 * E), e3 = __ldg(a.entry + p + 3 * E);
-          const float4 v0 = gather4<VEC>(Vc + static_cast<int64_t>(e0 >> 2) * a.ldv, nv);
-          const float4 v1 = gather4<VEC>(Vc + static_cast<int64_t>(e1 >> 2) * a.ldv, nv);
-          const float4 v2 = gather4<VEC>(Vc + static_cast<int64_t>(e2 >> 2) * a.ldv, nv);
-          const float4 v3 = gather4<VEC>(Vc + static_cast<int64_t>(e3 >> 2) * a.ldv, nv);
+          const float4 v0 = gather4(Vc + static_cast<int64_t>(e0 >> 2) * a.ldv);
+          const float4 v1 = gather4(Vc + static_cast<int64_t>(e1 >> 2) * a.ldv);
+          const float4 v2 = gather4(Vc + static_cast<int64_t>(e2 >> 2) * a.ldv);
+          const float4 v3 = gather4(Vc + static_cast<int64_t>(e3 >> 2) * a.ldv);
           fma4(acc, entry_x(e0, mu), v0);
           fma4(acc, entry_x(e1, mu), v1);
           fma4(acc, entry_x(e2, mu), v2);
@@ -320,7 +283,7 @@ __global__ void __launch_bounds__(256) k_apply(const ApplyArgs a) {
         }
         for (; p < p1; p += E) {
           const uint32_t e = __ldg(a.entry + p);
-          fma4(acc, entry_x(e, mu), gather4<VEC>(Vc + static_cast<int64_t>(e >> 2) * a.ldv, nv));
+          fma4(acc, entry_x(e, mu), gather4(Vc + static_cast<int64_t>(e >> 2) * a.ldv));
         }
       }
 #pragma unroll
@@ -338,10 +301,9 @@ __global__ void __launch_bounds__(256) k_apply(const ApplyArgs a) {
       const double s3 = div * (static_cast<double>(acc.w) - dmu * sv[3]);
       if (!KV) {
         if (g == 0)
-          st4(a.out + j * a.ldo + col,
+          *reinterpret_cast<float4*>(a.out + j * a.ldo + col) =
               make_float4(static_cast<float>(a.scale * s0), static_cast<float>(a.scale * s1),
-                          static_cast<float>(a.scale * s2), static_cast<float>(a.scale * s3)),
-              nv, VEC);
+                          static_cast<float>(a.scale * s2), static_cast<float>(a.scale * s3));
         continue;
       }
       const double f = a.scale * div;
@@ -359,30 +321,28 @@ __global__ void __launch_bounds__(256) k_apply(const ApplyArgs a) {
         const uint32_t e0 = __ldg(a.entry + p), e1 = __ldg(a.entry + p + E);
         const uint32_t e2 = __ldg(a.entry + p + 2 * E), e3 = __ldg(a.entry + p + 3 * E);
         float x = entry_x(e0, mu);
-        scatter4<VEC>(Oc + static_cast<int64_t>(e0 >> 2) * a.ldo,
-                      make_float4(x * wv.x, x * wv.y, x * wv.z, x * wv.w), nv);
+        scatter4(Oc + static_cast<int64_t>(e0 >> 2) * a.ldo,
+                      make_float4(x * wv.x, x * wv.y, x * wv.z, x * wv.w));
         x = entry_x(e1, mu);
-        scatter4<VEC>(Oc + static_cast<int64_t>(e1 >> 2) * a.ldo,
-                      make_float4(x * wv.x, x * wv.y, x * wv.z, x * wv.w), nv);
+        scatter4(Oc + static_cast<int64_t>(e1 >> 2) * a.ldo,
+                      make_float4(x * wv.x, x * wv.y, x * wv.z, x * wv.w));
         x = entry_x(e2, mu);
-        scatter4<VEC>(Oc + static_cast<int64_t>(e2 >> 2) * a.ldo,
-                      make_float4(x * wv.x, x * wv.y, x * wv.z, x * wv.w), nv);
+        scatter4(Oc + static_cast<int64_t>(e2 >> 2) * a.ldo,
+                      make_float4(x * wv.x, x * wv.y, x * wv.z, x * wv.w));
         x = entry_x(e3, mu);
-        scatter4<VEC>(Oc + static_cast<int64_t>(e3 >> 2) * a.ldo,
-                      make_float4(x * wv.x, x * wv.y, x * wv.z, x * wv.w), nv);
+        scatter4(Oc + static_cast<int64_t>(e3 >> 2) * a.ldo,
+                      make_float4(x * wv.x, x * wv.y, x * wv.z, x * wv.w));
       }
       for (; p < p1; p += E) {
         const uint32_t e = __ldg(a.entry + p);
         const float x = entry_x(e, mu);
-        scatter4<VEC>(Oc + static_cast<int64_t>(e >> 2) * a.ldo,
-                      make_float4(x * wv.x, x * wv.y, x * wv.z, x * wv.w), nv);
+        scatter4(Oc + static_cast<int64_t>(e >> 2) * a.ldo,
+                      make_float4(x * wv.x, x * wv.y, x * wv.z, x * wv.w));
       }
     }
-    if (KV && g == 0) {
-      if (nv > 0) atomicAdd(a.corr + col, cacc[0]);
-      if (nv > 1) atomicAdd(a.corr + col + 1, cacc[1]);
-      if (nv > 2) atomicAdd(a.corr + col + 2, cacc[2]);
-      if (nv > 3) atomicAdd(a.corr + col + 3, cacc[3]);
+    if (KV && g == 0 && active) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) atomicAdd(a.corr + col + t, cacc[t]);
     }
   }
 }
@@ -463,6 +423,7 @@ void free_sparse(coherit_sparse* h) {
   cudaFree(h->d_inv);
   cudaFree(h->d_ws);
   cudaFree(h->d_diag);
+  cudaFree(h->d_stage);
   delete h;
 }
 
@@ -545,45 +506,46 @@ inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 
 // One full wave of a persistent grid: every SM holds as many 256-thread
 // blocks of this kernel as its registers allow, and each warp strides over
 // the SNPs (a partial second wave of equal-work blocks would idle SMs).
-template <int L, bool KV, bool VEC>
+template <int L, bool KV>
 void launch_one(int sm_count, int64_t m, const ApplyArgs& a, cudaStream_t st) {
   static int per_sm = 0;
   if (per_sm == 0) {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_apply<L, KV, VEC>, 256, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_apply<L, KV>, 256, 0) !=
             cudaSuccess || nb < 1)
       nb = 1;
     per_sm = nb;
   }
   const unsigned grid = blocks_for(std::max<int64_t>(m, 1) * 32, 256,
                                    static_cast<int64_t>(sm_count) * per_sm);
-  k_apply<L, KV, VEC><<<grid, 256, 0, st>>>(a);
-}
-
-template <bool KV, bool VEC>
-void launch_apply_t(int sm_count, int64_t m, const ApplyArgs& a, cudaStream_t st) {
-  const int k = a.k;
-  if (k <= 4)
-    launch_one<1, KV, VEC>(sm_count, m, a, st);
-  else if (k <= 8)
-    launch_one<2, KV, VEC>(sm_count, m, a, st);
-  else if (k <= 16)
-    launch_one<4, KV, VEC>(sm_count, m, a, st);
-  else if (k <= 32)
-    launch_one<8, KV, VEC>(sm_count, m, a, st);
-  else
-    launch_one<16, KV, VEC>(sm_count, m, a, st);
+  k_apply<L, KV><<<grid, 256, 0, st>>>(a);
 }
 
 template <bool KV>
 int launch_apply(coherit_sparse* h, const ApplyArgs& a, cudaStream_t st) {
-  // Vector accesses need every 4-column group complete and 16-byte rows.
-  if (a.k % 4 == 0 && a.vec_in && a.vec_out)
-    launch_apply_t<KV, true>(h->sm_count, h->m, a, st);
+  const int k = a.k;
+  if (k <= 4)
+    launch_one<1, KV>(h->sm_count, h->m, a, st);
+  else if (k <= 8)
+    launch_one<2, KV>(h->sm_count, h->m, a, st);
+  else if (k <= 16)
+    launch_one<4, KV>(h->sm_count, h->m, a, st);
+  else if (k <= 32)
+    launch_one<8, KV>(h->sm_count, h->m, a, st);
   else
-    launch_apply_t<KV, false>(h->sm_count, h->m, a, st);
+    launch_one<16, KV>(h->sm_count, h->m, a, st);
   note_launch();
   CO_CUDA(cudaGetLastError());
+  return COHERIT_OK;
+}
+
+int ensure_stage(coherit_sparse* h, size_t bytes) {
+  if (bytes <= h->stage_bytes) return COHERIT_OK;
+  cudaFree(h->d_stage);
+  h->d_stage = nullptr;
+  h->stage_bytes = 0;
+  CO_CUDA(cudaMalloc(&h->d_stage, bytes));
+  h->stage_bytes = bytes;
   return COHERIT_OK;
 }
 
@@ -597,29 +559,54 @@ int sparse_apply(coherit_sparse* h, bool kv, const float* V, int64_t ldv, int32_
   CO_CHECK(static_cast<const void*>(V) != static_cast<const void*>(out), COHERIT_E_SHAPE,
            "out must not alias V");
   CO_CUDA(cudaSetDevice(h->device));
-  int rc = ensure_ws(h, k);
+  const int64_t out_rows = kv ? h->n : h->m;
+  // The kernels take k % 4 == 0 and 16-byte rows; other blocks go through a
+  // zero-padded staging copy of V and of the output.
+  const bool direct = k % 4 == 0 && aligned16(V) && ldv % 4 == 0 && aligned16(out) &&
+                      ldo % 4 == 0;
+  const float* Vr = V;
+  float* outr = out;
+  int64_t ldvr = ldv, ldor = ldo;
+  int32_t kr = k;
+  int rc = COHERIT_OK;
+  if (!direct) {
+    kr = (k + 3) / 4 * 4;
+    const size_t vfl = static_cast<size_t>(h->n) * kr;
+    rc = ensure_stage(h, sizeof(float) * (vfl + static_cast<size_t>(out_rows) * kr));
+    if (rc != COHERIT_OK) return rc;
+    float* vs = h->d_stage;
+    if (kr != k) CO_CUDA(cudaMemsetAsync(vs, 0, sizeof(float) * vfl, st));
+    CO_CUDA(cudaMemcpy2DAsync(vs, sizeof(float) * kr, V, sizeof(float) * ldv, sizeof(float) * k,
+                              h->n, cudaMemcpyDeviceToDevice, st));
+    Vr = vs;
+    outr = h->d_stage + vfl;
+    ldvr = ldor = kr;
+  }
+  rc = ensure_ws(h, kr);
   if (rc != COHERIT_OK) return rc;
   double* sumv = h->d_ws;
   double* corr = h->d_ws + h->k_cap;
   CO_CUDA(cudaMemsetAsync(h->d_ws, 0, sizeof(double) * 2 * h->k_cap, st));
   const dim3 blk(32, 8);
-  const dim3 grd(static_cast<unsigned>((k + 31) / 32),
+  const dim3 grd(static_cast<unsigned>((kr + 31) / 32),
                  static_cast<unsigned>(std::min<int64_t>((h->n + 63) / 64, 4096)));
-  k_prep<<<grd, blk, 0, st>>>(V, ldv, h->n, k, theta_e, kv ? out : nullptr, ldo, sumv); note_launch();
+  k_prep<<<grd, blk, 0, st>>>(Vr, ldvr, h->n, kr, theta_e, kv ? outr : nullptr, ldor, sumv); note_launch();
   CO_CUDA(cudaGetLastError());
   if (h->m > 0 && h->eff > 0.0) {
-    ApplyArgs a{h->d_col_off, h->d_entry, h->d_mean, h->d_inv, h->m, V, ldv, k, sumv, scale,
-                out, ldo, corr, (aligned16(V) && ldv % 4 == 0) ? 1 : 0,
-                (aligned16(out) && ldo % 4 == 0) ? 1 : 0};
+    ApplyArgs a{h->d_col_off, h->d_entry, h->d_mean, h->d_inv, h->m, Vr, ldvr, kr, sumv, scale,
+                outr, ldor, corr};
     rc = kv ? launch_apply<true>(h, a, st) : launch_apply<false>(h, a, st);
     if (rc != COHERIT_OK) return rc;
     if (kv) {
-      k_finish<<<grd, blk, 0, st>>>(out, ldo, h->n, k, corr); note_launch();
+      k_finish<<<grd, blk, 0, st>>>(outr, ldor, h->n, kr, corr); note_launch();
       CO_CUDA(cudaGetLastError());
     }
   } else if (!kv && h->m > 0) {
-    CO_CUDA(cudaMemset2DAsync(out, sizeof(float) * ldo, 0, sizeof(float) * k, h->m, st));
+    CO_CUDA(cudaMemset2DAsync(outr, sizeof(float) * ldor, 0, sizeof(float) * kr, h->m, st));
   }
+  if (!direct && out_rows > 0)
+    CO_CUDA(cudaMemcpy2DAsync(out, sizeof(float) * ldo, outr, sizeof(float) * kr,
+                              sizeof(float) * k, out_rows, cudaMemcpyDeviceToDevice, st));
   return COHERIT_OK;
 }
 

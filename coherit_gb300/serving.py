@@ -87,7 +87,7 @@ class _Target:
 
 
 class _Op:
-    __slots__ = ("req", "V", "scale", "theta_e", "done", "out", "error")
+    __slots__ = ("req", "V", "scale", "theta_e", "done", "out", "error", "next_col", "cols_done")
 
     def __init__(self, req, V, scale, theta_e):
         self.req = req
@@ -97,6 +97,8 @@ class _Op:
         self.done = threading.Event()
         self.out = None
         self.error = None
+        self.next_col = 0   # first column not yet placed in a launch
+        self.cols_done = 0  # columns whose results are back
 
 
 class _Batcher:
@@ -104,6 +106,11 @@ class _Batcher:
 
     A launch goes out when every active fit has an application pending, or
     ``window_s`` after the first pending one arrived, whichever is first.
+    Launches are filled to ``max_cols`` columns: an application whose block
+    does not fit the rest of a launch is split by columns, its first columns
+    riding in this launch and the others in the next (the operator acts on
+    columns independently), so every launch but the last of a round streams
+    the genotypes for a full-width block.
     """
 
     def __init__(self, streamer: GenoBlockStreamer, precision: str, window_s: float,
@@ -134,6 +141,9 @@ class _Batcher:
         if V2.shape[0] != req.n_sub:
             raise ValueError(f"V has {V2.shape[0]} rows, the request has {req.n_sub} samples")
         op = _Op(req, V2, float(scale), None if theta_e is None else float(theta_e))
+        op.out = torch.empty_like(V2)
+        if V2.shape[1] == 0:
+            return op.out[:, 0] if vec else op.out
         with self.cv:
             if self.stop:
                 raise RuntimeError("REMLServer is closed.")
@@ -150,7 +160,8 @@ class _Batcher:
             self.cv.notify_all()
         self.thread.join(timeout=30)
 
-    def _take(self) -> list[_Op]:
+    def _take(self) -> list[tuple]:
+        """Pieces (op, first column, last column + 1) of the next launch."""
         with self.cv:
             while not self.pending and not self.stop:
                 self.cv.wait()
@@ -162,60 +173,69 @@ class _Batcher:
                 if left <= 0:
                     break
                 self.cv.wait(timeout=left)
-            batch, rest, cols = [], [], 0
-            for op in self.pending:
-                k = op.V.shape[1]
-                if batch and cols + k > self.max_cols:
-                    rest.append(op)
-                else:
-                    batch.append(op)
-                    cols += k
-            self.pending = rest
-            return batch
+            pieces, cols = [], 0
+            while self.pending and cols < self.max_cols:
+                op = self.pending[0]
+                lo = op.next_col
+                hi = min(op.V.shape[1], lo + self.max_cols - cols)
+                pieces.append((op, lo, hi))
+                cols += hi - lo
+                op.next_col = hi
+                if hi == op.V.shape[1]:
+                    self.pending.pop(0)
+            return pieces
 
     def _loop(self) -> None:
         while True:
-            batch = self._take()
-            if not batch:
+            pieces = self._take()
+            if not pieces:
                 return
             try:
-                self._launch(batch)
-            except BaseException as err:  # handed to every fit in the batch
-                for op in batch:
-                    op.error = err
-            for op in batch:
-                op.done.set()
+                self._launch(pieces)
+            except BaseException as err:  # handed to every fit in the launch
+                with self.cv:
+                    for op, _, _ in pieces:
+                        op.error = err
+                        if op in self.pending:
+                            self.pending.remove(op)
+                for op, _, _ in pieces:
+                    op.done.set()
+                continue
+            for op, lo, hi in pieces:
+                op.cols_done += hi - lo
+                if op.cols_done == op.V.shape[1]:
+                    op.done.set()
 
-    def _launch(self, batch: list[_Op]) -> None:
+    def _launch(self, pieces: list[tuple]) -> None:
         st = self.st
-        widths = [op.V.shape[1] for op in batch]
+        widths = [hi - lo for _, lo, hi in pieces]
         K = int(sum(widths))
-        col_start = np.zeros(len(batch) + 1, dtype=np.int32)
+        col_start = np.zeros(len(pieces) + 1, dtype=np.int32)
         col_start[1:] = np.cumsum(widths)
         Vf = torch.zeros((st.n, K), dtype=torch.float32, device=st.dev)
-        for op, c0, k in zip(batch, col_start[:-1], widths):
+        for (op, lo, hi), c0 in zip(pieces, col_start[:-1]):
             if op.req.idx is None:
-                Vf[:, c0:c0 + k] = op.V
+                Vf[:, c0:c0 + hi - lo] = op.V[:, lo:hi]
             else:
-                Vf[op.req.idx, c0:c0 + k] = op.V
-        slots = np.asarray([op.req.slot for op in batch], dtype=np.int32)
-        scale = np.asarray([op.scale for op in batch], dtype=np.float32)
-        te = np.asarray([0.0 if op.theta_e is None else op.theta_e for op in batch],
+                Vf[op.req.idx, c0:c0 + hi - lo] = op.V[:, lo:hi]
+        slots = np.asarray([op.req.slot for op, _, _ in pieces], dtype=np.int32)
+        scale = np.asarray([op.scale for op, _, _ in pieces], dtype=np.float32)
+        te = np.asarray([0.0 if op.theta_e is None else op.theta_e for op, _, _ in pieces],
                         dtype=np.float32)
         out = torch.empty_like(Vf)
         with self.lib_lock:
             _lib.check(_lib.load().coherit_geno_kv_batched(
-                st.handle, len(batch), col_start.ctypes.data, slots.ctypes.data, self.prec,
+                st.handle, len(pieces), col_start.ctypes.data, slots.ctypes.data, self.prec,
                 Vf.data_ptr(), K, K, scale.ctypes.data, te.ctypes.data, out.data_ptr(), K,
                 _lib.stream_ptr()), "batched kv")
         st.op_stats["apps"] += 1
         st.op_stats["cols"] += K
         self.launches += 1
         self.columns += K
-        self.requests_per_launch.append(len(batch))
-        for op, c0, k in zip(batch, col_start[:-1], widths):
-            blk = out[:, c0:c0 + k]
-            op.out = (blk if op.req.idx is None else blk[op.req.idx]).contiguous()
+        self.requests_per_launch.append(len({id(op) for op, _, _ in pieces}))
+        for (op, lo, hi), c0 in zip(pieces, col_start[:-1]):
+            blk = out[:, c0:c0 + hi - lo]
+            op.out[:, lo:hi] = blk if op.req.idx is None else blk[op.req.idx]
 
 
 def _init_device_linalg(dev) -> None:
