@@ -59,6 +59,24 @@ def _dist():
     return ws, rank, local
 
 
+def replica_totals(dev_s: float, e2e_s: float, steps: int, requests: int, dist=None,
+                   device="cpu"):
+    """Whole-job fits/hr of N independent replicas (one per rank, no
+    data-path collective): every rank served steps x requests fits and the
+    job took as long as its slowest rank (MAX over ranks of both times).
+    Returns (device s, end-to-end s, value, e2e value)."""
+    import torch
+
+    ws = 1
+    if dist is not None:
+        t = torch.tensor([dev_s, e2e_s], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, e2e_s = float(t[0]), float(t[1])
+        ws = dist.get_world_size()
+    total = steps * requests * ws
+    return dev_s, e2e_s, total / (dev_s / 3600.0), total / (e2e_s / 3600.0)
+
+
 def _peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -435,13 +453,7 @@ def run_ours(args, wl):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     srv.close()
-    if dist is not None:
-        t = torch.tensor([dev_s, e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s, e2e_s = float(t[0]), float(t[1])
-    total_fits = args.steps * R * ws
-    value = total_fits / (dev_s / 3600.0)
-    e2e_val = total_fits / (e2e_s / 3600.0)
+    dev_s, e2e_s, value, e2e_val = replica_totals(dev_s, e2e_s, args.steps, R, dist, dev)
     result = None
     if rank == 0:
         k_typ = max(16, int(round(op_cols / max(op_launches, 1))))
