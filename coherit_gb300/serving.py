@@ -104,9 +104,11 @@ class _Op:
 class _Batcher:
     """Collects operator applications of concurrent fits into batched launches.
 
-    A launch goes out when every active fit has an application pending, or
-    ``window_s`` after the first pending one arrived, whichever is first.
-    Launches are filled to ``max_cols`` columns: an application whose block
+    A launch goes out when every active fit has an application pending;
+    otherwise, while the previous launch still runs on the device, the
+    batcher keeps gathering (a launch now would only queue behind it), and
+    from the moment the device has finished it waits at most ``window_s``
+    for the fits that launch served to submit again.  Launches are filled to ``max_cols`` columns: an application whose block
     does not fit the rest of a launch is split by columns, its first columns
     riding in this launch and the others in the next (the operator acts on
     columns independently), so every launch but the last of a round streams
@@ -127,6 +129,8 @@ class _Batcher:
         self.launches = 0
         self.columns = 0
         self.requests_per_launch: list[int] = []
+        self.last_launch: torch.cuda.Event | None = None  # completion of the latest launch
+        self._busy_cap_s = 0.25  # longest wait for stragglers while the device is busy
         self.thread = threading.Thread(target=self._loop, name="coherit-batcher", daemon=True)
         self.thread.start()
 
@@ -167,12 +171,26 @@ class _Batcher:
                 self.cv.wait()
             if not self.pending:
                 return []
-            deadline = time.perf_counter() + self.window_s
+            start = time.perf_counter()
+            idle_since = None
             while len(self.pending) < self.n_active and not self.stop:
-                left = deadline - time.perf_counter()
+                now = time.perf_counter()
+                # While the previous launch still runs on the device a launch
+                # now would only queue behind it: keep gathering.  The fits it
+                # serves submit again shortly after it completes, so the
+                # window for them opens when the device finishes.
+                if self.last_launch is not None and not self.last_launch.query():
+                    idle_since = None
+                    if now - start >= self._busy_cap_s:
+                        break
+                    self.cv.wait(timeout=0.0005)
+                    continue
+                if idle_since is None:
+                    idle_since = now
+                left = self.window_s - (now - idle_since)
                 if left <= 0:
                     break
-                self.cv.wait(timeout=left)
+                self.cv.wait(timeout=min(left, 0.0005))
             pieces, cols = [], 0
             while self.pending and cols < self.max_cols:
                 op = self.pending[0]
@@ -228,6 +246,9 @@ class _Batcher:
                 st.handle, len(pieces), col_start.ctypes.data, slots.ctypes.data, self.prec,
                 Vf.data_ptr(), K, K, scale.ctypes.data, te.ctypes.data, out.data_ptr(), K,
                 _lib.stream_ptr()), "batched kv")
+        ev = torch.cuda.Event()
+        ev.record()
+        self.last_launch = ev
         st.op_stats["apps"] += 1
         st.op_stats["cols"] += K
         self.launches += 1
