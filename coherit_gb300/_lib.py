@@ -116,6 +116,7 @@ _SIGNATURES = {
     "coherit_sparse_info": (C.c_int, [_p, _p, _p, _p, _p, _p]),
     "coherit_sparse_stats": (C.c_int, [_p, _p, _p, _p, _p, _p, _p, _p]),
     "coherit_sparse_read_csc": (C.c_int, [_p, _p, _p, _p]),
+    "coherit_sparse_set_stats": (C.c_int, [_p, _p, _p, _p]),
     "coherit_sparse_kv": (C.c_int, [_p, _p, _i64, _i32, C.c_double, _f32, _p, _i64, _p]),
     "coherit_sparse_xtv": (C.c_int, [_p, _p, _i64, _i32, C.c_double, _p, _i64, _p]),
     "coherit_sparse_extract_columns": (C.c_int, [_p, _p, _i32, _p, _i64, _p]),

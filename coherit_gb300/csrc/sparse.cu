@@ -19,6 +19,7 @@
 // flight per step), reduces across the entry lanes, forms s_j in FP64 and
 // scatters inv_j x_p s_j back with vector atomics into the L2-resident out.
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -492,6 +493,7 @@ int finish_sparse(coherit_sparse* h, cudaStream_t st) {
 
 int ensure_ws(coherit_sparse* h, int32_t k) {
   if (k <= h->k_cap) return COHERIT_OK;
+  if (h->d_ws != nullptr) CO_CUDA(cudaDeviceSynchronize());
   cudaFree(h->d_ws);
   h->d_ws = nullptr;
   h->k_cap = 0;
@@ -508,14 +510,13 @@ inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 
 // the SNPs (a partial second wave of equal-work blocks would idle SMs).
 template <int L, bool KV>
 void launch_one(int sm_count, int64_t m, const ApplyArgs& a, cudaStream_t st) {
-  static int per_sm = 0;
-  if (per_sm == 0) {
+  static const int per_sm = [] {
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_apply<L, KV>, 256, 0) !=
             cudaSuccess || nb < 1)
       nb = 1;
-    per_sm = nb;
-  }
+    return nb;
+  }();
   const unsigned grid = blocks_for(std::max<int64_t>(m, 1) * 32, 256,
                                    static_cast<int64_t>(sm_count) * per_sm);
   k_apply<L, KV><<<grid, 256, 0, st>>>(a);
@@ -541,6 +542,8 @@ int launch_apply(coherit_sparse* h, const ApplyArgs& a, cudaStream_t st) {
 
 int ensure_stage(coherit_sparse* h, size_t bytes) {
   if (bytes <= h->stage_bytes) return COHERIT_OK;
+  // The old buffer may still be read by queued work.
+  if (h->d_stage != nullptr) CO_CUDA(cudaDeviceSynchronize());
   cudaFree(h->d_stage);
   h->d_stage = nullptr;
   h->stage_bytes = 0;
@@ -840,6 +843,37 @@ int coherit_sparse_stats(const coherit_sparse_t* h, float* mean, float* inv, int
   if (n_miss && m) std::memcpy(n_miss, h->n_miss.data(), sizeof(int64_t) * m);
   if (eff_m) *eff_m = h->eff;
   if (mean_diag_atom) *mean_diag_atom = h->atom;
+  return COHERIT_OK;
+}
+
+int coherit_sparse_set_stats(coherit_sparse_t* h, const float* mean, const float* inv,
+                             void* stream) {
+  CO_CHECK(h != nullptr, COHERIT_E_CLOSED, "sparse handle is NULL");
+  CO_CHECK(h->m == 0 || (mean != nullptr && inv != nullptr), COHERIT_E_SHAPE,
+           "mean and inv are required");
+  for (int64_t j = 0; j < h->m; ++j)
+    CO_CHECK(std::isfinite(mean[j]) && std::isfinite(inv[j]) && inv[j] >= 0.f, COHERIT_E_SHAPE,
+             "SNP %lld: mean and inverse sd must be finite, inverse sd >= 0", (long long)j);
+  CO_CUDA(cudaSetDevice(h->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (h->m > 0) {
+    std::memcpy(h->mean.data(), mean, sizeof(float) * h->m);
+    std::memcpy(h->inv.data(), inv, sizeof(float) * h->m);
+    CO_CUDA(cudaMemcpyAsync(h->d_mean, mean, sizeof(float) * h->m, cudaMemcpyHostToDevice, st));
+    CO_CUDA(cudaMemcpyAsync(h->d_inv, inv, sizeof(float) * h->m, cudaMemcpyHostToDevice, st));
+    CO_CUDA(cudaStreamSynchronize(st));
+  }
+  double eff = 0.0, mass = 0.0, base = 0.0;
+  for (int64_t j = 0; j < h->m; ++j) {
+    if (!(h->inv[j] > 0.f)) continue;
+    eff += 1.0;
+    mass += static_cast<double>(h->n - h->n_miss[j]);
+    const float z0 = (0.f - h->mean[j]) * h->inv[j];
+    base += static_cast<double>(z0) * static_cast<double>(z0);
+  }
+  h->eff = eff;
+  h->atom = eff > 0.0 ? mass / (static_cast<double>(h->n) * eff) : 0.0;
+  h->diag_base = base;
   return COHERIT_OK;
 }
 

@@ -311,7 +311,115 @@ def build_projected_core_atoms_partitioned(U, streamer: GenoBlockStreamer, *, mi
     return streamer.build_projected_core_atoms(U, subtract_identity=subtract_identity)
 
 
+# ------------------------------------------------------ rare-variant shards
+
+def _host(x) -> np.ndarray:
+    """Host numpy view of a numpy array or (device) tensor."""
+    if isinstance(x, torch.Tensor):
+        return x.detach().cpu().numpy()
+    return np.asarray(x)
+
+
+class _TransientSparse:
+    """A resident sparse matrix built from one shard's host entry arrays
+    (csc_all_rows / cols / vals, columns local to the shard and ascending,
+    sparse_stream.py:1037-1145) with the shard's own statistics installed."""
+
+    def __init__(self, n, m, mean, inv, rows, cols, vals, device):
+        self._lib = _lib.load()
+        self.n, self.m = int(n), int(m)
+        rows = np.ascontiguousarray(_host(rows), dtype=np.int32).reshape(-1)
+        cols = _host(cols).astype(np.int64, copy=False).reshape(-1)
+        vals = _host(vals).reshape(-1)
+        if not (rows.size == cols.size == vals.size):
+            raise ValueError("csc_all_rows, csc_all_cols and csc_all_vals must have one length.")
+        if cols.size and (np.any(np.diff(cols) < 0) or cols[0] < 0 or cols[-1] >= self.m):
+            raise ValueError("csc_all_cols must be ascending shard-local SNP indices in [0, m).")
+        if vals.dtype == np.int8:
+            codes = vals
+        else:
+            # Merged float values are 1 (het), 2 (hom-alt) or the SNP mean
+            # (missing, sparse_stream.py:609-647); a missing entry whose mean
+            # is exactly 1 or 2 contributes the same value either way.
+            v = vals.astype(np.float32)
+            codes = np.where(v == 1.0, 1, np.where(v == 2.0, 2, 3)).astype(np.int8)
+        codes = np.ascontiguousarray(codes, dtype=np.int8)
+        col_off = np.zeros(self.m + 1, dtype=np.int64)
+        np.cumsum(np.bincount(cols, minlength=self.m), out=col_off[1:])
+        mean = np.ascontiguousarray(_host(mean), dtype=np.float32).reshape(-1)
+        inv = np.ascontiguousarray(_host(inv), dtype=np.float32).reshape(-1)
+        if mean.size != self.m or inv.size != self.m:
+            raise ValueError(f"mean/inv must have m={self.m} entries.")
+        self.h = C.c_void_p()
+        stream = _lib.stream_ptr()
+        with torch.cuda.device(device):
+            _lib.check(self._lib.coherit_sparse_create_csc(
+                self.n, self.m, col_off.ctypes.data, rows.ctypes.data, codes.ctypes.data,
+                device.index, stream, C.byref(self.h)), "sparse shard")
+            _lib.check(self._lib.coherit_sparse_set_stats(self.h, mean.ctypes.data,
+                                                          inv.ctypes.data, stream), "shard stats")
+        self.dev = device
+
+    def apply(self, V, *, kv: bool):
+        V, squeeze = as_rhs(V, self.dev)
+        if V.shape[0] != self.n:
+            raise ValueError(f"V has {V.shape[0]} rows, expected n={self.n}")
+        k = int(V.shape[1])
+        rows = self.n if kv else self.m
+        out = torch.empty((rows, k), dtype=torch.float32, device=self.dev)
+        if kv:
+            _lib.check(self._lib.coherit_sparse_kv(self.h, V.data_ptr(), k, k, 1.0, 0.0,
+                                                   out.data_ptr(), k, _lib.stream_ptr()), "kv")
+        else:
+            _lib.check(self._lib.coherit_sparse_xtv(self.h, V.data_ptr(), k, k, 1.0,
+                                                    out.data_ptr(), k, _lib.stream_ptr()), "xtv")
+        return out[:, 0] if squeeze else out
+
+    def close(self):
+        if self.h:
+            self._lib.coherit_sparse_destroy(self.h)
+            self.h = C.c_void_p()
+
+
+def sparse_xtv_shard(V, *, m: int, mean, inv, csc_all_rows, csc_all_cols, csc_all_vals):
+    """Standardised Z^T V of one rare-variant shard, shape (m, k) or (m,)
+    (kv_impl.py:823-845)."""
+    n = int(torch.as_tensor(V).shape[0])
+    ts = _TransientSparse(n, m, mean, inv, csc_all_rows, csc_all_cols, csc_all_vals, _device(V))
+    try:
+        return ts.apply(V, kv=False)
+    finally:
+        ts.close()
+
+
+def sparse_projected_core_atom_shard(U, *, m: int, mean, inv, csc_all_rows, csc_all_cols,
+                                     csc_all_vals):
+    """(Z^T U)^T (Z^T U) of one shard before m_eff scaling (kv_impl.py:848-870)."""
+    if torch.as_tensor(U).ndim != 2:
+        raise ValueError("sparse_projected_core_atom_shard expects U with shape (n, k).")
+    blk = sparse_xtv_shard(U, m=m, mean=mean, inv=inv, csc_all_rows=csc_all_rows,
+                           csc_all_cols=csc_all_cols, csc_all_vals=csc_all_vals)
+    return blk.T @ blk
+
+
+def sparse_kv_shard(V, *, n: int, m: int, sum_v=None, mean, b=None, inv_sq, row_b=None,
+                    sum_a0_sq=None, csc_all_rows, csc_all_cols, csc_all_vals):
+    """Unnormalised Z Z^T V of one shard (kv_impl.py:873-905).  The shard's
+    inverse sds are sqrt(inv_sq); b, row_b, sum_a0_sq and sum_v are derived
+    from the entries and statistics on the device and are accepted for call
+    compatibility."""
+    inv = np.sqrt(np.maximum(_host(inv_sq).astype(np.float32), 0.0)).astype(np.float32)
+    ts = _TransientSparse(n, m, mean, inv, csc_all_rows, csc_all_cols, csc_all_vals, _device(V))
+    try:
+        return ts.apply(V, kv=True)
+    finally:
+        ts.close()
+
+
 __all__ = [
+    "sparse_xtv_shard",
+    "sparse_projected_core_atom_shard",
+    "sparse_kv_shard",
     "kv_impl_streamed",
     "kv_impl_snp_weighted_streamed",
     "xtv_impl_streamed",

@@ -308,6 +308,13 @@ int coherit_sparse_info(const coherit_sparse_t* h, int64_t* n, int64_t* m, int64
 int coherit_sparse_stats(const coherit_sparse_t* h, float* mean, float* inv, int64_t* n_het,
                          int64_t* n_hom, int64_t* n_miss, double* eff_m, double* mean_diag_atom);
 
+/* Install caller-supplied FP32 mean / inverse sd (host, m each), e.g. the
+ * statistics a shard payload carries (sparse_stream.py:1037-1145); m_eff,
+ * the mean-diagonal atom and the exact-diagonal base follow them.
+ * Synchronises `stream`.                                                    */
+int coherit_sparse_set_stats(coherit_sparse_t* h, const float* mean, const float* inv,
+                             void* stream);
+
 /* Host copy of the entries: col_off[m+1], rows[nnz], vals[nnz].            */
 int coherit_sparse_read_csc(const coherit_sparse_t* h, int64_t* col_off, int32_t* rows,
                             int8_t* vals);

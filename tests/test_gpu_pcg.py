@@ -20,7 +20,7 @@ def _true_relative(hv, x, b):
 
 
 def T(a, dev):
-    return torch.as_tensor(np.asarray(a, np.float32), device=dev)
+    return torch.as_tensor(np.array(a, np.float32), device=dev)
 
 
 @pytest.mark.parametrize("check_every", [1, 2, 5])

@@ -234,3 +234,41 @@ def test_dense_plus_rare_fit_matches_oracle(cuda, tmp_path):
         fitter.predict(eff, test_fitter=fitter)
     for s in fitter.streamers:
         s.close()
+
+
+@pytest.mark.parametrize("merged_float", [False, True])
+def test_kv_impl_shard_functions(cuda, merged_float):
+    """sparse_kv_shard / sparse_xtv_shard / sparse_projected_core_atom_shard
+    on a shard payload (host arrays with the shard's own statistics), as the
+    reference's sparse streamer passes them (kv_impl.py:823-905)."""
+    from coherit_gb300 import kv_impl
+
+    n, m = 2000, 900
+    codes = _codes(61, n, m, missing=0.02)
+    col_off, rows, vals = osp.csc_from_codes(codes)
+    mean, inv, _ = og.stats(codes)
+    cols = np.repeat(np.arange(m), np.diff(col_off)).astype(np.int32)
+    if merged_float:
+        v, _ = osp.entry_values(col_off, vals, mean)
+        vals_in = v.astype(np.float32)
+    else:
+        vals_in = vals
+    pay = osp.shard_payload(col_off, rows, vals, mean, inv, n)
+    V = np.random.default_rng(3).normal(size=(n, 7)).astype(np.float32) + 0.2
+    Vd = torch.as_tensor(V, device=cuda)
+    got = kv_impl.sparse_kv_shard(
+        Vd, n=n, m=m, sum_v=Vd.sum(0), mean=mean, b=pay["b"].astype(np.float32),
+        inv_sq=(inv.astype(np.float32) ** 2), row_b=pay["row_b"].astype(np.float32),
+        sum_a0_sq=np.float32(pay["sum_a0_sq"]), csc_all_rows=rows, csc_all_cols=cols,
+        csc_all_vals=vals_in).cpu().numpy()
+    ref = osp.kv_f64(col_off, rows, vals, mean, inv, V)
+    assert _rel(got, ref) < 1e-5
+    xt = kv_impl.sparse_xtv_shard(Vd, m=m, mean=mean, inv=inv, csc_all_rows=rows,
+                                  csc_all_cols=cols, csc_all_vals=vals_in).cpu().numpy()
+    assert _rel(xt, osp.xtv_f64(col_off, rows, vals, mean, inv, V)) < 1e-5
+    core = kv_impl.sparse_projected_core_atom_shard(
+        Vd, m=m, mean=mean, inv=inv, csc_all_rows=rows, csc_all_cols=cols,
+        csc_all_vals=vals_in).cpu().numpy()
+    cref = osp.projected_core_atom_f64(col_off, rows, vals, mean, inv, V, 1.0,
+                                       subtract_identity=False)
+    np.testing.assert_allclose(core, cref, rtol=1e-4, atol=1e-4 * np.abs(cref).max())
