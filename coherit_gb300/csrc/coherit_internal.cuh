@@ -2,7 +2,7 @@
 //
 // HBM layout of the resident genotypes (both copies hold every genotype):
 //   * SNP "slots": component g occupies slots [slot_start[g], slot_start[g] +
-//     m_g) followed by zero padding up to a multiple of kAlign (128); the
+//     m_g) followed by zero padding up to a multiple of kAlign (256); the
 //     total m_pad is a multiple of kAlign.  Padding slots have inv_sd = 0 and
 //     never contribute.
 //   * samples are padded with genotype code 0 up to n_pad (multiple of kAlign).
@@ -32,13 +32,12 @@ constexpr int kBlockRows = 128;
 constexpr int kBlockBytes = kRowBytes * kBlockRows;  // 2048
 constexpr int kPanel = 64;                           // slots per panel / samples per chunk
 constexpr int kTile = 128;                           // rows per block
-// Blocks per pipeline stage of the tensor-core operator: components and the
-// sample count are padded to multiples of kStageBlocks * 64 (and of 128).
-#ifndef COHERIT_STAGE_BLOCKS
-#define COHERIT_STAGE_BLOCKS 2
-#endif
-constexpr int kStageBlocks = COHERIT_STAGE_BLOCKS;
-constexpr int kAlign = kPanel * kStageBlocks > kTile ? kPanel * kStageBlocks : kTile;
+// Largest pipeline stage of the tensor-core operator (2 KB blocks along K):
+// components and the sample count are padded to multiples of
+// kMaxStageBlocks * 64, so that every launch's stage size divides them.
+constexpr int kMaxStageBlocks = 4;
+constexpr int kAlign = kPanel * kMaxStageBlocks;  // 256, a multiple of kTile
+static_assert(kAlign % kTile == 0, "padding must hold whole 128-row tiles");
 
 // -------------------------------------------------------------- status
 void set_error(const char* fmt, ...);

@@ -28,33 +28,37 @@
 
 namespace coherit {
 
-// Decoder warp sets (stages decoded concurrently).
-#ifndef COHERIT_SETS
-#define COHERIT_SETS 3
-#endif
-// A-ring depth floor: at least one slot per decoder set, and never fewer
-// than 3.  A 2-slot ring with two CTAs per SM (two decoder sets, 32-column
-// bf16x3 blocks) gave results 5e-3 off at n = 50,000, m = 500,000, while the
-// same ring with one CTA per SM and 3-slot rings with two CTAs per SM were
-// exact; the cause was not found, so no launch uses fewer than 3 slots.
-#ifndef COHERIT_TMEM_MIN_SLOTS
-#define COHERIT_TMEM_MIN_SLOTS (COHERIT_SETS > 3 ? COHERIT_SETS : 3)
-#endif
-constexpr int kSets = COHERIT_SETS;  // decoder warp sets (stages in flight through the A ring)
-constexpr int kThreads = 32 * (3 + 4 * kSets);
+// Pipeline configurations of the tensor-core operator, chosen per launch:
+//  * StageCfg<2, 3> ("narrow"): stages of 2 blocks (K = 128), 3 decoder warp
+//    sets, a 9-deep genotype ring, an A ring of 3..6 slots of 64 columns;
+//    two CTAs per SM for blocks of <= 16 columns, one CTA otherwise.
+//  * StageCfg<4, 2> ("wide"): stages of 4 blocks (K = 256), 2 decoder sets,
+//    an 8-deep genotype ring, an A ring of 2..3 slots of 128 columns; half
+//    the barrier round trips per K of the narrow form (at n = 50,000,
+//    m = 500,000 it applies 32-48 columns in 9.2-9.9 ms against 11.3-11.7 ms).
+// Ring rules: the genotype ring depth is a multiple of the decoder sets, so
+// every ring slot is consumed by one set in stage order; the A ring has at
+// least one slot per decoder set, so no set waits on an A slot whose previous
+// use is more than one barrier phase behind (parity waits see one phase).
+// The narrow form keeps at least 3 A slots: a 2-slot ring with its 3 sets
+// broke the second rule (5e-3 off at n = 50,000, m = 500,000).
+template <int SB_, int SETS_>
+struct StageCfg {
+  static constexpr int SB = SB_;        // 2 KB blocks per stage
+  static constexpr int SETS = SETS_;    // decoder warp sets
+  static constexpr int RG = SETS_ == 3 ? 9 : 8;  // genotype ring depth
+  static constexpr int MIN_RA = SETS_ >= 3 ? 3 : SETS_;
+  static constexpr int THREADS = 32 * (3 + 4 * SETS_);
+  static_assert(RG % SETS_ == 0, "genotype ring depth must be a multiple of the decoder sets");
+  static_assert(SB_ <= kMaxStageBlocks, "stage larger than the layout padding");
+};
+using CfgNarrow = StageCfg<2, 3>;
+using CfgWide = StageCfg<4, 2>;
 constexpr int kWarpG = 0, kWarpMMA = 1, kWarpB = 2, kWarpDec0 = 3;
-// Genotype ring depth (stages of kStageBlocks 2 KB blocks).  It must be a
-// multiple of the number of decoder sets: then every ring slot is only ever
-// consumed by one set, in stage order, so a set never waits on a slot whose
-// previous fill is still in flight (parity waits see one phase only).  Nine
-// stages keep the decoders' waits on genotype data short and leave shared
-// memory for a deeper B ring.
-constexpr int kRG = 9;
-static_assert(kRG % kSets == 0, "genotype ring depth must be a multiple of the decoder sets");
-// Tensor-memory A ring depth limit (slots of 32 * kStageBlocks columns).  Depths
-// up to 6 are the configurations exercised on GB300; a 7-slot ring with a
-// 64-column accumulator raised an illegal-instruction fault whose cause was
-// not found, so the policy never builds one.
+// Tensor-memory A ring depth limit.  Depths up to 6 (64-column slots) are
+// the configurations exercised on GB300; a 7-slot ring with a 64-column
+// accumulator raised an illegal-instruction fault whose cause was not found,
+// so the policy never builds one.
 constexpr int kMaxRA = 6;
 constexpr int kMaxRB = 16;     // B ring depth limit
 constexpr int kMaxGroups = 32;
@@ -392,8 +396,9 @@ __global__ void k_prep_s_from_b(const float* __restrict__ b, int64_t ldb,
 // accumulating them one after another into one accumulator loses accuracy
 // on long chains (measured 6.5e-4 relative at n = 50,000, m = 500,000).
 static inline int max_kp_for(const coherit_geno* h, int nsplit) {
-  const int budget = h->smem_optin - 4096 - kBarrierBytes - kRG * kStageBlocks * kBlockBytes;
-  const int per_col = 2 * kStageBlocks * nsplit * kPanel * 2;
+  const int budget =
+      h->smem_optin - 4096 - kBarrierBytes - CfgNarrow::RG * CfgNarrow::SB * kBlockBytes;
+  const int per_col = 2 * CfgNarrow::SB * nsplit * kPanel * 2;
   return std::min((256 / nsplit) / 16 * 16, (budget / per_col) / 16 * 16);
 }
 
@@ -419,16 +424,17 @@ struct SplitPlan {
   int64_t nr;     // K2 component blocks (G when stacked, else 1)
 };
 
-static SplitPlan split_plan(const coherit_geno* h, bool stacked, int64_t target_ctas) {
+// K shares of one launch whose stages hold `sb` blocks.
+static SplitPlan split_plan(const coherit_geno* h, bool stacked, int64_t target_ctas, int sb) {
   SplitPlan s;
   s.nr = stacked ? h->G : 1;
-  s.k1 = split_count(h->n_chunks / kStageBlocks, h->n_ttiles, target_ctas);
-  int64_t stages2 = h->n_panels / kStageBlocks;
+  s.k1 = split_count(h->n_chunks / sb, h->n_ttiles, target_ctas);
+  int64_t stages2 = h->n_panels / sb;
   if (stacked) {
     stages2 = 0;
     for (int g = 0; g < h->G; ++g)
       stages2 = std::max<int64_t>(
-          stages2, (h->comp_slot_start[g + 1] - h->comp_slot_start[g]) / kPanel / kStageBlocks);
+          stages2, (h->comp_slot_start[g + 1] - h->comp_slot_start[g]) / kPanel / sb);
   }
   s.k2 = split_count(stages2, h->n_stiles * s.nr, target_ctas);
   return s;
@@ -447,8 +453,10 @@ static size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255);
 // over both output modes.  K1's partials are consumed before K2 runs.
 static int64_t part_rows_needed(const coherit_geno* h) {
   int64_t rows = 0;
-  for (int stacked = 0; stacked < 2; ++stacked) {
-    const SplitPlan s = split_plan(h, stacked != 0, target_ctas(h));
+  for (int q = 0; q < 4; ++q) {
+    const bool stacked = (q & 1) != 0;
+    const int sb = (q & 2) ? CfgWide::SB : CfgNarrow::SB;
+    const SplitPlan s = split_plan(h, stacked, target_ctas(h), sb);
     if (s.k1 > 1) rows = std::max<int64_t>(rows, s.k1 * h->m_pad);
     if (s.k2 > 1) rows = std::max<int64_t>(rows, s.k2 * s.nr * h->n_pad);
   }
@@ -539,6 +547,8 @@ static int fill_epi(coherit_geno* h, const OpDesc& d, int kp, int nsplit, EpiPar
 }
 
 struct TcLaunchCfg {
+  bool wide;   // StageCfg<4, 2> instead of StageCfg<2, 3>
+  int sb;      // blocks per stage of that configuration
   int RB, RA;
   bool side;
   uint32_t bslot;
@@ -548,22 +558,52 @@ struct TcLaunchCfg {
 
 // Accumulator: NSPLIT*kp columns, the split terms side by side in N (one MMA
 // per K step, N <= 256).  The A ring takes the remaining tensor-memory
-// columns (3..6 slots of 32 * kStageBlocks).
+// columns.  Blocks of <= 16 columns use the narrow form at two CTAs per SM;
+// wider blocks use the wide form where its B ring (>= 2 stages) fits shared
+// memory, else the narrow form, always at one CTA per SM: two-CTA layouts
+// of wider blocks returned wrong lane quarters when K was split (bf16x1 and
+// bf16x2 at 32-48 columns, 3e-2 to 1e-1 off at n = 20,000, m = 30,000), and
+// one CTA per SM allocates all 512 tensor-memory columns so no second CTA
+// can share the SM.
 static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
   TcLaunchCfg c;
   c.side = nsplit > 1 && nsplit * kp <= 256;
   const int acc = c.side ? nsplit * kp : kp;
   c.acc_cols = static_cast<uint32_t>(round_up(acc, 32));
-  const uint32_t slot_cols = 32u * kStageBlocks;
-  const uint32_t need = c.acc_cols + COHERIT_TMEM_MIN_SLOTS * slot_cols;
-  uint32_t cols = 32;
-  while (cols < need) cols <<= 1;
+  const size_t cap = static_cast<size_t>(h->smem_optin);
+  if (kp > 16) {
+    const uint32_t slot = 32u * CfgWide::SB;
+    const uint32_t bslot = static_cast<uint32_t>(CfgWide::SB) * nsplit * kp * kPanel * 2;
+    const size_t fixed = kBarrierBytes + static_cast<size_t>(CfgWide::RG) * CfgWide::SB * kBlockBytes;
+    const int ra = std::min<int>(kMaxRA, static_cast<int>((512u - c.acc_cols) / slot));
+    if (c.acc_cols + CfgWide::MIN_RA * slot <= 512u && ra >= CfgWide::MIN_RA &&
+        fixed + 2 * static_cast<size_t>(bslot) <= cap - 4096) {
+      c.wide = true;
+      c.sb = CfgWide::SB;
+      c.tmem_cols = 512;
+      c.RA = ra;
+      c.bslot = bslot;
+      int rb = static_cast<int>((cap - 4096 - fixed) / bslot);
+      c.RB = std::max(2, std::min(kMaxRB, rb));
+      c.smem = fixed + static_cast<size_t>(c.RB) * bslot;
+      return c;
+    }
+  }
+  c.wide = false;
+  c.sb = CfgNarrow::SB;
+  const uint32_t slot_cols = 32u * CfgNarrow::SB;
+  uint32_t cols = 512;
+  if (kp <= 16) {
+    const uint32_t need = c.acc_cols + CfgNarrow::MIN_RA * slot_cols;
+    cols = 32;
+    while (cols < need) cols <<= 1;
+  }
   c.tmem_cols = cols;
   c.RA = std::min<int>(kMaxRA, static_cast<int>((cols - c.acc_cols) / slot_cols));
-  c.bslot = static_cast<uint32_t>(kStageBlocks) * nsplit * kp * kPanel * 2;
-  const size_t fixed = kBarrierBytes + static_cast<size_t>(kRG) * kStageBlocks * kBlockBytes;
+  c.bslot = static_cast<uint32_t>(CfgNarrow::SB) * nsplit * kp * kPanel * 2;
+  const size_t fixed =
+      kBarrierBytes + static_cast<size_t>(CfgNarrow::RG) * CfgNarrow::SB * kBlockBytes;
   const int ctas_tmem = 512 / static_cast<int>(cols);
-  const size_t cap = static_cast<size_t>(h->smem_optin);
   const size_t target = ctas_tmem >= 2 ? std::min<size_t>(112 * 1024, cap) : cap - 4096;
   int rb = static_cast<int>((target - fixed) / c.bslot);
   rb = std::max(2, std::min(kMaxRB, rb));
@@ -578,20 +618,27 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
   return c;
 }
 
-template <bool IS_K1>
-static int launch_tc(int nsplit, bool side, dim3 grid, size_t smem, cudaStream_t st,
-                     const TcParams& p) {
+template <bool IS_K1, class Cfg>
+static int launch_tc_cfg(int nsplit, bool side, dim3 grid, size_t smem, cudaStream_t st,
+                         const TcParams& p) {
   auto go = [&](auto kern) -> int {
     CO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));
-    kern<<<grid, kThreads, smem, st>>>(p); note_launch();
+    kern<<<grid, Cfg::THREADS, smem, st>>>(p); note_launch();
     CO_CUDA(cudaGetLastError());
     return COHERIT_OK;
   };
-  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false>);
+  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false, Cfg>);
   CO_CHECK(side, COHERIT_E_SHAPE, "split terms must fit side by side (nsplit * kp <= 256)");
-  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true>);
-  return go(k_tc_op<IS_K1, 3, true>);
+  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true, Cfg>);
+  return go(k_tc_op<IS_K1, 3, true, Cfg>);
+}
+
+template <bool IS_K1>
+static int launch_tc(const TcLaunchCfg& cfg, int nsplit, dim3 grid, cudaStream_t st,
+                     const TcParams& p) {
+  if (cfg.wide) return launch_tc_cfg<IS_K1, CfgWide>(nsplit, cfg.side, grid, cfg.smem, st, p);
+  return launch_tc_cfg<IS_K1, CfgNarrow>(nsplit, cfg.side, grid, cfg.smem, st, p);
 }
 
 // Column-block width when k exceeds what one launch holds (each block
@@ -681,11 +728,11 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   e.rbuf = rbuf;
   const int nr = e.stacked ? h->G : 1;
   CO_CUDA(cudaMemsetAsync(rbuf, 0, sizeof(double) * nr * kp, st));
-  const SplitPlan sp = split_plan(h, e.stacked != 0, target_ctas(h));
+  const TcLaunchCfg cfg = tc_config(h, kp, nsplit);
+  const SplitPlan sp = split_plan(h, e.stacked != 0, target_ctas(h), cfg.sb);
   float* part = reinterpret_cast<float*>(ws + L.part);
   const unsigned col_blocks = static_cast<unsigned>((kp / 16 + 3) / 4);
 
-  const TcLaunchCfg cfg = tc_config(h, kp, nsplit);
   TcParams p;
   memset(&p, 0, sizeof(p));
   p.RB = cfg.RB;
@@ -715,9 +762,9 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
     p.part = sp.k1 > 1 ? part : nullptr;
     p.part_stride = h->m_pad * kp;
     p.part_rows = h->m_pad;
-    rc = launch_tc<true>(nsplit, cfg.side,
+    rc = launch_tc<true>(cfg, nsplit,
                          dim3(static_cast<unsigned>(h->n_ttiles), 1, static_cast<unsigned>(sp.k1)),
-                         cfg.smem, st, p);
+                         st, p);
     if (rc != COHERIT_OK) return rc;
     if (sp.k1 > 1) {
       k_k1_finish<<<dim3(static_cast<unsigned>(h->m_pad / 32), col_blocks), dim3(32, 4), 0, st>>>(
@@ -739,10 +786,10 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   p.part = sp.k2 > 1 ? part : nullptr;
   p.part_stride = static_cast<int64_t>(nr) * h->n_pad * kp;
   p.part_rows = h->n_pad;
-  rc = launch_tc<false>(nsplit, cfg.side,
+  rc = launch_tc<false>(cfg, nsplit,
                         dim3(static_cast<unsigned>(h->n_stiles), static_cast<unsigned>(nr),
                              static_cast<unsigned>(sp.k2)),
-                        cfg.smem, st, p);
+                        st, p);
   if (rc != COHERIT_OK) return rc;
   if (sp.k2 > 1) {
     k_k2_finish<<<dim3(static_cast<unsigned>(h->n_pad / 32), col_blocks, static_cast<unsigned>(nr)),

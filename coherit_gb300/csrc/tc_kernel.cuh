@@ -1,12 +1,12 @@
 // tc_kernel.cuh -- the tcgen05 mainloop + epilogues of the genotype operator.
 //
 // One CTA owns a 128-row tile (K1: 128 SNP slots, K2: 128 samples) and walks
-// K in stages of kStageBlocks x 64 (K1: samples, K2: SNP slots).  Per stage:
-//   warp 0   bulk-copies the kStageBlocks consecutive 2 KB genotype blocks into
+// K in stages of Cfg::SB x 64 (K1: samples, K2: SNP slots).  Per stage:
+//   warp 0   bulk-copies the Cfg::SB consecutive 2 KB genotype blocks into
 //            a shared ring;
 //   warp 2   bulk-copies the B tile (all split terms of V or S for these 64
 //            K values) into a shared ring;
-//   warps 3.. decode in kSets sets of 4 warps (one per tensor-memory lane
+//   warps 3.. decode in Cfg::SETS sets of 4 warps (one per tensor-memory lane
 //            quarter); a set turns the 16-byte rows (64 codes) of one chunk
 //            into 32 BF16 pairs per row stored with tcgen05.st into an A ring
 //            in tensor memory, and the sets take successive chunks so that
@@ -24,8 +24,11 @@
 // with the number of MMAs into one accumulator), so the host bounds every
 // chain this way.
 
-template <bool IS_K1, int NSPLIT, bool SIDE>
-__global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __grid_constant__ TcParams p) {
+template <bool IS_K1, int NSPLIT, bool SIDE, class Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant__ TcParams p) {
+  constexpr int kStageBlocks = Cfg::SB;
+  constexpr int kSets = Cfg::SETS;
+  constexpr int kRG = Cfg::RG;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint64_t* fullG = reinterpret_cast<uint64_t*>(smem);
   uint64_t* emptyG = fullG + kRG;
@@ -103,7 +106,7 @@ __global__ void __launch_bounds__(kThreads, kSets >= 4 ? 1 : 2) k_tc_op(const __
     // RA >= kSets: a decoder set never waits on an A slot whose previous use
     // is more than one barrier phase behind (parity waits are ambiguous
     // beyond one phase).
-    const bool cfg_ok = p.RA >= kSets && p.RA >= 3 && p.RA <= kMaxRA && p.RB >= 1 &&
+    const bool cfg_ok = p.RA >= kSets && p.RA >= Cfg::MIN_RA && p.RA <= kMaxRA && p.RB >= 1 &&
                         p.RB <= kMaxRB &&
                         p.ksplit >= 1 && static_cast<int>(gridDim.z) == p.ksplit &&
                         (p.ksplit == 1 || p.part != nullptr) &&

@@ -288,3 +288,30 @@ def test_accuracy_at_scale_vs_dense_fp64(cuda):
     for k in (20, 32, 48, 64, 80):
         got = st.kv(wide[:, :k].contiguous())
         assert col_rel(got.cpu().numpy(), ref16[:, :k].cpu().numpy()) < 1e-6, k
+
+
+@pytest.mark.parametrize("m", [30000, 80000])
+def test_reduced_precisions_with_and_without_split_k(cuda, m):
+    """bf16x1 / bf16x2 X^T V and K V at 16-48 columns against FP64, with K
+    split into shares writing partials (m = 30,000: fewer SNP tiles than the
+    CTA target) and without (m = 80,000).  Two-CTA-per-SM layouts of blocks
+    wider than 16 columns returned whole wrong lane quarters in the split
+    case (3e-2 to 1e-1 off); every width here must stay at its precision's
+    error level: bf16x1 (one BF16 term) < 1e-2, bf16x2 < 2e-5 relative per
+    column."""
+    n = 20000
+    st = _streamer(n, m, seed=5)
+    codes = og.synth_codes(5, n, np.arange(m))
+    mean, inv = st._means_host, st._inv_sds_host
+    eff = float(st._eff_m_host)
+    for prec, tol in (("bf16x1", 1e-2), ("bf16x2", 2e-5)):
+        for k in (16, 32, 48):
+            V = np.random.default_rng(k).normal(size=(n, k)).astype(np.float32)
+            Vd = torch.as_tensor(V, device=cuda)
+            xt = st.xtv(Vd, precision=prec).cpu().numpy()
+            assert col_rel(xt, og.xtv_f64(codes, mean, inv, V)) < tol, (prec, k, "xtv")
+            kv = st.kv(Vd, precision=prec).cpu().numpy()
+            assert col_rel(kv, og.kv_f64(codes, mean, inv, V, comp_scale=[1 / eff])) < tol, \
+                (prec, k, "kv")
+    st.check()
+    st.close()
