@@ -131,9 +131,14 @@ def _bim_records(prefix: str):
 
 
 def run_continuous_gwas(fitter, y, covar=None, *, out_prefix: str) -> GWASSummary:
-    """Scan every streamer of the fitter and write ``<out_prefix>.gwas.tsv``
+    """Scan every dense streamer of the fitter (fitters with rare-variant
+    streamers are rejected, gwas.py:77-86) and write ``<out_prefix>.gwas.tsv``
     and ``<out_prefix>.gwas_metadata.json`` (gwas.py:70-230)."""
+    if getattr(fitter, "_has_sparse", False):
+        raise ValueError("GWAS currently supports dense genotype inputs only.")
     streamers = list(getattr(fitter, "streamers", ()))
+    n_dense = getattr(fitter, "_n_dense_streamers", len(streamers))
+    streamers = streamers[:n_dense]
     if not streamers:
         raise ValueError("GWAS requires at least one dense genotype streamer.")
     if not out_prefix:

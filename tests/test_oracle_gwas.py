@@ -26,3 +26,17 @@ def test_fwl_statistics_equal_direct_least_squares():
         cov = sigma2 * np.linalg.inv(A.T @ A)
         np.testing.assert_allclose(out["beta_std"][j], coef[-1], rtol=1e-5, atol=1e-9)
         np.testing.assert_allclose(out["se_std"][j], np.sqrt(cov[-1, -1]), rtol=1e-4)
+
+
+def test_gwas_rejects_fitters_with_rare_variant_streamers(tmp_path):
+    """gwas.py:77-86: sparse genotype inputs are not scanned."""
+    import types
+
+    from coherit_gb300.gwas import run_continuous_gwas
+
+    fake = types.SimpleNamespace(_has_sparse=True, streamers=[object()], _n_dense_streamers=1)
+    with pytest.raises(ValueError, match="dense genotype inputs only"):
+        run_continuous_gwas(fake, np.zeros(4), out_prefix=str(tmp_path / "g"))
+    empty = types.SimpleNamespace(_has_sparse=False, streamers=[], _n_dense_streamers=0)
+    with pytest.raises(ValueError, match="at least one dense"):
+        run_continuous_gwas(empty, np.zeros(4), out_prefix=str(tmp_path / "g"))
