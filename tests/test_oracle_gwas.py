@@ -1,5 +1,6 @@
 """The GWAS oracle against direct least squares of y on [X, z_j] (CPU)."""
 import numpy as np
+import pytest
 
 from oracle import geno as og
 from oracle import gwas as ogw
