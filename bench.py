@@ -335,13 +335,15 @@ def serve_step(srv, ys, Xs, host: bool):
     return [f.result() for f in futs]
 
 
-def serving_stream(st, wl, n_requests: int, rate_per_s: float, seed: int, max_active: int):
+def serving_stream(st, wl, n_requests: int, rate_per_s: float, seed: int, max_active: int,
+                   min_subset: int | None = None):
     """A bounded stream of heterogeneous requests with Poisson arrivals over
     the resident genotypes (the serving workload's request mix on this
     matrix): each request a random sample subset (size log-uniform in
-    [n/5, n]), 1-20 N(0,1) covariates + intercept, h2 ~ U(0.05, 0.8) from
-    wl.n_causal causal SNPs.  Requests arrive while earlier ones are on the
-    GPU and join their batched launches.  Returns the stream's summary."""
+    [min_subset, n], default n/5), 1-20 N(0,1) covariates + intercept,
+    h2 ~ U(0.05, 0.8) from wl.n_causal causal SNPs.  Requests arrive while
+    earlier ones are on the GPU and join their batched launches.  Returns the
+    stream's summary."""
     import torch
 
     from coherit_gb300.serving import REMLServer
@@ -355,7 +357,8 @@ def serving_stream(st, wl, n_requests: int, rate_per_s: float, seed: int, max_ac
     G = st.zxb(torch.as_tensor(B, device=st.dev)).double().cpu().numpy()
     reqs = []
     for r in range(n_requests):
-        size = int(np.exp(rng.uniform(np.log(n / 5), np.log(n))))
+        lo = float(min_subset) if min_subset else n / 5
+        size = int(np.exp(rng.uniform(np.log(lo), np.log(n))))
         mask = np.zeros(n, dtype=bool)
         mask[rng.choice(n, size=size, replace=False)] = True
         h2 = rng.uniform(0.05, 0.8)
@@ -373,17 +376,26 @@ def serving_stream(st, wl, n_requests: int, rate_per_s: float, seed: int, max_ac
     for (y, X, mask), gap in zip(reqs, gaps):
         time.sleep(float(gap))
         futs.append(srv.submit(y, X, sample_mask=mask))
-    res = [f.result() for f in futs]
-    wall = time.perf_counter() - t0
-    per_launch = srv.batcher.requests_per_launch
-    srv.close()
-    lat = [r.latency for r in res]
-    return {"requests": n_requests, "arrival_rate_per_s": round(rate_per_s, 3),
-            "fits_per_hr": round(n_requests / (wall / 3600.0), 1),
+    res, failed = [], []
+    try:
+        for i, f in enumerate(futs):
+            try:
+                res.append(f.result())
+            except Exception as err:  # a failed fit is reported, not fatal
+                failed.append(f"request {i}: {type(err).__name__}: {str(err)[:200]}")
+        wall = time.perf_counter() - t0
+        per_launch = list(srv.batcher.requests_per_launch)
+        launches = srv.batcher.launches - b0
+    finally:
+        srv.close()
+    lat = [r.latency for r in res] or [float("nan")]
+    return {"requests": n_requests, "completed": len(res), "failed": failed,
+            "arrival_rate_per_s": round(rate_per_s, 3),
+            "fits_per_hr": round(len(res) / (wall / 3600.0), 1),
             "latency_s": {"p50": round(statistics.median(lat), 3),
                           "p99": round(_percentile(lat, 0.99), 3)},
             "subset_sizes": [int(m.sum()) for _, _, m in reqs][:8],
-            "operator_launches": srv.batcher.launches - b0,
+            "operator_launches": launches,
             "mean_requests_per_launch": round(float(np.mean(per_launch)), 2) if per_launch else 0.0,
             "max_active": max_active, "seed": seed}
 
@@ -643,6 +655,32 @@ def run_operator_only(args, wl):
             "gpu_launches": int(launches), "peak_source": peak_src}
 
 
+def run_stream_only(args, wl):
+    """Only the Poisson request stream (``--stream-only``) on the workload's
+    matrix, e.g. a prefix of the c4 serving stream (``--config c4``: n=200,000
+    x m=600,000, subsets log-uniform in [1e4, 2e5])."""
+    import torch
+
+    from coherit_gb300.configs import C4_SUBSET_MIN
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    t0 = time.perf_counter()
+    st = build_problem(wl, dev)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    sampler = ClockSampler(0)
+    sampler.start()
+    out = serving_stream(st, wl, args.stream, args.stream_rate, seed=wl.seed + 99,
+                         max_active=args.requests,
+                         min_subset=C4_SUBSET_MIN if wl.name.startswith("c4") else None)
+    clocks = sampler.stop()
+    st.close()
+    out.update({"metric": "REML fits/hr over a Poisson request stream", "config": wl.name,
+                "n": wl.n, "m": wl.m, "build_s": round(build_s, 2), "clocks": clocks})
+    return out
+
+
 def run_sparse_only(args, wl):
     """Rare-variant operator micro-benchmark (``--sparse K``) at the
     workload's n x m (or --n/--m), as reported in the ``sparse12`` object of
@@ -690,6 +728,8 @@ def main():
                     help="right-hand-side columns per fit assumed by the reference arm")
     ap.add_argument("--operator", type=int, default=0, metavar="K",
                     help="time bare operator applications of width K instead of fits")
+    ap.add_argument("--stream-only", action="store_true",
+                    help="run only the Poisson request stream on the workload's matrix")
     ap.add_argument("--sparse", type=int, default=0, metavar="K",
                     help="time the rare-variant operator at width K instead of fits")
     ap.add_argument("--n", type=int, default=0, help="with --operator/--sparse: samples")
@@ -702,6 +742,8 @@ def main():
         out = run_operator_only(args, wl)
     elif args.sparse > 0:
         out = run_sparse_only(args, wl)
+    elif args.stream_only:
+        out = run_stream_only(args, wl)
     elif args.impl == "reference":
         out = run_reference(args, wl)
     else:

@@ -45,4 +45,10 @@ C3 = REMLWorkload("c3_n100000_m1000000_G8", n=100000, m=1000000, h2=0.4, n_causa
                   n_covar=10, slq_samples=128, slq_m=30, pcg_tol=1e-5, seed=2,
                   components=(125000,) * 8, precond_rank=256)
 
-WORKLOADS = {"c1": C1, "c2": C2, "c3": C3}
+# c4's requests are drawn per request by the stream (h2, subset, covariates);
+# h2 / n_causal / n_covar here are the generator's defaults for full fits.
+C4 = REMLWorkload("c4_n200000_m600000", n=200000, m=600000, h2=0.3, n_causal=5000, n_covar=10,
+                  slq_samples=64, slq_m=30, pcg_tol=1e-5, seed=4, precond_rank=256)
+C4_SUBSET_MIN = 10000
+
+WORKLOADS = {"c1": C1, "c2": C2, "c3": C3, "c4": C4}

@@ -402,19 +402,23 @@ static inline int max_kp_for(const coherit_geno* h, int nsplit) {
   return std::min((256 / nsplit) / 16 * 16, (budget / per_col) / 16 * 16);
 }
 
-// Split K.  Longest chain one accumulator takes: 512 stages (65,536 K values,
-// 4,096 MMAs of K = 16).  Measured on GB300 at n = 50,000: K2 chains over
-// 62,500 SNPs stay within 2e-6 relative of FP64, over 500,000 SNPs 4.5e-5.
-// Short problems are split further, down to 16 stages a share, until the
-// grid holds about two waves.
-constexpr int64_t kMaxChainStages = 512;
-constexpr int64_t kMinShareStages = 16;
+// Split K.  Longest chain one accumulator takes: 65,536 K values (4,096 MMAs
+// of K = 16; 512 two-block or 256 four-block stages).  Measured on GB300 at
+// n = 50,000: K2 chains over 62,500 SNPs stay within 2e-6 relative of FP64,
+// over 500,000 SNPs 4.5e-5; chains of 131,072 (512 four-block stages) let a
+// served PCG at n = 200,000, m = 600,000 stall at 1.4e-5 against a 1e-5
+// tolerance.  Short problems are split further, down to 2,048 K values a
+// share, until the grid holds about two waves.
+constexpr int64_t kMaxChainK = 65536;
+constexpr int64_t kMinShareK = 2048;
 
-static int split_count(int64_t stages, int64_t ctas, int64_t target_ctas) {
-  int64_t P = std::max<int64_t>(1, (stages + kMaxChainStages - 1) / kMaxChainStages);
+static int split_count(int64_t stages, int64_t ctas, int64_t target_ctas, int sb) {
+  const int64_t max_stages = kMaxChainK / (kPanel * sb);
+  const int64_t min_stages = std::max<int64_t>(1, kMinShareK / (kPanel * sb));
+  int64_t P = std::max<int64_t>(1, (stages + max_stages - 1) / max_stages);
   if (ctas * P < target_ctas) {
     const int64_t want = (target_ctas + ctas - 1) / ctas;
-    P = std::max(P, std::min(want, stages / kMinShareStages));
+    P = std::max(P, std::min(want, stages / min_stages));
   }
   return static_cast<int>(std::min<int64_t>(P, 1024));
 }
@@ -428,7 +432,7 @@ struct SplitPlan {
 static SplitPlan split_plan(const coherit_geno* h, bool stacked, int64_t target_ctas, int sb) {
   SplitPlan s;
   s.nr = stacked ? h->G : 1;
-  s.k1 = split_count(h->n_chunks / sb, h->n_ttiles, target_ctas);
+  s.k1 = split_count(h->n_chunks / sb, h->n_ttiles, target_ctas, sb);
   int64_t stages2 = h->n_panels / sb;
   if (stacked) {
     stages2 = 0;
@@ -436,7 +440,7 @@ static SplitPlan split_plan(const coherit_geno* h, bool stacked, int64_t target_
       stages2 = std::max<int64_t>(
           stages2, (h->comp_slot_start[g + 1] - h->comp_slot_start[g]) / kPanel / sb);
   }
-  s.k2 = split_count(stages2, h->n_stiles * s.nr, target_ctas);
+  s.k2 = split_count(stages2, h->n_stiles * s.nr, target_ctas, sb);
   return s;
 }
 

@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant
     bbase = p.bsrc + p0 * p.b_chunk_bytes;
   }
   // This CTA's share of the K stages: [s0, s0 + nch).  The host keeps a
-  // share at most 512 stages long (split K), so 32-bit stage counters hold.
+  // share at most 65,536 K values long (split K), so 32-bit stage counters
+  // hold.
   const int64_t s0 = ntot * zsplit / p.ksplit;
   const int nch = static_cast<int>(ntot * (zsplit + 1) / p.ksplit - s0);
   gbase += s0 * (kStageBlocks * kBlockBytes);
