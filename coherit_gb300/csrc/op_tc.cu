@@ -35,7 +35,7 @@ namespace coherit {
 //  * StageCfg<4, 2> ("wide"): stages of 4 blocks (K = 256), 2 decoder sets,
 //    an 8-deep genotype ring, an A ring of 2..3 slots of 128 columns; half
 //    the barrier round trips per K of the narrow form (at n = 50,000,
-//    m = 500,000 it applies 32-48 columns in 9.2-9.9 ms against 11.3-11.7 ms).
+//    m = 500,000 it applies 32-48 columns in 9.0-9.8 ms against 11.3-11.7 ms).
 // Ring rules: the genotype ring depth is a multiple of the decoder sets, so
 // every ring slot is consumed by one set in stage order; the A ring has at
 // least one slot per decoder set, so no set waits on an A slot whose previous
