@@ -655,6 +655,62 @@ def run_operator_only(args, wl):
             "gpu_launches": int(launches), "peak_source": peak_src}
 
 
+def run_smile_only(args, wl):
+    """SMILE block-weighted operator at the c5 shape (``--smile K``): n=100,000
+    x m=300,000 (or --n/--m), blocks of 500 SNPs with W_b ~ Wishart(500, I)/500
+    in FP32 (seeded), kernel-trace normalisation; K V at width K timed with
+    CUDA events on the launching stream.  Algorithmic work: the two genome
+    contractions (4nmk flops, n*ceil(m/4) genotype bytes) plus the W_b
+    products (2*m*500*k flops, 4*500*m bytes of W)."""
+    import torch
+
+    from coherit_gb300.geno_stream import GenoBlockStreamer, SyntheticSource
+    from coherit_gb300.smile_block_w import SmileBlockWeightedOperator
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n, m, block, k = args.n or 100000, args.m or 300000, 500, args.smile
+    if m % block:
+        raise ValueError("m must be a multiple of the 500-SNP block size")
+    hbm_peak, tensor_peak, peak_src = _peaks()
+    st = GenoBlockStreamer(SyntheticSource(n, m, seed=5), device=dev, precision="bf16x3")
+    rng = np.random.default_rng(5)
+    Ws = []
+    for _ in range(m // block):
+        A = rng.standard_normal((block, block), dtype=np.float32)
+        Ws.append((A @ A.T / np.float32(block)).astype(np.float32))
+    t0 = time.perf_counter()
+    op = SmileBlockWeightedOperator(st, Ws, normalization="kernel_trace", diag_mode="mean")
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    V = torch.randn(n, k, device=dev)
+    for _ in range(max(3, args.warmup)):
+        op.kv(V)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        op.kv(V)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    flops = 4.0 * n * m * k + 2.0 * m * block * k
+    nbytes = n * ((m + 3) // 4) + 4 * block * m + 8 * n * k + 8 * m
+    tfs = flops / (ms * 1e-3) / 1e12
+    st.close()
+    return {"metric": "SMILE block-weighted operator application time", "value": round(ms, 4),
+            "unit": "ms", "higher_is_better": False, "steps": args.steps,
+            "config": {"workload": f"c5_n{n}_m{m}_blocks{m // block}x{block}", "k": k},
+            "build_s": round(build_s, 2),
+            "roofline": {"bound": "tensor", "achieved": round(tfs, 1), "peak": tensor_peak,
+                         "unit": "TFLOP/s", "frac": round(tfs / tensor_peak, 4), "traffic": None,
+                         "algorithmic_flops": flops, "algorithmic_bytes": nbytes,
+                         "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1)},
+            "peak_source": peak_src}
+
+
 def run_stream_only(args, wl):
     """Only the Poisson request stream (``--stream-only``) on the workload's
     matrix, e.g. a prefix of the c4 serving stream (``--config c4``: n=200,000
@@ -728,6 +784,8 @@ def main():
                     help="right-hand-side columns per fit assumed by the reference arm")
     ap.add_argument("--operator", type=int, default=0, metavar="K",
                     help="time bare operator applications of width K instead of fits")
+    ap.add_argument("--smile", type=int, default=0, metavar="K",
+                    help="time the SMILE block-weighted operator (c5 shape) at width K")
     ap.add_argument("--stream-only", action="store_true",
                     help="run only the Poisson request stream on the workload's matrix")
     ap.add_argument("--sparse", type=int, default=0, metavar="K",
@@ -744,6 +802,8 @@ def main():
         out = run_sparse_only(args, wl)
     elif args.stream_only:
         out = run_stream_only(args, wl)
+    elif args.smile > 0:
+        out = run_smile_only(args, wl)
     elif args.impl == "reference":
         out = run_reference(args, wl)
     else:
