@@ -184,9 +184,12 @@ class InfinitesimalREMLFitter:
                             component_variant_indices=cfg.component_variant_indices,
                             sample_mask=cfg.sample_mask, device=cfg.device,
                             precision=cfg.precision)
-            streamers = [GenoBlockStreamer(src, **dense_kw) for src in (cfg.sources or ())]
-            streamers += [GenoBlockStreamer(bed_prefix=p, **dense_kw)
-                          for p in _prefix_list(cfg.bed_prefix)]
+            # Sources take precedence over BED prefixes (reml_model.py:506-546).
+            if cfg.sources is not None:
+                streamers = [GenoBlockStreamer(src, **dense_kw) for src in cfg.sources]
+            else:
+                streamers = [GenoBlockStreamer(bed_prefix=p, **dense_kw)
+                             for p in _prefix_list(cfg.bed_prefix)]
             if has_rare:
                 from .sparse_stream import SparseGenoBlockStreamer
 
