@@ -1,8 +1,10 @@
 """Pin the CPU oracle to the known-answer checks of the reference's own tests.
 
 Each test restates one check of the reference suite (file:line given) and
-runs it against the oracle restatement.  The same checks run against the GPU
-implementation in the gpu-marked tests.
+runs it against the oracle restatement.  The package runs the same checks:
+the PCG ones on the GPU (test_gpu_pcg.py), the SLQ, affine-SLQ and Fisher-step
+ones on CPU tensors (test_reml_host.py), since that code reaches the device
+only through the operator callable.
 """
 import numpy as np
 import pytest

@@ -1,0 +1,445 @@
+"""Host numerics of the REML driver, run on CPU tensors against the oracle.
+
+The package's SLQ (slq.py:143-213 of the reference), affine SLQ
+(reml.py:367-486), projected-core preconditioner (precond.py:42-276) and
+bounded Fisher step (reml.py:979-1247) are plain torch / numpy code that runs
+on whatever device its inputs live on; on the device they only see the
+genotype operator through a callable.  Here they run on CPU over dense
+operators, so the same known-answer checks that pin the oracle pin them too,
+and each result is compared with the oracle on the same probes.
+"""
+import numpy as np
+import pytest
+import torch
+
+from coherit_gb300 import precond as prec
+from coherit_gb300 import reml
+from coherit_gb300 import slq
+from oracle import precond as oprec
+from oracle import reml as oreml
+from oracle import slq as oslq
+
+CPU = torch.device("cpu")
+EPS32 = float(np.finfo(np.float32).eps)
+EPS64 = float(np.finfo(np.float64).eps)
+
+
+# ------------------------------------------------------------------- SLQ
+
+def _slq_problem(kind):
+    # tests/test_multi_slq_score_consistency.py:19-35 of the reference
+    rng = np.random.default_rng(904)
+    n = 24
+    kernels = []
+    for width in (13, 21, 37):
+        raw = rng.normal(size=(n, width))
+        kernels.append(raw @ raw.T / width)
+    if kind == "scalar":
+        kernels = [np.eye(n), 2 * np.eye(n), 3 * np.eye(n)]
+    elif kind == "clustered":
+        kernels = [np.eye(n) + 1e-4 * k for k in kernels]
+    theta = np.array([.21, .16, .28, .57])
+    if kind == "zero":
+        theta[:3] = 0
+    elif kind == "ill_conditioned":
+        theta[:] = [.8, .01, .01, .002]
+    return np.stack([*kernels, np.eye(n)]), theta
+
+
+_PROBES = np.random.default_rng(73).choice([-1.0, 1.0], size=(24, 4))
+
+
+def _package_slq(directions, theta, depth, *, dtype=torch.float64, budget=64 * 1024 ** 2,
+                 value_only=False, eps=EPS64, accept_value=None):
+    D = torch.as_tensor(directions, dtype=dtype)
+    t = torch.as_tensor(theta, dtype=dtype)
+    A = torch.einsum("k,kij->ij", t, D)
+
+    def mv(v):
+        return A @ v
+
+    def pullback(left, right):
+        products = torch.einsum("kij,js->kis", D, left)
+        return (torch.einsum("k,kns->ns", t, products),
+                torch.einsum("ns,kns->k", right, products).double())
+
+    value, grad = slq.logdet_value_and_grad(
+        mv, None if value_only else pullback, 24, 0, nsamples=_PROBES.shape[1], m=depth,
+        workspace_bytes=budget, dtype=dtype, accept_value=accept_value, device=CPU,
+        probes=torch.as_tensor(_PROBES), eps=eps)
+    return float(value), (None if grad is None else grad.numpy())
+
+
+def _oracle_slq(directions, theta, depth, *, budget=64 * 1024 ** 2, eps=EPS64, itemsize=8):
+    A = np.einsum("k,kij->ij", theta, directions)
+
+    def pullback(left, right):
+        products = np.einsum("kij,js->kis", directions, left)
+        return np.einsum("k,kns->ns", theta, products), np.einsum("ns,kns->k", right, products)
+
+    return oslq.logdet_value_and_grad(lambda v: A @ v, pullback, 24, _PROBES, m=depth,
+                                      workspace_bytes=budget, itemsize=itemsize, eps=eps)
+
+
+@pytest.mark.parametrize("kind", ["regular", "scalar", "clustered", "zero", "ill_conditioned"])
+@pytest.mark.parametrize("depth", [1, 10, 30])
+def test_slq_fp64_equals_oracle(kind, depth):
+    d, t = _slq_problem(kind)
+    value, grad = _package_slq(d, t, depth)
+    ref_value, ref_grad = _oracle_slq(d, t, depth)
+    np.testing.assert_allclose(value, ref_value, rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(grad, ref_grad, rtol=1e-8, atol=1e-9)
+
+
+# tests/test_multi_slq_score_consistency.py:54-71 of the reference
+@pytest.mark.parametrize("kind", ["regular", "ill_conditioned"])
+def test_slq_gradient_matches_finite_difference(kind):
+    d, t = _slq_problem(kind)
+    value, grad = _package_slq(d, t, 10)
+    delta = 1e-6 if kind == "ill_conditioned" else 2e-5
+    fd = []
+    for k in range(len(t)):
+        off = np.eye(len(t))[k] * delta
+        fd.append((_package_slq(d, t + off, 10)[0] - _package_slq(d, t - off, 10)[0])
+                  / (2 * delta))
+    np.testing.assert_allclose(grad, fd, rtol=2e-3, atol=3e-3)
+
+
+# tests/test_multi_slq_score_consistency.py:74-97 of the reference
+@pytest.mark.parametrize("kind", ["regular", "scalar", "clustered", "zero", "ill_conditioned"])
+def test_slq_full_depth_equals_dense_probe_form(kind):
+    d, t = _slq_problem(kind)
+    value, grad = _package_slq(d, t, 50, eps=EPS32)
+    matrix = np.einsum("k,kij->ij", t, d)
+    vals, vecs = np.linalg.eigh(matrix)
+    z = _PROBES
+    log_matrix = (vecs * np.log(vals)) @ vecs.T
+    expected = np.einsum("ns,nm,ms->", z, log_matrix, z) / 4
+    assert np.isfinite(grad).all()
+    np.testing.assert_allclose(value, expected, rtol=1e-3, atol=1e-3)
+    gap = vals[:, None] - vals[None, :]
+    divided = np.divide(np.log(vals[:, None]) - np.log(vals[None, :]), gap,
+                        out=1 / np.broadcast_to(vals, gap.shape).copy(), where=np.abs(gap) > 1e-12)
+    coeff = vecs.T @ z
+    gm = vecs @ (divided * (coeff @ coeff.T / 4)) @ vecs.T
+    np.testing.assert_allclose(grad, np.einsum("ij,kij->k", gm, d), rtol=2e-3, atol=2e-3)
+    vo = _package_slq(d, t, 50, value_only=True, eps=EPS32)
+    assert vo[0] == value and vo[1] is None
+
+
+# tests/test_multi_slq_score_consistency.py:100-107 of the reference
+def test_slq_probe_batching_invariance():
+    d, t = _slq_problem("regular")
+    full = _package_slq(d, t, 10)
+    single = _package_slq(d, t, 10, budget=1)
+    np.testing.assert_allclose(single[0], full[0], atol=1e-10)
+    np.testing.assert_allclose(single[1], full[1], atol=1e-9)
+
+
+def test_slq_deferred_gradient_follows_accept_value():
+    d, t = _slq_problem("regular")
+    full = _package_slq(d, t, 10)
+    rejected = _package_slq(d, t, 10, accept_value=lambda v: False)
+    accepted = _package_slq(d, t, 10, accept_value=lambda v: True)
+    assert rejected[0] == full[0] and rejected[1] is None
+    assert accepted[0] == full[0]
+    np.testing.assert_allclose(accepted[1], full[1], rtol=1e-12, atol=1e-14)
+
+
+def test_slq_fp32_within_logdet_tolerance_of_oracle():
+    d, t = _slq_problem("regular")
+    value, grad = _package_slq(d, t, 10, dtype=torch.float32, eps=EPS32)
+    ref_value, ref_grad = _oracle_slq(d, t, 10, eps=EPS32, itemsize=4)
+    np.testing.assert_allclose(value, ref_value, rtol=1e-4)
+    np.testing.assert_allclose(grad, ref_grad, rtol=1e-3, atol=1e-4)
+
+
+def test_slq_rejects_non_finite_operator():
+    d, t = _slq_problem("regular")
+    with pytest.raises(FloatingPointError):
+        slq.logdet_value_and_grad(lambda v: v * float("nan"), None, 24, 0, nsamples=4, m=5,
+                                  dtype=torch.float64, device=CPU,
+                                  probes=torch.as_tensor(_PROBES))
+
+
+def test_rademacher_probes_are_signs_and_seeded():
+    a = slq.rademacher(50, 7, 11, CPU)
+    b = slq.rademacher(50, 7, 11, CPU)
+    assert torch.equal(a, b)
+    assert set(torch.unique(a).tolist()) <= {-1.0, 1.0}
+    assert not torch.equal(a, slq.rademacher(50, 7, 12, CPU))
+
+
+@pytest.mark.parametrize("args", [(100, 64, 30, 256 * 1024 ** 2), (5000, 128, 30, 1),
+                                  (3, 9, 50, 10 ** 6), (50000, 64, 30, 2 * 1024 ** 3)])
+def test_workspace_layout_equals_oracle(args):
+    assert slq.workspace_layout(*args) == oslq.workspace_layout(*args)
+
+
+# ------------------------------------------------------------ affine SLQ
+
+def _affine_problem(n=12, width=20, seed=5):
+    rng = np.random.default_rng(seed)
+    raw = rng.normal(size=(n, width))
+    K = raw @ raw.T / width + 0.08 * np.eye(n)
+    z = rng.choice([-1.0, 1.0], size=(n, 6))
+    return K, z
+
+
+@pytest.mark.parametrize("m", [4, 12])
+def test_affine_slq_equals_oracle(m):
+    K, z = _affine_problem()
+    n = K.shape[0]
+    Kt = torch.as_tensor(K, dtype=torch.float32)
+    cache = reml._build_affine_slq_cache(lambda v: Kt @ v, n, 0, nsamples=z.shape[1], m=m,
+                                         probes=torch.as_tensor(z), device=CPU)
+    ref = oslq.affine_cache(lambda v: K @ v, n, z, m)
+    for tg, te in [(0.4, 0.6), (1.3, 0.2), (0.0, 1.0)]:
+        ld, der = reml._affine_slq_logdet(cache, tg, te, return_derivatives=True)
+        ref_ld, ref_der = oslq.affine_logdet(ref, tg, te)
+        np.testing.assert_allclose(float(ld), ref_ld, rtol=1e-4)
+        np.testing.assert_allclose(der.numpy(), ref_der, rtol=1e-3, atol=1e-4)
+        assert float(reml._affine_slq_logdet(cache, tg, te)) == float(ld)
+
+
+# tests/test_affine_slq_score_consistency.py:149-169 of the reference
+def test_affine_slq_derivatives_finite_at_zero_genetic_variance():
+    rng = np.random.default_rng(20260723)
+    n = 10
+    raw = rng.normal(size=(n, 14))
+    K = torch.as_tensor(raw @ raw.T / raw.shape[1] + 0.08 * np.eye(n), dtype=torch.float32)
+    z = torch.as_tensor(rng.choice([-1.0, 1.0], size=(n, 5)))
+    cache = reml._build_affine_slq_cache(lambda v: K @ v, n, 0, nsamples=5, m=n, probes=z,
+                                         device=CPU)
+    ld, der = reml._affine_slq_logdet(cache, 0.0, 1.0, return_derivatives=True)
+    assert np.isfinite(float(ld)) and bool(torch.all(torch.isfinite(der)))
+    eps = 2e-3
+    fwd = (float(reml._affine_slq_logdet(cache, eps, 1.0)) - float(ld)) / eps
+    np.testing.assert_allclose(float(der[0]), fwd, atol=2e-2, rtol=2e-2)
+    np.testing.assert_allclose(float(der[1]), n, atol=2e-4, rtol=2e-5)
+
+
+# ------------------------------------------------------ projected core
+
+def _precond_problem(n=40, r=6, G=2, seed=3):
+    rng = np.random.default_rng(seed)
+    U, _ = np.linalg.qr(rng.normal(size=(n, r)))
+    atoms = []
+    for _ in range(G):
+        a = rng.normal(size=(r, r))
+        atoms.append(a @ a.T / r)
+    return U, np.stack(atoms)
+
+
+def _confs(U, atoms, diag_atoms, residual_atoms):
+    G, r = atoms.shape[0], U.shape[1]
+    conf = prec.ProjectedCorePrecondConf(
+        U=torch.as_tensor(U), core_atoms=torch.as_tensor(atoms), total_rank=r, n_grm=G,
+        diag_mode="scalar_identity", diag_atoms=torch.as_tensor(diag_atoms),
+        residual_diag_atoms=torch.as_tensor(residual_atoms))
+    oconf = oprec.Conf(U=U, core_atoms=atoms, total_rank=r, n_grm=G, diag_atoms=diag_atoms,
+                       residual_diag_atoms=residual_atoms)
+    return conf, oconf
+
+
+def test_projected_core_equals_oracle():
+    U, atoms = _precond_problem()
+    conf, oconf = _confs(U, atoms, np.array([0.9, 1.1]), np.array([1.0, 0.5]))
+    theta_g, theta_e = np.array([0.3, 0.7]), np.array([0.4, 0.2])
+    d = prec.scalar_diag_from_precond_conf(conf, torch.as_tensor(theta_g), theta_e)
+    od = oprec.scalar_diag(oconf, theta_g, theta_e)
+    assert float(d) == pytest.approx(od, rel=1e-14)
+    rt = prec.build_projected_core_runtime(conf, theta_g, d, eps=1e-3, need_invsqrt=True)
+    ort = oprec.runtime(oconf, theta_g, od, eps=1e-3, need_invsqrt=True)
+    v = np.random.default_rng(8).normal(size=(U.shape[0], 3))
+    apply = prec.make_projected_core_precond_from_runtime(rt)
+    np.testing.assert_allclose(apply(torch.as_tensor(v)).numpy(), oprec.apply_inverse(ort, v),
+                               rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(apply(torch.as_tensor(v[:, 0])).numpy(),
+                               oprec.apply_inverse(ort, v[:, 0]), rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(prec.projected_core_apply_invsqrt(rt, torch.as_tensor(v)).numpy(),
+                               oprec.apply_invsqrt(ort, v), rtol=1e-12, atol=1e-13)
+    n = U.shape[0]
+    assert float(prec.projected_core_logdet(rt, n)) == pytest.approx(oprec.logdet(ort, n),
+                                                                     rel=1e-13)
+    # M = d I + U C U^T: the inverse inverts it and the inverse square root squares to it.
+    C = np.tensordot(theta_g, atoms, axes=1)
+    M = float(rt.d) * np.eye(n) + U @ C @ U.T
+    np.testing.assert_allclose(M @ apply(torch.as_tensor(v)).numpy(), v, atol=1e-11)
+    half = prec.projected_core_apply_invsqrt(rt, torch.as_tensor(np.eye(n))).numpy()
+    np.testing.assert_allclose(half @ half @ M, np.eye(n), atol=1e-10)
+    np.testing.assert_allclose(float(prec.projected_core_logdet(rt, n)),
+                               np.linalg.slogdet(M)[1], rtol=1e-12)
+
+
+def test_projected_core_contract_errors():
+    U, atoms = _precond_problem()
+    conf, _ = _confs(U, atoms, np.array([1.0, 1.0]), np.array([1.0, 1.0, 1.0]))
+    with pytest.raises(ValueError, match="residual_diag_atoms"):
+        prec.scalar_diag_from_precond_conf(conf, torch.as_tensor([0.3, 0.7]), [0.4, 0.2])
+    conf.diag_mode = None
+    assert prec.scalar_diag_from_precond_conf(conf, torch.as_tensor([0.3, 0.7]), [0.4]) is None
+    with pytest.raises(NotImplementedError):
+        prec.build_projected_core_runtime(conf, [0.3, 0.7], 1.0)
+    conf.diag_mode = "scalar_identity"
+    with pytest.raises(ValueError, match="scalar diagonal"):
+        prec.build_projected_core_runtime(conf, [0.3, 0.7], [1.0, 2.0])
+    rt = prec.build_projected_core_runtime(conf, [0.3, 0.7], 1.0)
+    with pytest.raises(ValueError, match="eigendecomposition"):
+        prec.projected_core_apply_invsqrt(rt, torch.ones(U.shape[0]))
+    with pytest.raises(ValueError, match="smaller than"):
+        prec.projected_core_logdet(rt, U.shape[1] - 1)
+    assert prec.build_projected_core_runtime(None, [0.3], 1.0) is None
+    assert prec.make_precond(None, [0.3], 1.0) is None
+
+
+def test_lowrank_basis_equals_oracle():
+    rng = np.random.default_rng(12)
+    n, width = 60, 9
+    raw = rng.normal(size=(n, width))
+    K = raw @ raw.T / width
+    omega = rng.normal(size=(n, 7 + 4))
+    Kt = torch.as_tensor(K)
+    U, ev = prec.build_lowrank_basis(lambda v: Kt @ v, n, 7, oversample=4, dtype=torch.float64,
+                                     device=CPU, omega=torch.as_tensor(omega))
+    oU, oev = oprec.lowrank_basis(lambda v: K @ v, omega, 7)
+    np.testing.assert_allclose(ev.numpy(), oev, rtol=1e-10, atol=1e-12)
+    # Eigenvectors are defined up to sign: compare the projectors.
+    np.testing.assert_allclose(U.numpy() @ U.numpy().T, oU @ oU.T, atol=1e-9)
+    np.testing.assert_allclose(U.numpy().T @ U.numpy(), np.eye(7), atol=1e-12)
+    # A rank-9 kernel sketched with 11 columns recovers its leading spectrum.
+    np.testing.assert_allclose(ev.numpy(), np.linalg.eigvalsh(K)[::-1][:7], rtol=1e-8)
+
+
+# ------------------------------------------------------- Fisher step
+
+def _fisher_cases():
+    rng = np.random.default_rng(2026)
+    cases = []
+    for G in (1, 2, 4, 8):
+        for case in range(6):
+            P = G + 1
+            a = rng.normal(size=(P, P))
+            ai = a @ a.T / P + 0.05 * np.eye(P)
+            param = np.abs(rng.normal(size=P)) * 0.5
+            grad = rng.normal(size=P)
+            if case >= 2:
+                param[: G // 2 + 1] = 0.0          # genetic components at their bound
+            if case >= 3:
+                grad[0] = -abs(grad[0])            # pushing further into the bound: frozen
+            if case >= 4:
+                param[G] = 1e-2                    # residual at its floor
+                grad[G] = -abs(grad[G])
+            if case == 5:
+                ai = np.outer(a[0], a[0])          # rank-one: needs the ridge and jitter
+            cases.append((G, param, grad, ai))
+    return cases
+
+
+@pytest.mark.parametrize("alpha", [1.0, 0.5, 0.25])
+def test_fisher_step_equals_oracle(alpha):
+    for G, param, grad, ai in _fisher_cases():
+        FI = reml.AverageInfoMatrix(mat=ai)
+        d, frozen = reml._projected_fisher_direction(param, grad, FI, n_genetic=G,
+                                                     genetic_zero_tol=1e-8, residual_floor=1e-2,
+                                                     trial_alpha=alpha)
+        od = oreml.fisher_step(param, grad, ai, G=G, zero_tol=1e-8, floor=1e-2, alpha=alpha)
+        np.testing.assert_allclose(d, od, rtol=1e-9, atol=1e-10)
+        new, delta = reml._apply_projected_step(param, d, alpha, n_genetic=G,
+                                                genetic_zero_tol=1e-8, residual_floor=1e-2)
+        onew = oreml.apply_step(param, od, alpha, G=G, zero_tol=1e-8, floor=1e-2)
+        np.testing.assert_allclose(new, onew, rtol=1e-9, atol=1e-10)
+        np.testing.assert_allclose(delta, new - param)
+        assert np.all(new[:G] >= 0) and np.all(new[G:] >= 1e-2)
+        assert frozen.shape == (G,)
+
+
+def test_fisher_step_is_kkt_point_of_the_bounded_qp():
+    for G, param, grad, ai in _fisher_cases():
+        FI = reml.AverageInfoMatrix(mat=ai)
+        d, _ = reml._projected_fisher_direction(param, grad, FI, n_genetic=G,
+                                                genetic_zero_tol=1e-8, residual_floor=1e-2)
+        lower = np.concatenate([np.zeros(G), np.full(param.size - G, 1e-2)]) - param
+        system = 0.5 * (ai + ai.T) + reml.FI_SYSTEM_RIDGE * np.eye(param.size)
+        kkt = grad - system @ d
+        at_bound = d <= lower + 1e-10
+        tol = 1e-6 * max(1.0, np.max(np.abs(grad))) * 10
+        assert np.all(d >= lower - 1e-10)
+        np.testing.assert_allclose(kkt[~at_bound], 0.0, atol=tol)
+        assert np.all(kkt[at_bound] <= tol)
+
+
+def test_fisher_step_contract_errors():
+    FI = reml.AverageInfoMatrix(mat=np.eye(3))
+    with pytest.raises(ValueError):
+        reml._projected_fisher_direction([1, 1, 1], [0, 0, 0], FI, n_genetic=4,
+                                         genetic_zero_tol=1e-8)
+    with pytest.raises(ValueError):
+        reml._projected_fisher_direction([1, 1, 1], [0, 0, 0], FI, genetic_zero_tol=1e-8,
+                                         residual_floor=-1.0)
+    with pytest.raises(ValueError):
+        reml._projected_fisher_direction([1, 1, 1], [0, 0, 0], FI, genetic_zero_tol=1e-8,
+                                         trial_alpha=0.0)
+    with pytest.raises(ValueError, match="shape"):
+        reml._projected_fisher_direction([1, 1], [0, 0], FI, genetic_zero_tol=1e-8)
+    with pytest.raises(FloatingPointError):
+        reml._projected_fisher_direction([1, 1, 1], [0, np.nan, 0], FI, genetic_zero_tol=1e-8)
+
+
+def test_fisher_stats_record_the_active_set():
+    stats = reml.FisherSolveStats()
+    FI = reml.AverageInfoMatrix(mat=np.eye(3), stats=stats)
+    d, frozen = reml._projected_fisher_direction([0.0, 0.5, 0.3], [-1.0, 0.2, 0.1], FI,
+                                                 genetic_zero_tol=1e-8, residual_floor=1e-2)
+    assert frozen.tolist() == [True, False]
+    assert d[0] == 0.0
+    assert stats.frozen_genetic == 1 and stats.free_dim == 2
+
+
+# ------------------------------------------------- small host helpers
+
+def test_standardize_response_equals_oracle():
+    y = np.random.default_rng(4).normal(3.0, 2.5, size=513).astype(np.float32)
+    ys, mu, scale = reml.standardize_response(y)
+    oys, omu, oscale = oreml.standardize(y)
+    np.testing.assert_allclose(ys.numpy(), oys, rtol=1e-6, atol=1e-6)
+    assert float(mu) == pytest.approx(omu, rel=1e-6)
+    assert float(scale) == pytest.approx(oscale, rel=1e-6)
+    for bad in ([], [1.0, float("nan")], [2.0, 2.0, 2.0]):
+        with pytest.raises(ValueError):
+            reml.standardize_response(np.asarray(bad, np.float32))
+
+
+def test_stable_cholesky_equals_oracle():
+    rng = np.random.default_rng(6)
+    a = rng.normal(size=(5, 3))
+    for A in (a @ a.T, a @ a.T + np.eye(5), np.diag([1.0, 1e-14, 2.0])):
+        L = reml._stable_cho_factor_spd(torch.as_tensor(A)).numpy()
+        np.testing.assert_allclose(L, oreml.stable_chol(A), rtol=1e-10, atol=1e-12)
+    # The jitter grows to 10 x the mean |diagonal| (1 when that is 0): -I is
+    # rescued, an indefinite matrix with eigenvalues +-100 and zero diagonal is not.
+    np.testing.assert_allclose(reml._stable_cho_factor_spd(torch.as_tensor(-np.eye(3))).numpy(),
+                               oreml.stable_chol(-np.eye(3)), rtol=1e-12)
+    indefinite = np.array([[0.0, 100.0], [100.0, 0.0]])
+    for fn in (lambda: reml._stable_cho_factor_spd(torch.as_tensor(indefinite)),
+               lambda: oreml.stable_chol(indefinite)):
+        with pytest.raises(FloatingPointError):
+            fn()
+
+
+def test_fixed_effect_design_validation():
+    rng = np.random.default_rng(7)
+    X = np.column_stack([np.ones(50), rng.normal(size=50)])
+    reml._validate_fixed_effect_design(torch.as_tensor(X))
+    for bad in (np.column_stack([X, np.zeros(50)]), np.column_stack([X, 2 * X[:, 1]])):
+        with pytest.raises(ValueError):
+            reml._validate_fixed_effect_design(torch.as_tensor(bad))
+
+
+def test_mean_diag_atoms():
+    atoms = reml._mean_diag_atoms([1.5, np.array([1.0, 3.0]), torch.tensor(2.0)], n_samples=2)
+    np.testing.assert_array_equal(atoms, [1.5, 2.0, 2.0])
+    with pytest.raises(ValueError, match="length mismatch"):
+        reml._mean_diag_atoms([np.ones(3)], n_samples=2)
+    with pytest.raises(ValueError):
+        reml._mean_diag_atoms([np.array([-1.0, 1.0])])
