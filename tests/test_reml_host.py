@@ -146,6 +146,61 @@ def test_slq_deferred_gradient_follows_accept_value():
     np.testing.assert_allclose(accepted[1], full[1], rtol=1e-12, atol=1e-14)
 
 
+# tests/test_reml_lazy_evaluation.py:79-105 of the reference: a rejected value
+# never costs a reverse pass when the batches fit the workspace, and the value
+# never repeats a forward product.
+@pytest.mark.parametrize("budget", [1, 50000, 1 << 20])
+@pytest.mark.parametrize("accepted", [False, True])
+@pytest.mark.parametrize("impl", ["package", "oracle"])
+def test_slq_gate_preserves_value_and_never_repeats_forward_products(budget, accepted, impl):
+    calls = {"forward": 0, "reverse": 0}
+    diag = np.linspace(.3, 2., 24)
+    probes = np.random.default_rng(54).choice([-1.0, 1.0], size=(24, 6))
+    if impl == "package":
+        matrix = torch.diag(torch.as_tensor(diag, dtype=torch.float32))
+
+        def mv(b):
+            calls["forward"] += 1
+            return matrix @ b
+
+        def pullback(left, right):
+            calls["reverse"] += 1
+            product = matrix @ left
+            return product, torch.sum(product * right).double().reshape(1)
+
+        def run(**kw):
+            return slq.logdet_value_and_grad(mv, pullback, 24, 0, nsamples=6, m=8,
+                                             workspace_bytes=budget, device=CPU,
+                                             probes=torch.as_tensor(probes), **kw)
+    else:
+        matrix = np.diag(diag)
+
+        def mv(b):
+            calls["forward"] += 1
+            return matrix @ b
+
+        def pullback(left, right):
+            calls["reverse"] += 1
+            product = matrix @ left
+            return product, np.asarray([np.sum(product * right)])
+
+        def run(**kw):
+            return oslq.logdet_value_and_grad(mv, pullback, 24, probes, m=8,
+                                              workspace_bytes=budget, **kw)
+    expected = run()
+    eager = dict(calls)
+    calls.update(forward=0, reverse=0)
+    actual = run(accept_value=lambda value: accepted)
+    assert float(actual[0]) == float(expected[0])
+    assert calls["forward"] == eager["forward"]
+    if accepted:
+        np.testing.assert_array_equal(np.asarray(actual[1]), np.asarray(expected[1]))
+        assert calls["reverse"] == eager["reverse"]
+    else:
+        assert actual[1] is None
+        assert calls["reverse"] == (eager["reverse"] if budget == 1 else 0)
+
+
 def test_slq_fp32_within_logdet_tolerance_of_oracle():
     d, t = _slq_problem("regular")
     value, grad = _package_slq(d, t, 10, dtype=torch.float32, eps=EPS32)
@@ -443,3 +498,142 @@ def test_mean_diag_atoms():
         reml._mean_diag_atoms([np.ones(3)], n_samples=2)
     with pytest.raises(ValueError):
         reml._mean_diag_atoms([np.array([-1.0, 1.0])])
+
+
+# ------------------------------------------- fit_reml up to its first evaluation
+#
+# fit_reml's validation, probe set-up, affine SLQ cache and right-hand-side
+# assembly run on the device of its inputs; the first device-bound step is
+# the first _eval_once (PCG on the genotype operator).  Replacing it with a
+# recorder that stops the fit checks that set-up on CPU.
+
+class _Stop(Exception):
+    pass
+
+
+def _record_first_eval(monkeypatch):
+    seen = []
+
+    def recorder(ctx, pvec, warm_all, warm_ai=None, **kw):
+        seen.append((ctx, np.array(pvec), kw))
+        raise _Stop
+
+    monkeypatch.setattr(reml, "_eval_once", recorder)
+    return seen
+
+
+def _kernels(groups):
+    d, _ = _slq_problem("regular")
+    mats = [torch.as_tensor(k, dtype=torch.float32) for k in d[:groups]]
+    return tuple(lambda b, k=k: k @ b for k in mats), tuple(torch.diagonal(k) for k in mats)
+
+
+# tests/test_multi_slq_score_consistency.py:110-137 of the reference
+@pytest.mark.parametrize("groups,optimizer,requested,residual,expected", [
+    (2, "strict", .005, False, 1e-5),
+    (2, "strict", 1e-6, False, 1e-6),
+    (1, "strict", .005, False, .005),
+    (1, "strict", .005, True, 1e-5),
+    (2, "smile_scoring", .005, False, .005),
+])
+def test_pcg_tolerance_clamp(monkeypatch, groups, optimizer, requested, residual, expected):
+    seen = _record_first_eval(monkeypatch)
+    K_mvs, diags = _kernels(groups)
+    y = np.random.default_rng(41).normal(size=24).astype(np.float32)
+    with pytest.raises(_Stop):
+        reml.fit_reml(y, K_mvs, diags, None, n_rand_vec=3, maxiter=100, minq_iter=0,
+                      slq_samples=3, slq_m=8, pcg_tol=requested, optimizer=optimizer,
+                      verbose=False, device="cpu",
+                      residual_diag_list=[torch.linspace(.5, 1.5, 24)] if residual else None)
+    assert [kw["minq_tol"] for _, _, kw in seen] == [expected]
+
+
+# tests/test_reml_lazy_evaluation.py:35-77 of the reference: strict fits carry
+# no Hutchinson probes in their right-hand sides; scoring fits cache K_i Z for
+# their probes, and switching back invalidates it.
+def test_probe_columns_and_cache_follow_the_optimizer(monkeypatch):
+    seen = _record_first_eval(monkeypatch)
+    K_mvs, diags = _kernels(2)
+    rng = np.random.default_rng(684)
+    args = dict(y=rng.normal(size=24).astype(np.float32), K_mvs=K_mvs, diag_list=diags,
+                covar=torch.ones((24, 1)), n_rand_vec=7, maxiter=100, minq_iter=1,
+                slq_samples=4, slq_m=8, pcg_tol=1e-5, verbose=False,
+                response_is_standardized=True, device="cpu")
+    cache = reml.REMLProbeCache()
+    with pytest.raises(_Stop):
+        reml.fit_reml(**args, probe_cache=cache)
+    ctx = seen[-1][0]
+    assert ctx.rhs_const.shape == (24, 2) and ctx.R_rand == 0 and ctx.kvrand_stack is None
+    assert cache.kvrand_stack is None
+    signature = cache.signature
+    with pytest.raises(_Stop):
+        reml.fit_reml(**{**args, "n_rand_vec": 17}, probe_cache=cache)
+    assert cache.signature == signature
+    with pytest.raises(_Stop):
+        reml.fit_reml(**args, optimizer="smile_scoring", probe_cache=cache)
+    ctx = seen[-1][0]
+    assert ctx.rhs_const.shape == (24, 9) and ctx.R_rand == 7
+    assert tuple(cache.kvrand_stack.shape) == (2, 24, 7)
+    probes = ctx.rhs_const[:, 2:]
+    for g in range(2):
+        torch.testing.assert_close(cache.kvrand_stack[g], K_mvs[g](probes))
+    with pytest.raises(_Stop):
+        reml.fit_reml(**args, probe_cache=cache)
+    assert cache.kvrand_stack is None
+
+
+def test_single_grm_affine_cache_is_reused_for_the_same_operator(monkeypatch):
+    seen = _record_first_eval(monkeypatch)
+    K_mvs, diags = _kernels(1)
+    y = np.random.default_rng(3).normal(size=24).astype(np.float32)
+    cache = reml.REMLProbeCache()
+    common = dict(n_rand_vec=3, maxiter=50, slq_samples=5, slq_m=6, verbose=False,
+                  device="cpu", probe_cache=cache)
+    with pytest.raises(_Stop):
+        reml.fit_reml(y, K_mvs, diags, None, **common)
+    first = cache.affine_slq
+    assert first is not None and seen[-1][0].affine_slq_cache is first
+    assert tuple(first.alphas_k.shape) == (6, 5) and tuple(first.betas_k.shape) == (5, 5)
+    with pytest.raises(_Stop):
+        reml.fit_reml(2 * y + 1, K_mvs, diags, None, **common)
+    assert cache.affine_slq is first and seen[-1][0].affine_slq_cache is first
+    with pytest.raises(_Stop):        # another operator tuple: rebuilt
+        reml.fit_reml(y, tuple(K_mvs), diags, None, **{**common, "seed": 1})
+    assert cache.affine_slq is not first
+
+
+def test_initial_parameters_and_standardisation(monkeypatch):
+    seen = _record_first_eval(monkeypatch)
+    K_mvs, diags = _kernels(2)
+    y = np.random.default_rng(8).normal(2.0, 3.0, size=24).astype(np.float32)
+    with pytest.raises(_Stop):
+        reml.fit_reml(y, K_mvs, diags, None, n_rand_vec=3, maxiter=50, h2_init=0.4,
+                      verbose=False, device="cpu")
+    ctx, p0, _ = seen[-1]
+    atoms = reml._mean_diag_atoms(diags, n_samples=24)
+    np.testing.assert_allclose(p0, np.r_[np.full(2, 0.4 / atoms.sum()), 0.6])
+    oys, _, _ = oreml.standardize(y)
+    np.testing.assert_allclose(ctx.y.numpy(), oys, rtol=1e-6, atol=1e-6)
+    with pytest.raises(_Stop):
+        reml.fit_reml(y, K_mvs, diags, None, n_rand_vec=3, maxiter=50, verbose=False,
+                      device="cpu", param_init=[-1.0, 1e-9 / 2, 1e-3])
+    np.testing.assert_array_equal(seen[-1][1], [0.0, 0.0, 1e-2])
+
+
+@pytest.mark.parametrize("kwargs,exc", [
+    (dict(n_rand_vec=0), ValueError), (dict(maxiter=0), ValueError),
+    (dict(minq_iter=-1), ValueError), (dict(slq_m=0), ValueError),
+    (dict(h2_init=1.5), ValueError), (dict(slq_mode="dense"), ValueError),
+    (dict(residual_floor=0.0), ValueError), (dict(optimizer="newton"), ValueError),
+    (dict(pcg_tol=0.0), ValueError), (dict(param_init=[1.0, 1.0]), ValueError),
+    (dict(covar=np.ones((24, 24))), ValueError), (dict(covar=np.ones((23, 1))), ValueError),
+    (dict(residual_diag_list=[-torch.ones(24)]), ValueError),
+    (dict(mean_information=object()), NotImplementedError),
+])
+def test_fit_reml_contract_errors(kwargs, exc):
+    K_mvs, diags = _kernels(2)
+    args = dict(y=np.ones(24, np.float32) + np.arange(24, dtype=np.float32), K_mvs=K_mvs,
+                diag_list=diags, covar=None, n_rand_vec=3, maxiter=50, verbose=False,
+                device="cpu")
+    with pytest.raises(exc):
+        reml.fit_reml(**{**args, **kwargs})
