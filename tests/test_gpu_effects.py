@@ -109,3 +109,31 @@ def test_batched_hinv_solves(cuda):
     with pytest.raises(RuntimeError, match="did not converge"):
         solve_hinv_columns_batched(hv=hv, precond=None, rhs=B[:, :4], warm_start=None, tol=1e-9,
                                    maxiter=1, batch_size=4, stage="screen")
+
+
+# tests/test_sparse_reml_regressions.py:437-455 of the reference
+def test_hinv_column_batches_bound_rhs_and_match_exact_solution(cuda):
+    rhs = np.arange(35, dtype=np.float32).reshape(7, 5) + 1.0
+    X, diag = solve_hinv_columns_batched(hv=lambda v: 2.0 * v, precond=lambda v: 0.5 * v, rhs=rhs,
+                                         warm_start=np.zeros_like(rhs), tol=1e-6, maxiter=10,
+                                         batch_size=2, stage="unit test")
+    np.testing.assert_allclose(X, rhs / 2.0, rtol=1e-6, atol=1e-6)
+    assert (diag["n_batches"], diag["n_columns"], diag["batch_size"]) == (3, 5, 2)
+    assert diag["max_iterations"] <= 2
+
+
+# tests/test_sparse_reml_regressions.py:458-473 of the reference
+def test_hinv_warm_hit_checks_the_true_residual_once_per_batch(cuda):
+    rhs = np.arange(35, dtype=np.float32).reshape(7, 5) + 1.0
+    calls = []
+
+    def hv(v):
+        calls.append(v.shape[1])
+        return 2.0 * v
+
+    X, diag = solve_hinv_columns_batched(hv=hv, precond=None, rhs=rhs, warm_start=rhs / 2.0,
+                                         tol=1e-6, maxiter=10, batch_size=2, stage="warm-hit test")
+    np.testing.assert_array_equal(X, rhs / 2.0)
+    assert calls == [2, 2, 1]
+    assert diag["total_batch_iterations"] == 0
+    assert diag["max_true_relative_residual"] == 0.0
