@@ -214,8 +214,10 @@ class InfinitesimalREMLFitter:
             raise ValueError("all streamers must share the sample set")
         self.n = ns.pop()
         self.precond_conf: ProjectedCorePrecondConf | None = None
-        self._probe_cache = REMLProbeCache() if cfg.cache_reml_setup else None
-        self._ops: _OperatorBundle | None = None
+        # (scope, operator bundle) reused across fits when cache_reml_setup is
+        # set, and the probe products that belong to that bundle.
+        self._reml_fit_setup: tuple | None = None
+        self._reml_probe_cache = REMLProbeCache()
         self._smile_operators = self._build_smile_operators()
 
     def _build_smile_operators(self) -> tuple:
@@ -395,13 +397,53 @@ class InfinitesimalREMLFitter:
         return conf
 
     # ------------------------------------------------------------------ fit
+    def _setup_scope(self) -> tuple:
+        """Objects a cached operator bundle and its probe products depend on
+        (reml_model.py:1849-1871): the SMILE operators, every streamer and its
+        statistics arrays.  Streamers replace these arrays when their
+        standardisation changes, so an identity comparison detects it."""
+        items = list(self._smile_operators)
+        for st in self.streamers:
+            items.append(st)
+            items.extend(getattr(st, name, None) for name in (
+                "_means_by_call", "_inv_by_call", "_component_snp_offsets",
+                "_component_eff_m_host", "_eff_m_const", "_cache_to_source_variant_indices"))
+        return tuple(items)
+
+    def close(self) -> None:
+        """Drop the cached set-up and close every streamer (reml_model.py:1818-1838)."""
+        self._reml_fit_setup = None
+        self._reml_probe_cache = REMLProbeCache()
+        self.precond_conf = None
+        for st in getattr(self, "streamers", ()):
+            close_streamer = getattr(st, "close", None)
+            if not callable(close_streamer):
+                continue
+            try:
+                close_streamer()
+            except (OSError, RuntimeError, ValueError, BufferError):
+                logger.debug("Failed to close fitter streamer.", exc_info=True)
+        self.streamers = []
+        self._has_sparse = False
+        self._sparse_streamers = ()
+        self._smile_operators = ()
+
     def fit_infinitesimal(self, y, covar=None, h2_init: float = 0.5, var_components_init=None,
                           *, slq_probes=None, trace_probes=None, precond: bool = True):
         t0 = time.time()
         cfg = self.cfg
-        if self._ops is None or not cfg.cache_reml_setup:
-            self._ops = self._assemble_reml_operators()
-        ops = self._ops
+        if not self.streamers:
+            raise RuntimeError("InfinitesimalREMLFitter is closed.")
+        if cfg.cache_reml_setup:
+            scope = self._setup_scope()
+            setup = self._reml_fit_setup
+            if setup is None or len(setup[0]) != len(scope) or any(
+                    old is not new for old, new in zip(setup[0], scope)):
+                self._reml_fit_setup = (scope, self._assemble_reml_operators())
+                self._reml_probe_cache = REMLProbeCache()
+            ops = self._reml_fit_setup[1]
+        else:
+            ops = self._assemble_reml_operators()
         G = len(ops.K_mvs)
         if precond and cfg.precond_rank > 0 and (self.precond_conf is None or not cfg.cache_reml_setup):
             self._build_projected_core_precond(ops, var_components_init)
@@ -423,7 +465,9 @@ class InfinitesimalREMLFitter:
             response_is_standardized=cfg.response_is_standardized,
             unit_variance_components=cfg.unit_variance_components,
             max_linesearch_trials=cfg.strict_max_linesearch_trials, return_diagnostics=True,
-            verbose=cfg.verbose, probe_cache=self._probe_cache, device=self.streamers[0].dev,
+            verbose=cfg.verbose,
+            probe_cache=self._reml_probe_cache if cfg.cache_reml_setup else None,
+            device=self.streamers[0].dev,
             slq_probes=slq_probes, trace_probes=trace_probes,
         )
         param, history, diag = out
