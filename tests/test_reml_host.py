@@ -637,3 +637,73 @@ def test_fit_reml_contract_errors(kwargs, exc):
                 device="cpu")
     with pytest.raises(exc):
         reml.fit_reml(**{**args, **kwargs})
+
+
+# tests/test_reml_probe_cache.py:55-114 of the reference (the set-up part: the
+# fits themselves need the device)
+@pytest.mark.parametrize("components", [1, 2])
+@pytest.mark.parametrize("optimizer", ["strict", "smile_scoring"])
+def test_probe_cache_follows_seed_and_operators_not_response(monkeypatch, components,
+                                                            optimizer):
+    seen = _record_first_eval(monkeypatch)
+    rng = np.random.default_rng(73)
+    n = 12
+    kernels = []
+    for _ in range(components):
+        x = rng.normal(size=(n, 16))
+        kernels.append(torch.as_tensor(x @ x.T / 16, dtype=torch.float32))
+    operators = tuple(lambda v, k=k: k @ v for k in kernels)
+    calls = {"probes": 0, "lanczos": 0}
+
+    def stacked(v):
+        if v.shape[1] == 7:
+            calls["probes"] += 1
+        return torch.stack([op(v) for op in operators])
+
+    original = reml._build_affine_slq_cache
+
+    def build(*args, **kwargs):
+        calls["lanczos"] += 1
+        return original(*args, **kwargs)
+
+    monkeypatch.setattr(reml, "_build_affine_slq_cache", build)
+    cache = reml.REMLProbeCache()
+    base = dict(K_mvs=operators, diag_list=[torch.diagonal(k) for k in kernels],
+                stacked_kv=stacked, covar=torch.ones((n, 1)), n_rand_vec=7, maxiter=100,
+                minq_iter=0, slq_samples=4, slq_m=8, response_is_standardized=True,
+                pcg_tol=1e-5, verbose=False, optimizer=optimizer, device="cpu")
+    traces = int(optimizer == "smile_scoring")
+    single = int(components == 1)
+
+    def fit(**kw):
+        with pytest.raises(_Stop):
+            reml.fit_reml(**{**base, **kw})
+        return seen[-1][0]
+
+    first = fit(y=rng.normal(size=n), probe_cache=cache)
+    assert calls == {"probes": traces, "lanczos": single}
+    theta = np.array([0.2] * components + [0.6])
+    cached = fit(y=rng.normal(size=n), param_init=theta, probe_cache=cache)
+    assert calls == {"probes": traces, "lanczos": single}
+    assert cached.kvrand_stack is first.kvrand_stack
+    assert cached.affine_slq_cache is first.affine_slq_cache
+    fresh = fit(y=rng.normal(size=n), param_init=theta)
+    assert calls == {"probes": 2 * traces, "lanczos": 2 * single}
+    if traces:
+        torch.testing.assert_close(fresh.kvrand_stack, cached.kvrand_stack)
+    if single:
+        torch.testing.assert_close(fresh.affine_slq_cache.alphas_k,
+                                   cached.affine_slq_cache.alphas_k)
+    before = dict(calls)
+    fit(y=rng.normal(size=n), seed=91, probe_cache=cache)
+    assert calls == {"probes": before["probes"] + traces, "lanczos": before["lanczos"] + single}
+    before = dict(calls)
+    previous = None if cache.kvrand_stack is None else cache.kvrand_stack.clone()
+    changed = tuple(lambda v, k=k: 2 * k @ v for k in kernels)
+    fit(y=rng.normal(size=n), seed=91, probe_cache=cache, K_mvs=changed, stacked_kv=None)
+    if traces:
+        torch.testing.assert_close(cache.kvrand_stack, 2 * previous)
+    else:
+        assert cache.kvrand_stack is None
+    assert cache.signature[0] == changed
+    assert calls["lanczos"] == before["lanczos"] + single
