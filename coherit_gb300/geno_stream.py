@@ -75,6 +75,55 @@ class SyntheticSource:
         return out
 
 
+def _normalize_component_block_sizes(m: int, component_block_sizes) -> list[int]:
+    """Contiguous component sizes: positive, summing to m (geno_stream.py:371-392)."""
+    if component_block_sizes is None:
+        return [int(m)]
+    sizes = np.asarray(component_block_sizes, dtype=np.int64).reshape(-1)
+    if sizes.size == 0:
+        raise ValueError("component_block_sizes must contain at least one block.")
+    if np.any(sizes <= 0):
+        raise ValueError("component_block_sizes must be strictly positive.")
+    total = int(np.sum(sizes))
+    if total != int(m):
+        raise ValueError(f"component_block_sizes must sum to m={int(m)}; got {total}.")
+    return [int(x) for x in sizes.tolist()]
+
+
+def _normalize_component_variant_indices(m: int, component_variant_indices):
+    """Arbitrary variant groups -> (sizes, cache_to_source) (geno_stream.py:395-437).
+
+    Each group is sorted, so the SNPs of a component sit in source order in
+    the cache; groups must be disjoint, free of duplicates and inside [0, m).
+    A group without SNPs is rejected (the reference accepts it as an empty
+    component).
+    """
+    groups = list(component_variant_indices or [])
+    if not groups:
+        raise ValueError("component_variant_indices must contain at least one component.")
+    normalized = []
+    for comp_idx, group in enumerate(groups):
+        arr = np.asarray(group, dtype=np.int64).reshape(-1)
+        if arr.size == 0:
+            raise ValueError(f"component_variant_indices[{comp_idx}] is empty; every "
+                             "component needs at least one SNP.")
+        if np.any((arr < 0) | (arr >= int(m))):
+            raise IndexError(f"component_variant_indices[{comp_idx}] contains out-of-range "
+                             f"SNP indices for m={int(m)}.")
+        uniq = np.unique(arr)
+        if uniq.size != arr.size:
+            raise ValueError(f"component_variant_indices[{comp_idx}] contains duplicate SNP "
+                             "indices.")
+        normalized.append(uniq)
+    cache_to_source = np.concatenate(normalized)
+    if cache_to_source.size > int(m):
+        raise ValueError(f"component_variant_indices assign {cache_to_source.size} SNPs, "
+                         f"which exceeds source m={int(m)}.")
+    if np.unique(cache_to_source).size != cache_to_source.size:
+        raise ValueError("component_variant_indices must be disjoint across components.")
+    return [int(g.size) for g in normalized], cache_to_source
+
+
 def _build_call_geometry(m: int, call_width: int, component_sizes: Sequence[int]):
     """Call blocks of width <= call_width inside each component (geno_stream.py:469-505)."""
     starts, widths, comps, offsets = [], [], [], [0]
@@ -207,20 +256,14 @@ class GenoBlockStreamer:
         self._has_component_partition = (
             component_block_sizes is not None or component_variant_indices is not None
         )
+        if component_block_sizes is not None and component_variant_indices is not None:
+            raise ValueError(
+                "Provide either component_block_sizes or component_variant_indices, not both.")
         if component_variant_indices is not None:
-            groups = [np.asarray(g, dtype=np.int64).reshape(-1) for g in component_variant_indices]
-            if not groups or any(g.size == 0 for g in groups):
-                raise ValueError("component_variant_indices groups must be non-empty.")
-            cache_to_source = np.concatenate(groups)
-            if np.any(cache_to_source < 0) or np.any(cache_to_source >= self.source_m):
-                raise IndexError("component_variant_indices out of range")
-            sizes = [int(g.size) for g in groups]
+            sizes, cache_to_source = _normalize_component_variant_indices(
+                self.source_m, component_variant_indices)
         elif component_block_sizes is not None:
-            sizes = [int(x) for x in component_block_sizes]
-            if any(s <= 0 for s in sizes) or sum(sizes) > self.source_m:
-                raise ValueError(
-                    f"component_block_sizes must be positive and sum to at most m={self.source_m}."
-                )
+            sizes = _normalize_component_block_sizes(self.source_m, component_block_sizes)
             cache_to_source = np.arange(sum(sizes), dtype=np.int64)
         else:
             sizes = [self.source_m]

@@ -50,8 +50,7 @@ def test_pack_block_equals_oracle(missing_val, w):
 def _fake_streamer(m_source, sizes, groups=None, sample_mask=None, call_width=8):
     """The attributes ``_pack_from_source`` reads, set as the constructor sets them."""
     if groups is not None:
-        cts = np.concatenate([np.asarray(x, np.int64) for x in groups])
-        sizes = [len(x) for x in groups]
+        sizes, cts = gs._normalize_component_variant_indices(m_source, groups)
     else:
         cts = None
     starts, widths, _, _ = gs._build_call_geometry(sum(sizes), call_width, sizes)
@@ -168,3 +167,34 @@ def test_constructor_contract_errors():
         gs.GenoBlockStreamer(src, bed_prefix="x")
     with pytest.raises(ValueError, match="must be provided"):
         gs.GenoBlockStreamer()
+
+
+# geno_stream.py:371-437 of the reference
+def test_component_variant_groups_are_sorted_into_cache_order():
+    sizes, cts = gs._normalize_component_variant_indices(8, [[5, 0, 2], [4, 1, 3]])
+    assert sizes == [3, 3]
+    np.testing.assert_array_equal(cts, [0, 2, 5, 1, 3, 4])
+    sizes, cts = gs._normalize_component_variant_indices(4, [np.array([3, 1]), [0, 2]])
+    np.testing.assert_array_equal(cts, [1, 3, 0, 2])
+
+
+@pytest.mark.parametrize("groups,exc,match", [
+    ([], ValueError, "at least one component"),
+    ([[0, 1], [1, 2]], ValueError, "disjoint"),
+    ([[0, 0, 1]], ValueError, "duplicate"),
+    ([[0, 4]], IndexError, "out-of-range"),
+    ([[-1, 2]], IndexError, "out-of-range"),
+    ([[0, 1], []], ValueError, "empty"),
+])
+def test_component_variant_group_errors(groups, exc, match):
+    with pytest.raises(exc, match=match):
+        gs._normalize_component_variant_indices(4, groups)
+
+
+def test_component_block_sizes_must_cover_every_snp():
+    assert gs._normalize_component_block_sizes(10, None) == [10]
+    assert gs._normalize_component_block_sizes(10, np.array([3, 7])) == [3, 7]
+    for sizes, match in (([], "at least one block"), ([3, 0, 7], "strictly positive"),
+                         ([3, 6], "sum to m=10; got 9"), ([4, 7], "got 11")):
+        with pytest.raises(ValueError, match=match):
+            gs._normalize_component_block_sizes(10, sizes)
