@@ -31,6 +31,8 @@ _EXPORTS: dict[str, str] = {
     "InfinitesimalREMLFitter": ".reml_model",
     "FitConfig": ".reml_model",
     "FitResult": ".reml_model",
+    "EffectEstimates": ".reml_model",
+    "PredictionEstimates": ".reml_model",
     "pcg_solve": ".pcg",
     "fit_reml": ".reml",
     "standardize_response": ".reml",
@@ -38,7 +40,11 @@ _EXPORTS: dict[str, str] = {
     "SmileBlockWeight": ".smile_block_w",
     "SmileBlockWeightedOperator": ".smile_block_w",
     "SmileMultiBlockWeightedOperator": ".smile_block_w",
+    "load_rds_matrix": ".smile_block_w",
+    "load_weight_matrix": ".smile_block_w",
+    "validate_weight_matrix": ".smile_block_w",
     "ServeResult": ".serving",
+    "GWASSummary": ".gwas",
     "run_continuous_gwas": ".gwas",
     "marginal_scan": ".gwas",
     "solve_hinv_columns_batched": ".hinv",

@@ -43,6 +43,27 @@ def test_status_mapping():
     _lib.check(_lib.OK)
 
 
+def test_package_exports_resolve():
+    import coherit_gb300
+
+    for name in coherit_gb300.__all__:
+        assert getattr(coherit_gb300, name) is not None, name
+    # The reference package's exports (__init__.py:6-48) that belong to the
+    # operator, solver, model, SMILE and GWAS layers.
+    hot_path = {
+        "GenoBlockStreamer", "BedBlockStreamer", "SparseGenoBlockStreamer",
+        "DensePackedBlockDescriptor", "Sparse12BlockDescriptor", "ProjectedCorePrecondConf",
+        "ProjectedCoreRuntime", "build_lowrank_basis", "build_projected_core_runtime",
+        "make_precond", "make_projected_core_precond", "projected_core_apply_invsqrt",
+        "projected_core_logdet", "InfinitesimalREMLFitter", "FitConfig", "FitResult",
+        "EffectEstimates", "PredictionEstimates", "pcg_solve", "fit_reml",
+        "compute_projected_hinv_vector", "GWASSummary", "run_continuous_gwas",
+        "SmileBlockWeight", "SmileBlockWeightedOperator", "load_rds_matrix",
+        "load_weight_matrix", "validate_weight_matrix",
+    }
+    assert hot_path <= set(coherit_gb300.__all__)
+
+
 def test_null_handle_is_rejected_without_gpu():
     lib = _lib.load()
     assert lib.coherit_geno_info(None, None, None, None, None, None, None, None) == _lib.E_CLOSED
