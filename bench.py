@@ -223,7 +223,7 @@ def make_fitter(st, wl, precision):
     cfg = FitConfig(slq_samples=wl.slq_samples, slq_m=wl.slq_m, precond_rank=wl.precond_rank,
                     reml_pcg_tol=wl.pcg_tol, minq_iter=wl.minq_iter, max_pcg_iters=1000,
                     slq_mode="raw", precision=precision, sketch_precision="bf16x1",
-                    cache_reml_setup=True, seed=wl.seed)
+                    cache_reml_setup=True, seed=wl.seed, verbose=False)
     return InfinitesimalREMLFitter(cfg, [st])
 
 

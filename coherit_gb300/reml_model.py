@@ -31,7 +31,14 @@ logger = logging.getLogger(__name__)
 
 @dataclasses.dataclass
 class FitConfig:
-    """Subset of the reference FitConfig (reml_model.py:34-83) used by the GPU path."""
+    """The reference FitConfig (reml_model.py:34-83), same fields and defaults,
+    plus the operator precisions of the GPU path.
+
+    The admixture fields are accepted so that configs carry over, but an
+    admixture-weighted fit raises NotImplementedError; ``cpu_threads``,
+    ``ring_depth`` and ``source_build_chunk_width`` size the reference's host
+    build threads and PCIe ring, which the resident operator does not have.
+    """
 
     bed_prefix: str | Sequence[str] = ""
     sources: Sequence | None = None
@@ -41,9 +48,16 @@ class FitConfig:
     rare_sources: Sequence | None = None
     vc_block_sizes: Sequence[int] | None = None
     component_variant_indices: Sequence[Sequence[int]] | None = None
+    admix_weights: np.ndarray | None = None
+    admix_component_names: Sequence[str] | None = None
+    admix_residual_mode: str = "shared"
+    # One (means, inv_sds) pair per dense source or BED prefix, or None.
+    standardization_overrides: Sequence[tuple] | None = None
     sample_mask: np.ndarray | None = None
     call_width: int = 131072
     device: str | None = "auto"
+    keep_host_stats: bool = True
+    cpu_threads: int | None = None
     n_rand_vec: int = 100
     max_pcg_iters: int = 400
     minq_iter: int = 50
@@ -56,7 +70,12 @@ class FitConfig:
     reml_pcg_tol: float = 1e-3
     response_is_standardized: bool = False
     unit_variance_components: bool = False
-    verbose: bool = False
+    # Replicate fits with seeds seed + 9973 r; their mean and Monte-Carlo
+    # standard errors are reported (reml_model.py:1891-1977).
+    n_reml_reps: int = 1
+    ring_depth: int | None = None
+    source_build_chunk_width: int | None = None
+    verbose: bool = True
     gpu_budget_bytes: float | None = None
     capture_reml_diagnostics: bool = False
     cache_reml_setup: bool = False
@@ -82,13 +101,21 @@ class FitConfig:
 
 @dataclasses.dataclass
 class FitResult:
+    """Fields of the reference FitResult (reml_model.py:112-125) plus the wall time."""
+
     var_components: np.ndarray
     history: list
+    rep_var_components: np.ndarray | None = None
+    effects: "EffectEstimates | None" = None
+    final_ai: np.ndarray | None = None
+    final_grad: np.ndarray | None = None
+    final_loglik: float | None = None
+    diagnostics: dict | None = None
     heritability: float | None = None
     genetic_trace_atoms: np.ndarray | None = None
     residual_trace_atoms: np.ndarray | None = None
-    diagnostics: dict | None = None
-    final_loglik: float | None = None
+    monte_carlo_se_var: np.ndarray | None = None
+    monte_carlo_se_h2: float | None = None
     elapsed_sec: float = 0.0
 
 
@@ -177,25 +204,42 @@ class InfinitesimalREMLFitter:
 
     def __init__(self, cfg: FitConfig, streamers: Sequence[GenoBlockStreamer] | None = None):
         self.cfg = cfg
+        if cfg.admix_weights is not None:
+            raise NotImplementedError(
+                "Admixture-weighted GRMs are outside the GPU REML path; fit without admix_weights.")
         rare_prefixes = _prefix_list(cfg.rare_bed_prefix)
         has_rare = cfg.rare_sources is not None or bool(rare_prefixes)
         if streamers is None:
+            smile = bool(cfg.smile_identity or cfg.smile_w_files or cfg.smile_w_file_groups
+                         or cfg.smile_weight_matrices or cfg.smile_weight_matrix_groups)
+            host_kw = dict(keep_host_stats=bool(cfg.keep_host_stats or smile),
+                           build_threads=cfg.cpu_threads, ring_depth=cfg.ring_depth)
             dense_kw = dict(call_width=cfg.call_width, component_block_sizes=cfg.vc_block_sizes,
                             component_variant_indices=cfg.component_variant_indices,
                             sample_mask=cfg.sample_mask, device=cfg.device,
-                            precision=cfg.precision)
+                            precision=cfg.precision,
+                            source_build_chunk_width=cfg.source_build_chunk_width, **host_kw)
+            overrides = (None if cfg.standardization_overrides is None
+                         else list(cfg.standardization_overrides))
             # Sources take precedence over BED prefixes (reml_model.py:506-546).
             if cfg.sources is not None:
-                streamers = [GenoBlockStreamer(src, **dense_kw) for src in cfg.sources]
+                items, what = list(cfg.sources), "dense sources"
+                make = lambda src, ov: GenoBlockStreamer(src, standardization_override=ov,
+                                                         **dense_kw)
             else:
-                streamers = [GenoBlockStreamer(bed_prefix=p, **dense_kw)
-                             for p in _prefix_list(cfg.bed_prefix)]
+                items, what = _prefix_list(cfg.bed_prefix), "dense BED prefixes"
+                make = lambda p, ov: GenoBlockStreamer(bed_prefix=p, standardization_override=ov,
+                                                       **dense_kw)
+            if overrides is not None and len(overrides) != len(items):
+                raise ValueError(f"standardization_overrides must match the number of {what}.")
+            streamers = [make(item, None if overrides is None else overrides[i])
+                         for i, item in enumerate(items)]
             if has_rare:
                 from .sparse_stream import SparseGenoBlockStreamer
 
                 rare_kw = dict(call_width=cfg.call_width, sample_mask=cfg.sample_mask,
                                device=cfg.device, gpu_budget_bytes=cfg.gpu_budget_bytes,
-                               mixed_dense_sparse=bool(streamers))
+                               mixed_dense_sparse=bool(streamers), **host_kw)
                 streamers += [SparseGenoBlockStreamer(src, **rare_kw)
                               for src in (cfg.rare_sources or ())]
                 streamers += [SparseGenoBlockStreamer(bed_prefix=p, **rare_kw)
@@ -429,11 +473,23 @@ class InfinitesimalREMLFitter:
         self._smile_operators = ()
 
     def fit_infinitesimal(self, y, covar=None, h2_init: float = 0.5, var_components_init=None,
+                          estimate_effects: bool = False, mean_information=None,
                           *, slq_probes=None, trace_probes=None, precond: bool = True):
+        """AI-REML fit of the variance components (reml_model.py:1840-2010).
+
+        With ``n_reml_reps`` > 1 the fit is repeated with seeds
+        ``seed + 9973 r`` and the mean is returned with Monte-Carlo standard
+        errors of the components and of h2.  ``estimate_effects`` adds the
+        BLUP and SNP effects at the fitted components.  ``slq_probes`` /
+        ``trace_probes`` fix the probe matrices (then replicates only differ
+        through their seeds' unused streams).
+        """
         t0 = time.time()
         cfg = self.cfg
         if not self.streamers:
             raise RuntimeError("InfinitesimalREMLFitter is closed.")
+        if mean_information is not None:
+            raise NotImplementedError("sparse mean information is outside the GPU REML path")
         if cfg.cache_reml_setup:
             scope = self._setup_scope()
             setup = self._reml_fit_setup
@@ -451,37 +507,61 @@ class InfinitesimalREMLFitter:
         refresh = None
         if conf is not None and G > 1:
             refresh = lambda p: self._build_projected_core_precond(ops, theta_ref=np.asarray(p)[:G])
-        out = fit_reml(
-            y=y, K_mvs=ops.K_mvs, diag_list=ops.diag_list, covar=covar,
-            n_rand_vec=cfg.n_rand_vec, maxiter=cfg.max_pcg_iters, seed=cfg.seed, h2_init=h2_init,
-            param_init=var_components_init, minq_iter=cfg.minq_iter, slq_samples=cfg.slq_samples,
-            slq_m=cfg.slq_m, slq_mode=cfg.slq_mode,
-            slq_workspace_bytes=default_workspace_bytes(cfg.gpu_budget_bytes),
-            precond_conf=conf, slq_precond_conf=conf, precond_refresh_fn=refresh,
-            precond_eps=cfg.pcg_ridge, weighted_hv=ops.weighted_hv, stacked_kv=ops.stacked_kv,
-            optimizer=cfg.smile_optimizer if self._smile_operators else cfg.optimizer,
-            scoring_step_tol=(cfg.smile_scoring_step_tol if self._smile_operators else 1e-4),
-            pcg_tol=cfg.reml_pcg_tol,
-            response_is_standardized=cfg.response_is_standardized,
-            unit_variance_components=cfg.unit_variance_components,
-            max_linesearch_trials=cfg.strict_max_linesearch_trials, return_diagnostics=True,
-            verbose=cfg.verbose,
-            probe_cache=self._reml_probe_cache if cfg.cache_reml_setup else None,
-            device=self.streamers[0].dev,
-            slq_probes=slq_probes, trace_probes=trace_probes,
-        )
-        param, history, diag = out
-        ga = diag.get("genetic_trace_atoms")
-        ra = diag.get("residual_trace_atoms")
-        if cfg.unit_variance_components:
-            gen, res = float(np.sum(param[:G])), float(np.sum(param[G:]))
-        else:
-            gen, res = float(param[:G] @ ga), float(param[G:] @ ra)
-        h2 = gen / max(gen + res, 1e-8)
-        return FitResult(var_components=param, history=history, heritability=h2,
-                         genetic_trace_atoms=ga, residual_trace_atoms=ra,
-                         diagnostics=diag if cfg.capture_reml_diagnostics else None,
-                         final_loglik=float(diag["loglik"]), elapsed_sec=time.time() - t0)
+        reps = []
+        n_reps = max(1, int(cfg.n_reml_reps))
+        for r in range(n_reps):
+            reps.append(fit_reml(
+                y=y, K_mvs=ops.K_mvs, diag_list=ops.diag_list, covar=covar,
+                n_rand_vec=cfg.n_rand_vec, maxiter=cfg.max_pcg_iters, seed=cfg.seed + r * 9973,
+                h2_init=h2_init, param_init=var_components_init, minq_iter=cfg.minq_iter,
+                slq_samples=cfg.slq_samples, slq_m=cfg.slq_m, slq_mode=cfg.slq_mode,
+                slq_workspace_bytes=default_workspace_bytes(cfg.gpu_budget_bytes),
+                precond_conf=conf, slq_precond_conf=conf, precond_refresh_fn=refresh,
+                precond_eps=cfg.pcg_ridge, weighted_hv=ops.weighted_hv, stacked_kv=ops.stacked_kv,
+                optimizer=cfg.smile_optimizer if self._smile_operators else cfg.optimizer,
+                scoring_step_tol=(cfg.smile_scoring_step_tol if self._smile_operators else 1e-4),
+                pcg_tol=cfg.reml_pcg_tol,
+                response_is_standardized=cfg.response_is_standardized,
+                unit_variance_components=cfg.unit_variance_components,
+                max_linesearch_trials=cfg.strict_max_linesearch_trials, return_diagnostics=True,
+                verbose=cfg.verbose,
+                probe_cache=self._reml_probe_cache if cfg.cache_reml_setup else None,
+                device=self.streamers[0].dev,
+                slq_probes=slq_probes, trace_probes=trace_probes,
+            ))
+        param, history, diag = reps[0]
+        ga = np.asarray(diag.get("genetic_trace_atoms"), np.float64)
+        ra = np.asarray(diag.get("residual_trace_atoms"), np.float64)
+
+        def reported_h2(theta):
+            theta = np.asarray(theta, np.float64)
+            if cfg.unit_variance_components:
+                gen, res = np.sum(theta[..., :G], axis=-1), np.sum(theta[..., G:], axis=-1)
+            else:
+                gen, res = theta[..., :G] @ ga, theta[..., G:] @ ra
+            return gen / np.maximum(gen + res, 1e-8)
+
+        rep_vc = se_var = se_h2 = None
+        if n_reps > 1:
+            rep_vc = np.stack([np.asarray(p, np.float64) for p, _, _ in reps])
+            param = rep_vc.mean(axis=0)
+            denom = float(n_reps * (n_reps - 1))
+            se_var = np.sqrt(np.maximum(0.0, np.sum((rep_vc - param) ** 2, axis=0) / denom))
+            h2_reps = reported_h2(rep_vc)
+            se_h2 = float(np.sqrt(max(0.0, float(np.sum((h2_reps - h2_reps.mean()) ** 2)) / denom)))
+            # The AI, gradient and likelihood of one replicate do not describe the mean.
+            diag = None
+        h2 = float(reported_h2(param))
+        effects = (self.estimate_effects(y, var_components=param, covar=covar)
+                   if estimate_effects else None)
+        return FitResult(
+            var_components=param, history=history, rep_var_components=rep_vc, effects=effects,
+            final_ai=None if diag is None else np.asarray(diag["ai"]),
+            final_grad=None if diag is None else np.asarray(diag["grad"]),
+            final_loglik=None if diag is None else float(diag["loglik"]),
+            diagnostics=diag if cfg.capture_reml_diagnostics else None,
+            heritability=h2, genetic_trace_atoms=ga, residual_trace_atoms=ra,
+            monte_carlo_se_var=se_var, monte_carlo_se_h2=se_h2, elapsed_sec=time.time() - t0)
 
 
     # ------------------------------------------------------------ effects

@@ -1,6 +1,8 @@
-"""Fitter assembly on CPU with stand-in streamers (no device work): source
-precedence, dense-before-sparse ordering and the reference's error
-messages (reml_model.py:448-666)."""
+"""The fitter's host logic on CPU with stand-in streamers and a recorded
+fit_reml (no device work): source precedence, dense-before-sparse ordering
+and the reference's error messages (reml_model.py:448-666), config fields
+reaching the streamers, the cached set-up and close() (:1818-1871), and
+replicate fits with their Monte-Carlo errors (:1891-1977)."""
 import pytest
 
 from coherit_gb300 import reml_model
@@ -11,7 +13,7 @@ class _Dense:
     has_sparse_backend = False
 
     def __init__(self, source=None, *, bed_prefix=None, **kw):
-        self.source, self.bed_prefix, self.n = source, bed_prefix, 10
+        self.source, self.bed_prefix, self.n, self.kw = source, bed_prefix, 10, kw
 
 
 class _Rare(_Dense):
@@ -92,7 +94,7 @@ def _recording_fit(monkeypatch):
     def fit(**kwargs):
         captured.append((kwargs["K_mvs"], kwargs["probe_cache"]))
         diag = {"genetic_trace_atoms": np.ones(1), "residual_trace_atoms": np.ones(1),
-                "loglik": 0.0}
+                "loglik": 0.0, "ai": np.eye(2), "grad": np.zeros(2)}
         return np.array([0.3, 0.7]), [], diag
 
     monkeypatch.setattr(reml_model, "fit_reml", fit)
@@ -144,3 +146,77 @@ def test_close_tolerates_streamers_that_fail_to_close():
     fitter = InfinitesimalREMLFitter(FitConfig(precond_rank=0), [_Failing(), good])
     fitter.close()
     assert good.closed == 1 and fitter.streamers == []
+
+
+def test_replicate_fits_report_mean_and_monte_carlo_errors(monkeypatch):
+    """reml_model.py:1891-1977: seeds seed + 9973 r, mean components, Monte-Carlo SE."""
+    import numpy as np
+
+    seeds = []
+    params = {0: [0.2, 0.8], 9973: [0.4, 0.6], 19946: [0.3, 0.9]}
+
+    def fit(**kwargs):
+        seeds.append(kwargs["seed"])
+        diag = {"genetic_trace_atoms": np.array([2.0]), "residual_trace_atoms": np.ones(1),
+                "loglik": -1.0, "ai": np.eye(2), "grad": np.zeros(2)}
+        return np.array(params[kwargs["seed"]]), [{"iter": 1}], diag
+
+    monkeypatch.setattr(reml_model, "fit_reml", fit)
+    cfg = FitConfig(precond_rank=0, n_reml_reps=3, capture_reml_diagnostics=True)
+    res = InfinitesimalREMLFitter(cfg, [_Operator()]).fit_infinitesimal(np.ones(8))
+    assert seeds == [0, 9973, 19946]
+    reps = np.array(list(params.values()))
+    np.testing.assert_allclose(res.rep_var_components, reps)
+    np.testing.assert_allclose(res.var_components, reps.mean(axis=0))
+    se = np.sqrt(np.sum((reps - reps.mean(axis=0)) ** 2, axis=0) / 6)
+    np.testing.assert_allclose(res.monte_carlo_se_var, se)
+    h2 = 2 * reps[:, 0] / (2 * reps[:, 0] + reps[:, 1])
+    assert res.monte_carlo_se_h2 == pytest.approx(np.sqrt(np.sum((h2 - h2.mean()) ** 2) / 6))
+    mean = reps.mean(axis=0)
+    assert res.heritability == pytest.approx(2 * mean[0] / (2 * mean[0] + mean[1]))
+    assert res.diagnostics is None and res.final_ai is None and res.final_loglik is None
+
+
+def test_single_fit_result_and_effects_flag(monkeypatch):
+    import numpy as np
+
+    _recording_fit(monkeypatch)
+    calls = []
+    monkeypatch.setattr(InfinitesimalREMLFitter, "estimate_effects",
+                        lambda self, y, *, var_components, covar=None: calls.append(
+                            (np.asarray(var_components), covar)) or "effects")
+    fitter = InfinitesimalREMLFitter(FitConfig(precond_rank=0), [_Operator()])
+    res = fitter.fit_infinitesimal(np.ones(8))
+    assert res.effects is None and res.rep_var_components is None
+    assert res.monte_carlo_se_h2 is None and res.diagnostics is None
+    np.testing.assert_array_equal(res.final_ai, np.eye(2))
+    assert res.final_loglik == 0.0 and res.heritability == pytest.approx(0.3)
+    res = fitter.fit_infinitesimal(np.ones(8), None, 0.5, None, True)
+    assert res.effects == "effects"
+    np.testing.assert_array_equal(calls[0][0], [0.3, 0.7])
+    with pytest.raises(NotImplementedError):
+        fitter.fit_infinitesimal(np.ones(8), mean_information=object())
+
+
+def test_config_fields_reach_the_streamers(fakes):
+    ov = [(1, 2), (3, 4)]
+    f = InfinitesimalREMLFitter(FitConfig(sources=["a", "b"], standardization_overrides=ov,
+                                          keep_host_stats=False, cpu_threads=3, ring_depth=2,
+                                          source_build_chunk_width=64))
+    assert [s.kw["standardization_override"] for s in f.streamers] == ov
+    kw = f.streamers[0].kw
+    assert kw["keep_host_stats"] is False and kw["build_threads"] == 3
+    assert kw["ring_depth"] == 2 and kw["source_build_chunk_width"] == 64
+    with pytest.raises(ValueError, match="number of dense sources"):
+        InfinitesimalREMLFitter(FitConfig(sources=["a", "b"], standardization_overrides=[ov[0]]))
+    with pytest.raises(ValueError, match="number of dense BED prefixes"):
+        InfinitesimalREMLFitter(FitConfig(bed_prefix=["a"], standardization_overrides=ov))
+    with pytest.raises(NotImplementedError, match="Admixture"):
+        InfinitesimalREMLFitter(FitConfig(sources=["a"], admix_weights=[[1.0]]))
+
+
+def test_config_defaults_follow_the_reference():
+    cfg = FitConfig()
+    assert cfg.verbose is True and cfg.n_reml_reps == 1 and cfg.keep_host_stats is True
+    assert (cfg.slq_samples, cfg.slq_m, cfg.slq_mode) == (4, 8, "projected_core_residual")
+    assert (cfg.precond_rank, cfg.n_rand_vec, cfg.max_pcg_iters) == (500, 100, 400)
