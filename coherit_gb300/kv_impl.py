@@ -244,6 +244,90 @@ def zxb_impl_streamed(b_by_call, true_widths, means_by_call, inv_by_call, *, n: 
             tg.close()
 
 
+def _stack_b_by_call(b_by_call_stack: torch.Tensor, true_widths, calls=None) -> torch.Tensor:
+    """(C, n_calls, width) per-call effect rows -> (sum of true widths, C) in
+    cache SNP order; calls outside ``calls`` (when given) contribute zeros."""
+    tw = np.asarray(torch.as_tensor(true_widths).cpu(), dtype=np.int64).reshape(-1)
+    starts = np.concatenate([[0], np.cumsum(tw)])
+    C = int(b_by_call_stack.shape[0])
+    B = torch.zeros((int(starts[-1]), C), dtype=torch.float32, device=b_by_call_stack.device)
+    for c in (range(tw.size) if calls is None else sorted(set(int(x) for x in calls))):
+        w = int(tw[c])
+        B[starts[c]: starts[c] + w] = b_by_call_stack[:, c, :w].T.to(torch.float32)
+    return B
+
+
+def zxb_impl_same_stream_multi(b_by_call_stack, true_widths, means_by_call, inv_by_call, *,
+                               n: int, n_calls: int, pop_block, missing_val: int = 3):
+    """Several components' predictions over one genotype matrix (kv_impl.py:605-661):
+    the C effect vectors become the C columns of one Z B launch."""
+    bs = torch.as_tensor(b_by_call_stack)
+    if bs.ndim != 3:
+        raise ValueError("zxb_impl_same_stream_multi expects shape "
+                         "(n_components, n_calls, max_unpack_width).")
+    n_components = int(bs.shape[0])
+    if n_components <= 0:
+        raise ValueError("zxb_impl_same_stream_multi requires at least one component.")
+    if int(bs.shape[1]) != int(n_calls):
+        raise ValueError(f"zxb_impl_same_stream_multi call mismatch: expected {int(n_calls)}, "
+                         f"got {int(bs.shape[1])}.")
+    if int(missing_val) != 3:
+        raise ValueError("packed genotypes use code 3 for missing values")
+    dev = bs.device if bs.is_cuda else torch.device("cuda", torch.cuda.current_device())
+    if int(n_calls) == 0:
+        zero = torch.zeros((int(n), n_components), device=dev)
+        return zero.sum(dim=1), tuple(zero[:, i] for i in range(n_components))
+    B = _stack_b_by_call(bs.to(dev), true_widths)
+    st = _owner(pop_block)
+    runner = st if (st is not None and means_by_call is st._means_by_call
+                    and inv_by_call is st._inv_by_call) else None
+    tg = None
+    if runner is None:
+        tg = _TransientGeno(n, n_calls, pop_block, true_widths, means_by_call, inv_by_call, dev)
+        runner = tg
+    try:
+        comps = runner.zxb(B)
+        return comps.sum(dim=1), tuple(comps[:, i] for i in range(n_components))
+    finally:
+        if tg is not None:
+            tg.close()
+
+
+def zxb_impl_multi_streamed(b_by_call_list, streamers: Sequence[GenoBlockStreamer], call_plan, *,
+                            missing_val: int = 3):
+    """Multi-GRM test prediction: sum over streamers of Z_g b_g, over the calls
+    ``call_plan`` lists, and each term (kv_impl.py:664-724)."""
+    if len(b_by_call_list) != len(streamers):
+        raise ValueError(f"zxb_impl_multi_streamed b_by_call_list length mismatch: "
+                         f"expected {len(streamers)}, got {len(b_by_call_list)}.")
+    if not streamers:
+        raise ValueError("zxb_impl_multi_streamed requires at least one streamer.")
+    if int(missing_val) != 3:
+        raise ValueError("packed genotypes use code 3 for missing values")
+    bl = [torch.as_tensor(b) for b in b_by_call_list]
+    for g, (b, st) in enumerate(zip(bl, streamers)):
+        if b.ndim != 2:
+            raise ValueError(f"zxb_impl_multi_streamed expects b_by_call_list[{g}] to be 2D, "
+                             f"got ndim={b.ndim}.")
+        if int(b.shape[0]) != int(st._n_calls):
+            raise ValueError(f"zxb_impl_multi_streamed row mismatch for component {g}: "
+                             f"expected n_calls={int(st._n_calls)}, got {int(b.shape[0])}.")
+    dev = streamers[0].dev
+    n = int(streamers[0].n)
+    comps = [torch.zeros(n, device=dev) for _ in streamers]
+    calls_of = [[] for _ in streamers]
+    for g, c in call_plan:
+        calls_of[int(g)].append(int(c))
+    for g, st in enumerate(streamers):
+        if calls_of[g]:
+            B = _stack_b_by_call(bl[g].to(dev)[None], st._call_true_widths, calls_of[g])
+            comps[g] = st.zxb(B[:, 0])
+    total = torch.zeros(n, device=dev)
+    for c in comps:
+        total = total + c
+    return total, tuple(comps)
+
+
 def kv_impl_multi_streamed_weighted(V, streamers: Sequence[GenoBlockStreamer], call_plan, theta_g,
                                     *, theta_e=None, missing_val: int = 3):
     """sum_g theta_g K_g V (+ theta_e V) over several streamers (kv_impl.py:911-973)."""
@@ -426,6 +510,8 @@ __all__ = [
     "xtv_impl_multi_streamed",
     "xtv_impl_multi_streamed_concat",
     "zxb_impl_streamed",
+    "zxb_impl_same_stream_multi",
+    "zxb_impl_multi_streamed",
     "kv_impl_multi_streamed_weighted",
     "kv_impl_multi_streamed_stacked",
     "kv_impl_partitioned_component",

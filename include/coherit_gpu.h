@@ -228,7 +228,9 @@ int coherit_geno_xtv(coherit_geno_t* h, int32_t slot, int32_t precision, const f
                      void* stream);
 
 /* Z b: out (device, n x C, row stride ldo) = sum_j diff_ij inv_sd_j b[j,:]
- * for b (device, m x C, row stride ldb, cache order) (kv_impl.py:221-265).   */
+ * for b (device, m x C, row stride ldb, cache order) (kv_impl.py:221-265);
+ * replaces zxb_impl_streamed / _same_stream_multi / _multi_streamed
+ * (kv_impl.py:524-724), several effect vectors being the C columns.        */
 int coherit_geno_zxb(coherit_geno_t* h, int32_t slot, int32_t precision, const float* b,
                      int64_t ldb, int32_t C, float* out, int64_t ldo, void* stream);
 

@@ -87,3 +87,43 @@ def test_multi_streamer_weighted_and_stacked(cuda):
     stacked = kv_impl.kv_impl_multi_streamed_stacked(V, [st1, st2], [])
     assert stacked.shape == (2, st1.n, 2)
     assert rel(stacked[0].cpu(), r1 / 0.3) < TOL
+
+
+def _b_rows(st, flat):
+    b = np.zeros((st._n_calls, st._max_unpack_width), np.float32)
+    for c in range(st._n_calls):
+        s0, w = int(st._call_snp_starts[c]), int(st._call_true_widths[c])
+        b[c, :w] = flat[s0:s0 + w]
+    return b
+
+
+def test_zxb_same_stream_multi_and_multi_streamed(cuda):
+    st, codes = _setup()
+    rng = np.random.default_rng(3)
+    flats = rng.normal(size=(3, st.m)).astype(np.float32)
+    stack = np.stack([_b_rows(st, f) for f in flats])
+    blocks = [st._pop_cached(c) for c in range(st._n_calls)]
+    refs = [og.zxb_f64(codes, st._means_host, st._inv_sds_host, f) for f in flats]
+    for pop in (st._pop_cached, lambda c: blocks[c]):
+        total, comps = kv_impl.zxb_impl_same_stream_multi(
+            torch.as_tensor(stack, device=cuda), st._true_widths_dev, st._means_by_call,
+            st._inv_by_call, n=st.n, n_calls=st._n_calls, pop_block=pop)
+        assert len(comps) == 3
+        for g in range(3):
+            assert rel(comps[g].cpu()[:, None], refs[g][:, None]) < TOL
+        assert rel(total.cpu()[:, None], sum(refs)[:, None]) < TOL
+    st2, codes2 = _setup(seed=53)
+    flat2 = rng.normal(size=st2.m).astype(np.float32)
+    plan = [(0, c) for c in range(st._n_calls)] + [(1, c) for c in range(st2._n_calls)]
+    total, comps = kv_impl.zxb_impl_multi_streamed(
+        [torch.as_tensor(stack[0], device=cuda), _b_rows(st2, flat2)], [st, st2], plan)
+    ref2 = og.zxb_f64(codes2, st2._means_host, st2._inv_sds_host, flat2)
+    assert rel(comps[0].cpu()[:, None], refs[0][:, None]) < TOL
+    assert rel(comps[1].cpu()[:, None], ref2[:, None]) < TOL
+    assert rel(total.cpu()[:, None], (refs[0] + ref2)[:, None]) < TOL
+    # Calls left out of the plan contribute nothing.
+    part = kv_impl.zxb_impl_multi_streamed([stack[0]], [st], [(0, 0)])[1][0]
+    only0 = flats[0].copy()
+    only0[int(st._call_true_widths[0]):] = 0.0
+    ref0 = og.zxb_f64(codes, st._means_host, st._inv_sds_host, only0)
+    assert rel(part.cpu()[:, None], ref0[:, None]) < TOL
