@@ -981,16 +981,26 @@ def fit_reml(
         max_rel_dp = 0.0
         use_taylor = False
         freeze = np.zeros(G, dtype=bool)
+        step_norm = 0.0
+        step_sec = eval_sec = 0.0
+        eval_ai_pcg = 0
+        step_stats = FisherSolveStats(free_dim=int(param.size)).to_dict()
         limit = 1 if optimizer == "smile_scoring" else max_linesearch_trials
         while trial_count < limit:
             trial_count += 1
             alpha_used = alpha_try
+            t_step = time.perf_counter()
             step_dir, freeze = _projected_fisher_direction(
                 param, grad, FI, n_genetic=G, genetic_zero_tol=genetic_zero_tol,
                 residual_floor=residual_floor, trial_alpha=alpha_used)
+            step_sec += time.perf_counter() - t_step
+            n_frozen = int(np.sum(freeze))
+            step_stats = (FI.stats.to_dict() if FI.stats is not None else FisherSolveStats(
+                free_dim=int(param.size) - n_frozen, frozen_genetic=n_frozen).to_dict())
             upd, delta = _apply_projected_step(param, step_dir, alpha_used, n_genetic=G,
                                                genetic_zero_tol=genetic_zero_tol,
                                                residual_floor=residual_floor)
+            step_norm = float(np.linalg.norm(delta))
             max_rel_dp = float(np.max(np.abs(delta) / np.maximum(np.abs(param), 1e-8)))
             taylor = None
             trial_taylor = False
@@ -998,21 +1008,25 @@ def fit_reml(
                 taylor = logdet_c + torch.dot(torch.as_tensor(delta[:G], dtype=torch.float64, device=dev), trK) \
                     + torch.dot(torch.as_tensor(delta[G:], dtype=torch.float64, device=dev), trR)
                 trial_taylor = True
+            t_eval = time.time()
             try:
                 res = run_eval(upd, warm_all, warm_ai, True, True, taylor, compute_traces=False,
                                min_loglik=ll if optimizer == "strict" else None)
                 n_evals += 1
             except FloatingPointError as err:
+                eval_sec += time.time() - t_eval
                 if optimizer == "smile_scoring":
                     raise
                 last_err = err
                 ls_trace.append((alpha_used, float("-inf"), False, 0, 0, False))
                 alpha_try *= 0.5
                 continue
+            eval_sec += time.time() - t_eval
             ll_try, grad_try, FI_try, k_try, warm_try, wai_try, _, _, ld_try = res
             dll = ll_try - ll
             evaluated += 1
             ai_it = FI_try.stats.ai_pcg_iters if FI_try is not None and FI_try.stats else 0
+            eval_ai_pcg = int(ai_it)
             ok = dll >= 0.0 or optimizer == "smile_scoring"
             ls_trace.append((alpha_used, dll, ok, k_try, ai_it, trial_taylor))
             if ok:
@@ -1058,12 +1072,16 @@ def fit_reml(
             "rel_dll": float(rel),
             "pcg_iters": int(k_pcg),
             "pcg_tol": pcg_tol,
+            "step_norm": step_norm,
+            "step_sec": step_sec,
             "step_alpha": alpha_used,
             "line_search_trials": trial_count,
             "line_search_trace": [
                 {"alpha": a, "dll": d, "accepted": o, "pcg_iters": p, "ai_pcg_iters": q,
                  "used_taylor": t} for a, d, o, p, q, t in ls_trace],
             "n_freeze": int(np.sum(freeze)),
+            "eval_ai_pcg_iters": eval_ai_pcg,
+            "eval_sec": eval_sec,
             "iter_sec": time.time() - t_it,
             "params": [float(v) for v in (upd if accepted else param)],
             "slq_taylor": use_taylor,
@@ -1071,6 +1089,7 @@ def fit_reml(
             "pcg_precond_refreshed": refreshed,
             "y_mean": y_mean,
             "y_scale": y_scale,
+            **step_stats,
         })
         if full_log:
             logger.info("[REML] iter %d ll %.6e -> %.6e dll=%.3e alpha=%.3g ls=%d pcg=%d",

@@ -8,6 +8,8 @@ genotype operator through a callable.  Here they run on CPU over dense
 operators, so the same known-answer checks that pin the oracle pin them too,
 and each result is compared with the oracle on the same probes.
 """
+import types
+
 import numpy as np
 import pytest
 import torch
@@ -707,3 +709,71 @@ def test_probe_cache_follows_seed_and_operators_not_response(monkeypatch, compon
         assert cache.kvrand_stack is None
     assert cache.signature[0] == changed
     assert calls["lanczos"] == before["lanczos"] + single
+
+
+# -------------------------------------- the AI-REML driver on an analytic objective
+#
+# With the evaluation replaced by a concave quadratic log-likelihood whose AI
+# matrix under-estimates its curvature (so full steps overshoot and the line
+# search halves them) and whose unconstrained optimum has a negative genetic
+# component (so the bound is active), the package's fit_reml and the
+# oracle's fit must take the same steps (reml.py:1465-1880 of the reference).
+
+def _quadratic(G):
+    rng = np.random.default_rng(40 + G)
+    P = G + 1
+    a = rng.normal(size=(P, P))
+    A = a @ a.T / P + 0.5 * np.eye(P)
+    star = np.abs(rng.normal(size=P)) * 0.3 + 0.05
+    star[0] = -0.05                                    # outside theta_g >= 0
+    ll = lambda t: -3.0 - 0.5 * (t - star) @ A @ (t - star)
+    grad = lambda t: -A @ (t - star)
+    return ll, grad, 0.3 * A
+
+
+@pytest.mark.parametrize("G", [1, 2, 4])
+def test_driver_steps_equal_oracle_on_analytic_objective(monkeypatch, G):
+    ll_of, grad_of, ai = _quadratic(G)
+
+    def package_eval(ctx, pvec, warm_all, warm_ai=None, *, min_loglik=None, **kw):
+        t = np.asarray(pvec, np.float64)
+        ll = float(ll_of(t))
+        if min_loglik is not None and not ll >= min_loglik:
+            return (ll, None, None, 3, warm_all, None, None, None, None)
+        FI = reml.AverageInfoMatrix(mat=ai.copy(), stats=reml.FisherSolveStats(ai_pcg_iters=4))
+        return (ll, grad_of(t), FI, 7, warm_all, warm_ai, None, None, None)
+
+    def oracle_eval(ctx, theta, *, warm=None, min_loglik=None, taylor=None):
+        t = np.asarray(theta, np.float64)
+        ll = float(ll_of(t))
+        if min_loglik is not None and not ll >= min_loglik:
+            return dict(ll=ll, grad=None, ai=None, sol=None, logdet=None, pcg=3)
+        return dict(ll=ll, grad=grad_of(t), ai=ai.copy(), sol=None, logdet=None, pcg=7)
+
+    monkeypatch.setattr(reml, "_eval_once", package_eval)
+    monkeypatch.setattr(oreml, "evaluate", oracle_eval)
+    K_mvs, _ = _kernels(min(G, 3)) if G <= 3 else _kernels(3)
+    K_mvs = tuple(K_mvs[g % len(K_mvs)] for g in range(G))
+    atoms = np.linspace(0.8, 1.2, G)
+    diags = [torch.tensor(float(a)) for a in atoms]
+    y = np.random.default_rng(1).normal(size=24).astype(np.float32)
+    param, history, diag = reml.fit_reml(y, K_mvs, diags, None, n_rand_vec=3, maxiter=50,
+                                         minq_iter=30, slq_samples=3, slq_m=4, verbose=False,
+                                         device="cpu", return_diagnostics=True)
+    # The reference averages the kernel diagonals in FP32 (reml.py:187-212).
+    ctx = types.SimpleNamespace(G=G, E=1, R=None,
+                                diag_atoms=atoms.astype(np.float32).astype(np.float64))
+    oparam, ohist, _ = oreml.fit(ctx, minq_iter=30)
+    assert len(history) == len(ohist)
+    for h, o in zip(history, ohist):
+        assert h["accepted"] == o["accepted"]
+        np.testing.assert_allclose(h["params"], o["params"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(param, oparam, rtol=1e-12, atol=1e-14)
+    assert any(h["step_alpha"] < 1.0 for h in history)      # the line search halved
+    assert param[0] == 0.0                                    # the bound is active
+    last = history[-1]
+    assert last["stop_reason"] in ("rel_dll", "ll_down", "max_iter")
+    for key in ("step_norm", "step_sec", "eval_ai_pcg_iters", "eval_sec", "free_dim",
+                "frozen_genetic", "ai_pcg_iters", "ws_trace"):
+        assert key in last, key
+    assert diag["loglik"] == pytest.approx(ll_of(param))
