@@ -7,6 +7,10 @@ on whatever device its inputs live on; on the device they only see the
 genotype operator through a callable.  Here they run on CPU over dense
 operators, so the same known-answer checks that pin the oracle pin them too,
 and each result is compared with the oracle on the same probes.
+
+fit_reml itself runs here up to its first evaluation (set-up, probe caches,
+tolerance clamp), and to completion with the evaluation replaced by an
+analytic objective, where its steps must equal the oracle's fit.
 """
 import types
 
@@ -719,9 +723,9 @@ def test_probe_cache_follows_seed_and_operators_not_response(monkeypatch, compon
 # component (so the bound is active), the package's fit_reml and the
 # oracle's fit must take the same steps (reml.py:1465-1880 of the reference).
 
-def _quadratic(G):
-    rng = np.random.default_rng(40 + G)
-    P = G + 1
+def _quadratic(G, E=1):
+    rng = np.random.default_rng(40 + G + 10 * E)
+    P = G + E
     a = rng.normal(size=(P, P))
     A = a @ a.T / P + 0.5 * np.eye(P)
     star = np.abs(rng.normal(size=P)) * 0.3 + 0.05
@@ -731,9 +735,9 @@ def _quadratic(G):
     return ll, grad, 0.3 * A
 
 
-@pytest.mark.parametrize("G", [1, 2, 4])
-def test_driver_steps_equal_oracle_on_analytic_objective(monkeypatch, G):
-    ll_of, grad_of, ai = _quadratic(G)
+@pytest.mark.parametrize("G,E", [(1, 1), (2, 1), (4, 1), (1, 2), (3, 2)])
+def test_driver_steps_equal_oracle_on_analytic_objective(monkeypatch, G, E):
+    ll_of, grad_of, ai = _quadratic(G, E)
 
     def package_eval(ctx, pvec, warm_all, warm_ai=None, *, min_loglik=None, **kw):
         t = np.asarray(pvec, np.float64)
@@ -757,11 +761,14 @@ def test_driver_steps_equal_oracle_on_analytic_objective(monkeypatch, G):
     atoms = np.linspace(0.8, 1.2, G)
     diags = [torch.tensor(float(a)) for a in atoms]
     y = np.random.default_rng(1).normal(size=24).astype(np.float32)
-    param, history, diag = reml.fit_reml(y, K_mvs, diags, None, n_rand_vec=3, maxiter=50,
-                                         minq_iter=30, slq_samples=3, slq_m=4, verbose=False,
-                                         device="cpu", return_diagnostics=True)
+    # Residual diagonals exact in FP32, so both sides average the same values.
+    R = None if E == 1 else np.stack([np.ones(24), 0.5 + np.arange(24) / 16.0])
+    param, history, diag = reml.fit_reml(
+        y, K_mvs, diags, None, n_rand_vec=3, maxiter=50, minq_iter=30, slq_samples=3, slq_m=4,
+        verbose=False, device="cpu", return_diagnostics=True,
+        residual_diag_list=None if R is None else [torch.as_tensor(r) for r in R])
     # The reference averages the kernel diagonals in FP32 (reml.py:187-212).
-    ctx = types.SimpleNamespace(G=G, E=1, R=None,
+    ctx = types.SimpleNamespace(G=G, E=E, R=R,
                                 diag_atoms=atoms.astype(np.float32).astype(np.float64))
     oparam, ohist, _ = oreml.fit(ctx, minq_iter=30)
     assert len(history) == len(ohist)
