@@ -99,3 +99,102 @@ def phenotype(seed: int, n: int, m: int, *, h2: float, n_causal: int, missing_q2
     y = g + rng.normal(scale=np.sqrt(ve), size=n)
     X = np.column_stack([np.ones(n), rng.normal(size=(n, n_covar))]) if n_covar >= 0 else None
     return y.astype(np.float32), X.astype(np.float32), causal, beta
+
+
+# ------------------------------------------------- block-LD genotypes (8-GRM workload)
+
+def ld_block_genotypes(seed: int, n: int, m: int, *, block: int = 200, rho_range=(0.0, 0.9),
+                       maf_range=(0.05, 0.5)):
+    """Genotypes with linkage disequilibrium inside blocks of ``block`` SNPs.
+
+    Each block draws rho ~ U(rho_range); every sample carries two latent
+    haplotype chains h_0 ~ N(0, 1), h_j = rho h_{j-1} + sqrt(1 - rho^2) e_j,
+    and allele j is 1[h_j < Phi^-1(p_j)] with p_j ~ U(maf_range).  Each allele
+    is Bernoulli(p_j), so genotypes (two alleles) are in Hardy-Weinberg
+    equilibrium, and neighbouring SNPs are correlated through rho; blocks are
+    independent.  Host-side, for test-sized matrices.
+
+    Returns (codes (n, m) uint8 in {0, 1, 2}, maf (m,), rho per block).
+    """
+    from scipy.stats import norm
+
+    if block < 1:
+        raise ValueError("block must be positive")
+    lo, hi = (float(x) for x in rho_range)
+    if not 0.0 <= lo <= hi < 1.0:
+        raise ValueError("rho_range must satisfy 0 <= lo <= hi < 1")
+    rng = np.random.default_rng(seed)
+    maf = rng.uniform(maf_range[0], maf_range[1], size=m)
+    thr = norm.ppf(maf)
+    n_blocks = (m + block - 1) // block
+    rho = rng.uniform(lo, hi, size=n_blocks)
+    codes = np.zeros((n, m), dtype=np.uint8)
+    for b in range(n_blocks):
+        j0, j1 = b * block, min((b + 1) * block, m)
+        r, s = rho[b], np.sqrt(1.0 - rho[b] ** 2)
+        h = rng.normal(size=(2, n))
+        for j in range(j0, j1):
+            if j > j0:
+                h = r * h + s * rng.normal(size=(2, n))
+            codes[:, j] = (h[0] < thr[j]).astype(np.uint8) + (h[1] < thr[j]).astype(np.uint8)
+    return codes, maf, rho
+
+
+def block_ld_scores(codes: np.ndarray, block: int = 200) -> np.ndarray:
+    """LD score of each SNP: the sum of its r^2 with the SNPs of its block
+    (itself included); monomorphic SNPs score 0."""
+    g = np.asarray(codes, np.float64)
+    n, m = g.shape
+    out = np.zeros(m)
+    for j0 in range(0, m, block):
+        z = g[:, j0:j0 + block]
+        z = z - z.mean(axis=0)
+        sd = z.std(axis=0)
+        z = np.where(sd > 0, z / np.where(sd > 0, sd, 1.0), 0.0)
+        r = z.T @ z / n
+        out[j0:j0 + z.shape[1]] = np.sum(r * r, axis=1)
+    return out
+
+
+def maf_ld_partition(maf, ld_scores, n_maf_bins: int = 4) -> list:
+    """Component groups: MAF quantile bins, each split at its median LD score
+    into a lower and an upper half.  Returns 2 * n_maf_bins sorted SNP index
+    arrays ordered (bin 0 low LD, bin 0 high LD, bin 1 low LD, ...); together
+    they hold every SNP once."""
+    maf = np.asarray(maf, np.float64)
+    ld = np.asarray(ld_scores, np.float64)
+    order = np.argsort(maf, kind="stable")
+    groups = []
+    for part in np.array_split(order, n_maf_bins):
+        by_ld = part[np.argsort(ld[part], kind="stable")]
+        half = by_ld.size // 2
+        groups += [np.sort(by_ld[:half]), np.sort(by_ld[half:])]
+    return groups
+
+
+def dirichlet_h2(seed: int, n_components: int, total: float = 0.4) -> np.ndarray:
+    """Per-component heritabilities ~ Dirichlet(1, ..., 1) scaled to ``total``."""
+    return total * np.random.default_rng(seed).dirichlet(np.ones(n_components))
+
+
+def partitioned_phenotype(codes: np.ndarray, groups, h2s, *, seed: int, n_causal_per: int,
+                          n_covar: int = 0):
+    """Phenotype whose component g explains h2s[g] of the variance through
+    ``n_causal_per`` standardised causal SNPs drawn from groups[g]; the rest is
+    N(0, 1 - sum h2s) noise.  Returns (y float32, X float32 = [1, N(0,1) covariates])."""
+    rng = np.random.default_rng(seed)
+    g = np.asarray(codes, np.float64)
+    n = g.shape[0]
+    y = np.zeros(n)
+    for grp, h2 in zip(groups, h2s):
+        idx = rng.choice(np.asarray(grp), size=min(n_causal_per, len(grp)), replace=False)
+        z = g[:, idx] - g[:, idx].mean(axis=0)
+        sd = z.std(axis=0)
+        z = np.where(sd > 0, z / np.where(sd > 0, sd, 1.0), 0.0)
+        comp = z @ rng.normal(size=idx.size)
+        v = np.var(comp)
+        if v > 0 and h2 > 0:
+            y += comp * np.sqrt(h2 / v)
+    y += rng.normal(scale=np.sqrt(max(1e-6, 1.0 - float(np.sum(h2s)))), size=n)
+    X = np.column_stack([np.ones(n), rng.normal(size=(n, n_covar))])
+    return y.astype(np.float32), X.astype(np.float32)

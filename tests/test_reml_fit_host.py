@@ -111,3 +111,21 @@ def test_two_residual_components_fit_matches_oracle():
                                                           slq_m=12)
     _check(diag, h2, cur, h2_ref, param, po)
     assert param.size == 3
+
+
+def test_eight_grm_maf_ld_partition_fit_matches_oracle():
+    """The 8-GRM workload's form at a small size: LD-block genotypes, 4 MAF
+    bins x 2 LD-score halves, per-component h2 ~ Dirichlet(1) x 0.4."""
+    from coherit_gb300 import synth
+
+    n, m = 300, 1600
+    codes, maf, _ = synth.ld_block_genotypes(21, n, m, block=200)
+    groups = synth.maf_ld_partition(maf, synth.block_ld_scores(codes, block=200))
+    h2s = synth.dirichlet_h2(21, 8, total=0.4)
+    y, X = synth.partitioned_phenotype(codes, groups, h2s, seed=21, n_causal_per=25, n_covar=1)
+    mean, inv, _ = og.stats(codes)
+    Z = og.diff_f64(codes, mean) * inv.astype(np.float64)[None, :]
+    Ks = [Z[:, g] @ Z[:, g].T / float(np.count_nonzero(inv[g] > 0)) for g in groups]
+    param, diag, h2, po, cur, h2_ref, hist, ho = _fit_both(Ks, X, y, slq_m=12)
+    _check(diag, h2, cur, h2_ref, param, po)
+    assert param.size == 9 and len(hist) >= 2
