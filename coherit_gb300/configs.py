@@ -6,8 +6,10 @@ c2  single-GRM REML at scale, n=50000 x m=500000, h2=0.3 from 5000 causal,
     10 N(0,1) covariates (+ intercept), 64 Rademacher probes (a 65-column
     block with the phenotype), BF16 genotype tiles, FP32 PCG, FP64
     Lanczos/AI.
-c3  8-component REML, n=100000 x m=1000000 (4 MAF bins x 2 halves), 128
-    probes.
+c3  8-component REML, n=100000 x m=1000000 (4 MAF bins x 2 LD-score halves),
+    128 probes, per-component h2 ~ Dirichlet(1) x 0.4; genotypes with block
+    LD (synth.ld_block_genotypes / maf_ld_partition / dirichlet_h2, host
+    scale).
 c4  serving stream: 512 fits over one resident n=200000 x m=600000 matrix,
     h2 ~ U(0.05, 0.8), sample subsets ~ LogUniform(1e4, 2e5), 1-20 covariates,
     Poisson arrivals.
