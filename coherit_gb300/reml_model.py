@@ -501,8 +501,10 @@ class InfinitesimalREMLFitter:
         else:
             ops = self._assemble_reml_operators()
         G = len(ops.K_mvs)
-        if precond and cfg.precond_rank > 0 and (self.precond_conf is None or not cfg.cache_reml_setup):
-            self._build_projected_core_precond(ops, var_components_init)
+        if precond:
+            # Built once per fitter, at the first fit (reml_model.py:1392-1407);
+            # multi-GRM fits refresh it as theta moves.
+            self._ensure_projected_core_precond_ready(ops, var_components_init)
         conf = self.precond_conf if precond and cfg.precond_rank > 0 else None
         refresh = None
         if conf is not None and G > 1:

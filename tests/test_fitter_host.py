@@ -220,3 +220,36 @@ def test_config_defaults_follow_the_reference():
     assert cfg.verbose is True and cfg.n_reml_reps == 1 and cfg.keep_host_stats is True
     assert (cfg.slq_samples, cfg.slq_m, cfg.slq_mode) == (4, 8, "projected_core_residual")
     assert (cfg.precond_rank, cfg.n_rand_vec, cfg.max_pcg_iters) == (500, 100, 400)
+
+
+def test_preconditioner_is_built_once_per_fitter(monkeypatch):
+    """reml_model.py:1392-1407: the projected-core preconditioner is built at
+    the first fit and reused by later fits of the same fitter."""
+    import numpy as np
+
+    passed = []
+
+    def fit(**kwargs):
+        passed.append(kwargs["precond_conf"])
+        diag = {"genetic_trace_atoms": np.ones(1), "residual_trace_atoms": np.ones(1),
+                "loglik": 0.0, "ai": np.eye(2), "grad": np.zeros(2)}
+        return np.array([0.3, 0.7]), [], diag
+
+    built = []
+
+    def build(self, ops, var_components_init=None, theta_ref=None):
+        self.precond_conf = object()
+        built.append(var_components_init)
+        return self.precond_conf
+
+    monkeypatch.setattr(reml_model, "fit_reml", fit)
+    monkeypatch.setattr(InfinitesimalREMLFitter, "_build_projected_core_precond", build)
+    fitter = InfinitesimalREMLFitter(FitConfig(precond_rank=8), [_Operator()])
+    fitter.fit_infinitesimal(np.ones(8), var_components_init=[0.5, 0.5])
+    fitter.fit_infinitesimal(np.arange(8.0))
+    assert len(built) == 1 and built[0] == [0.5, 0.5]
+    assert passed[0] is passed[1] is fitter.precond_conf
+    fitter.fit_infinitesimal(np.ones(8), precond=False)
+    assert passed[2] is None
+    fitter.close()
+    assert fitter.precond_conf is None
