@@ -7,6 +7,7 @@ solve, runs the fitter's own assembly: GLS fixed effects, BLUP random
 effects per component, SNP effects, the projected-core preconditioner
 build, and prediction on a test streamer that takes the training
 standardisation.  Results must equal the dense FP64 formulas within 1e-5.
+The same stand-in runs fit_infinitesimal end to end against the oracle's fit.
 """
 import numpy as np
 import pytest
@@ -161,3 +162,43 @@ def test_effects_and_prediction_match_dense(monkeypatch, comps, precond_rank):
         fitter.predict(eff, test_fitter=test, test_covar=None)
     with pytest.raises(ValueError, match="length mismatch"):
         fitter.estimate_effects(y[:n_tr], var_components=theta[:-1], covar=X[:n_tr])
+
+
+@pytest.mark.parametrize("comps", [None, [300, 500]])
+def test_fit_infinitesimal_matches_oracle_fit(monkeypatch, comps):
+    """The model API end to end (operator bundle, projected-core
+    preconditioner and its refresh, SLQ, Fisher steps), PCG replaced by an
+    exact solve: |dh2| < 1e-3 against the oracle's fit."""
+    from coherit_gb300 import reml
+    from oracle import slq as oslq
+
+    monkeypatch.setattr(reml, "pcg_solve", _exact_solve)
+    n, m = 200, 800
+    codes = og.synth_codes(81, n, np.arange(m))
+    st = _HostGeno(codes, comps)
+    rng = np.random.default_rng(8)
+    beta = np.zeros(m)
+    beta[rng.choice(m, 50, replace=False)] = rng.normal(size=50)
+    g = st.Z @ beta
+    X = np.column_stack([np.ones(n), rng.normal(size=n)])
+    y = (g / g.std() * np.sqrt(0.5) + rng.normal(scale=np.sqrt(0.5), size=n)).astype(np.float32)
+    probes = rng.choice([-1.0, 1.0], size=(n, 16))
+    cfg = FitConfig(slq_samples=16, slq_m=16, precond_rank=12, reml_pcg_tol=1e-5, minq_iter=15,
+                    slq_mode="raw", vc_block_sizes=comps, verbose=False)
+    res = InfinitesimalREMLFitter(cfg, [st]).fit_infinitesimal(
+        y, X, slq_probes=torch.as_tensor(probes, dtype=torch.float32))
+    G = 1 if comps is None else 2
+    Zs = [st._Zg(k) for k in range(G)]
+    Ks = [Z @ Z.T / float(e) for Z, e in zip(Zs, st._component_eff_m_host)]
+    atoms = (np.asarray([st._mean_diag_atom_host]) if G == 1
+             else st._component_mean_diag_atoms_host.astype(np.float64))
+    yo, _, _ = oreml.standardize(y)
+    kw = (dict(affine_cache=oslq.affine_cache(lambda v: Ks[0] @ v, n, probes, 16)) if G == 1
+          else dict(slq_probes=probes, slq_m=16))
+    ctx = oreml.Context(yo, [(lambda v, K=K: K @ v) for K in Ks], X, diag_atoms=atoms,
+                        pcg_tol=1e-6, maxiter=1000, **kw)
+    po, _, cur = oreml.fit(ctx, minq_iter=15)
+    h2_ref = oreml.heritability(po, G, atoms)
+    assert abs(res.heritability - h2_ref) < 1e-3, (res.heritability, h2_ref)
+    assert abs(res.final_loglik - cur["ll"]) <= 1e-4 * abs(cur["ll"])
+    assert res.final_ai.shape == (G + 1, G + 1) and len(res.history) >= 1
