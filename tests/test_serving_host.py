@@ -6,7 +6,10 @@ an application must come back equal to that function however its columns
 were split across launches.  Covered: launches fill to the column limit,
 an application wider than the rest of a launch continues in the next one,
 every application completes exactly once, a failing launch fails exactly the
-applications it carried, and an empty block returns at once."""
+applications it carried, and an empty block returns at once.  The server's
+admission rule (active limit, statistics slots for subset requests, HBM
+budget) and its request validation are checked on a server object built
+without its device set-up."""
 import threading
 import types
 
@@ -149,3 +152,65 @@ def test_split_application_whose_first_launch_fails_does_not_hang():
     assert isinstance(errs[0], RuntimeError)
     assert calls[0] == [(0, 8)]
     assert b.pending == []
+
+
+def _bare_server(n=100, max_active=2, budget=1e6):
+    """A REMLServer without its device set-up or admission thread."""
+    srv = serving.REMLServer.__new__(serving.REMLServer)
+    srv.st = types.SimpleNamespace(n=n, dev=torch.device("cpu"))
+    srv.max_active = max_active
+    srv.budget = float(budget)
+    srv._free_slots = serving.deque(range(1, max_active + 1))
+    srv._active = 0
+    srv._bytes_active = 0.0
+    srv._closed = False
+    srv._cv = threading.Condition()
+    srv._waiting = serving.deque()
+    srv._next_id = 0
+    srv.fit_kwargs = dict(n_rand_vec=30, slq_samples=30, slq_m=30)
+    return srv
+
+
+def test_admission_respects_slots_budget_and_active_limit():
+    srv = _bare_server(max_active=2, budget=1000.0)
+    full = types.SimpleNamespace(mask=None, bytes_estimate=600.0)
+    subset = types.SimpleNamespace(mask=np.ones(3, bool), bytes_estimate=600.0)
+    assert srv._can_admit(full)
+    srv._active, srv._bytes_active = 1, 600.0
+    assert not srv._can_admit(full)             # over the HBM budget
+    srv._bytes_active = 300.0
+    assert srv._can_admit(full)
+    srv._active = 0
+    srv._bytes_active = 0.0
+    assert srv._can_admit(types.SimpleNamespace(mask=None, bytes_estimate=5000.0))  # alone: always
+    srv._free_slots.clear()
+    assert not srv._can_admit(subset)           # no statistics slot for a subset request
+    assert srv._can_admit(full)
+    srv._active = 2
+    assert not srv._can_admit(full)             # max_active
+
+
+def test_submit_validates_and_estimates_solver_memory():
+    srv = _bare_server(n=100)
+    fut = srv.submit(np.zeros(100), np.ones((100, 3)))
+    req = srv._waiting[-1]
+    assert req.n_sub == 100 and req.covar.shape == (100, 3) and not fut.done()
+    width = 3 + 1 + 30 + 30
+    assert req.bytes_estimate == 4 * 100 * (8 * width + 30 * 30)
+    mask = np.zeros(100, bool)
+    mask[:40] = True
+    srv.submit(np.zeros(40), None, mask, n_rand_vec=10)
+    req = srv._waiting[-1]
+    assert req.n_sub == 40 and req.fit_kwargs["n_rand_vec"] == 10
+    assert [r.rid for r in srv._waiting] == [0, 1]
+    with pytest.raises(ValueError, match="entries, the matrix has"):
+        srv.submit(np.zeros(40), None, np.ones(99, bool))
+    with pytest.raises(ValueError, match="selects no samples"):
+        srv.submit(np.zeros(0), None, np.zeros(100, bool))
+    with pytest.raises(ValueError, match="phenotype has 41"):
+        srv.submit(np.zeros(41), None, mask)
+    with pytest.raises(ValueError, match="one row per selected sample"):
+        srv.submit(np.zeros(40), np.ones((39, 2)), mask)
+    srv._closed = True
+    with pytest.raises(RuntimeError, match="closed"):
+        srv.submit(np.zeros(100))
