@@ -233,8 +233,13 @@ class GenoBlockStreamer:
         if self._sample_mask is not None and self._sample_mask.shape != (self._source_n,):
             raise ValueError(
                 "sample_mask is incompatible with the supplied source: "
-                f"mask length={self._sample_mask.size}, source.n={self._source_n}."
+                f"mask length={self._sample_mask.size}, "
+                f"selected={int(np.count_nonzero(self._sample_mask))}, source.n={self._source_n}."
             )
+        # The reference sizes its host ring with ring_depth (geno_stream.py:171-173);
+        # the resident operator has no ring, but the argument is checked alike.
+        if ring_depth is not None and int(ring_depth) <= 0:
+            raise ValueError("ring depth must be positive when provided.")
         self.n = int(self._sample_mask.sum()) if self._sample_mask is not None else self._source_n
         if self.n <= 0:
             raise ValueError("Genotype source must contain at least one selected sample.")
@@ -648,9 +653,11 @@ class GenoBlockStreamer:
     def standardized_columns(self, snp_indices) -> torch.Tensor:
         """Device FP32 (n, len(snp_indices)) standardised genotype columns
         (cache SNP order; missing -> 0), computed from the resident matrix."""
-        idx = np.asarray(snp_indices, dtype=np.int64).reshape(-1)
+        idx = np.asarray(snp_indices, dtype=np.int64)
+        if idx.ndim != 1:
+            raise ValueError("snp_indices must be 1D.")
         if idx.size and (idx.min() < 0 or idx.max() >= self.m):
-            raise IndexError(f"SNP indices must lie in [0, {self.m}).")
+            raise IndexError("snp_indices out of range.")
         out = torch.empty((self.n, idx.size), dtype=torch.float32, device=self.dev)
         if idx.size == 0:
             return out

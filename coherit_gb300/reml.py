@@ -833,8 +833,12 @@ def fit_reml(
         raise ValueError("log_detail must be 'compact' or 'full'.")
     if optimizer not in {"strict", "smile_scoring"}:
         raise ValueError("optimizer must be 'strict' or 'smile_scoring'.")
-    if scoring_step_tol < 0.0 or rel_dll_tol < 0.0 or taylor_threshold < 0.0:
-        raise ValueError("tolerances must be >= 0.")
+    if scoring_step_tol < 0.0:
+        raise ValueError("scoring_step_tol must be >= 0.")
+    if rel_dll_tol < 0.0:
+        raise ValueError("rel_dll_tol must be >= 0.")
+    if taylor_threshold < 0.0:
+        raise ValueError("taylor_threshold must be >= 0.")
     if pcg_tol <= 0.0:
         raise ValueError("pcg_tol must be > 0.")
     if mean_information is not None:
@@ -923,8 +927,12 @@ def fit_reml(
         tgp = torch.as_tensor(param[:G], dtype=torch.float32, device=dev)
         tep = torch.as_tensor(param[G:], dtype=torch.float32, device=dev)
         ref_diag = scalar_diag_from_precond_conf(slq_precond_conf, tgp, tep)
+        if ref_diag is None:
+            raise ValueError("projected_core_residual SLQ requires a scalar-identity reference.")
         slq_ref = build_projected_core_runtime(slq_precond_conf, tgp, ref_diag, eps=precond_eps,
                                                need_invsqrt=True)
+        if slq_ref is None:
+            raise RuntimeError("Failed to build the fixed projected-core SLQ reference.")
 
     parts = []
     x_cols = 0

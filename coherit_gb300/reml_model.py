@@ -145,8 +145,9 @@ class PredictionEstimates:
 
 
 def _validate_dense_prediction_streamers(train, test) -> None:
-    """Train/test streamers must share the SNP set and call geometry
-    (reml_model.py:223-272)."""
+    """Train/test streamers must share the SNP set, call geometry, partition
+    mode, cache-to-source SNP order and component layout (reml_model.py:223-272;
+    the variant-metadata comparison against .bim/.pvar files is not made)."""
     if len(train) != len(test):
         raise ValueError(
             f"Prediction component count mismatch: expected {len(train)}, got {len(test)}.")
@@ -157,12 +158,25 @@ def _validate_dense_prediction_streamers(train, test) -> None:
         if int(a._n_calls) != int(b._n_calls):
             raise ValueError(f"Prediction call geometry mismatch for component {idx}: "
                              f"expected {int(a._n_calls)} calls, got {int(b._n_calls)}.")
-        if not np.array_equal(a._call_snp_starts, b._call_snp_starts):
+        if not np.array_equal(np.asarray(a._call_snp_starts, np.int64),
+                              np.asarray(b._call_snp_starts, np.int64)):
             raise ValueError(f"Prediction SNP call starts mismatch for component {idx}.")
-        if not np.array_equal(a._call_true_widths, b._call_true_widths):
-            raise ValueError(f"Prediction SNP call widths mismatch for component {idx}.")
-        if a.n_components != b.n_components:
-            raise ValueError(f"Prediction component partition mismatch for component {idx}.")
+        if not np.array_equal(np.asarray(a._call_true_widths, np.int32),
+                              np.asarray(b._call_true_widths, np.int32)):
+            raise ValueError(f"Prediction call widths mismatch for component {idx}.")
+        partitioned = bool(getattr(a, "has_component_partition", False))
+        if partitioned != bool(getattr(b, "has_component_partition", False)):
+            raise ValueError(f"Prediction partitioning mode mismatch for component {idx}.")
+        ca = getattr(a, "_cache_to_source_variant_indices", None)
+        cb = getattr(b, "_cache_to_source_variant_indices", None)
+        if ca is not None or cb is not None:
+            if ca is None or cb is None:
+                raise ValueError(f"Prediction variant-order mapping mismatch for component {idx}.")
+            if not np.array_equal(np.asarray(ca, np.int64), np.asarray(cb, np.int64)):
+                raise ValueError(f"Prediction source-variant order mismatch for component {idx}.")
+        if partitioned and not np.array_equal(np.asarray(a._component_snp_offsets, np.int32),
+                                              np.asarray(b._component_snp_offsets, np.int32)):
+            raise ValueError("Prediction component block layout mismatch.")
 
 
 def _solve_small_spd(A: torch.Tensor, b: torch.Tensor, *, base_jitter=1e-6, max_tries=8):
@@ -182,7 +196,7 @@ def _solve_small_spd(A: torch.Tensor, b: torch.Tensor, *, base_jitter=1e-6, max_
             continue
         x = np.linalg.solve(L.T, np.linalg.solve(L, b_np))
         return torch.as_tensor(x, dtype=torch.float32, device=A.device)
-    raise FloatingPointError("GLS system is not positive definite.")
+    raise FloatingPointError("Failed to stabilize GLS normal equations with jitter escalation.")
 
 
 def _prefix_list(prefix) -> list:
@@ -209,6 +223,13 @@ class InfinitesimalREMLFitter:
                 "Admixture-weighted GRMs are outside the GPU REML path; fit without admix_weights.")
         rare_prefixes = _prefix_list(cfg.rare_bed_prefix)
         has_rare = cfg.rare_sources is not None or bool(rare_prefixes)
+        # One dense source split into components (reml_model.py:464-512).
+        partitioned = cfg.vc_block_sizes is not None or cfg.component_variant_indices is not None
+        if cfg.vc_block_sizes is not None and cfg.component_variant_indices is not None:
+            raise ValueError("Use either vc_block_sizes or component_variant_indices, not both.")
+        if partitioned and has_rare:
+            raise ValueError("single-source component partitioning is currently supported only "
+                             "for dense-only fits.")
         if streamers is None:
             smile = bool(cfg.smile_identity or cfg.smile_w_files or cfg.smile_w_file_groups
                          or cfg.smile_weight_matrices or cfg.smile_weight_matrix_groups)
@@ -223,13 +244,15 @@ class InfinitesimalREMLFitter:
                          else list(cfg.standardization_overrides))
             # Sources take precedence over BED prefixes (reml_model.py:506-546).
             if cfg.sources is not None:
-                items, what = list(cfg.sources), "dense sources"
+                items, what, one = list(cfg.sources), "dense sources", "dense source"
                 make = lambda src, ov: GenoBlockStreamer(src, standardization_override=ov,
                                                          **dense_kw)
             else:
-                items, what = _prefix_list(cfg.bed_prefix), "dense BED prefixes"
+                items, what, one = _prefix_list(cfg.bed_prefix), "dense BED prefixes", "dense BED prefix"
                 make = lambda p, ov: GenoBlockStreamer(bed_prefix=p, standardization_override=ov,
                                                        **dense_kw)
+            if partitioned and len(items) != 1:
+                raise ValueError(f"single-source component partitioning requires exactly one {one}.")
             if overrides is not None and len(overrides) != len(items):
                 raise ValueError(f"standardization_overrides must match the number of {what}.")
             streamers = [make(item, None if overrides is None else overrides[i])
@@ -291,7 +314,7 @@ class InfinitesimalREMLFitter:
         if self._has_sparse:
             raise ValueError("SMILE block-W mode is currently supported only for dense-only fits.")
         if len(self.streamers) != 1:
-            raise ValueError("SMILE block-W mode needs exactly one dense streamer.")
+            raise ValueError("SMILE block-W mode requires exactly one dense genotype source.")
         from .smile_block_w import SmileBlockWeightedOperator, SmileMultiBlockWeightedOperator
 
         st = self.streamers[0]

@@ -362,9 +362,11 @@ class SparseGenoBlockStreamer:
 
     def standardized_columns(self, snp_indices) -> torch.Tensor:
         """Device FP32 (n, len(snp_indices)) standardised columns (missing -> 0)."""
-        idx = np.asarray(snp_indices, dtype=np.int64).reshape(-1)
+        idx = np.asarray(snp_indices, dtype=np.int64)
+        if idx.ndim != 1:
+            raise ValueError("snp_indices must be 1D.")
         if idx.size and (idx.min() < 0 or idx.max() >= self.m):
-            raise IndexError(f"SNP indices must lie in [0, {self.m}).")
+            raise IndexError("snp_indices out of range.")
         out = torch.empty((self.n, idx.size), dtype=torch.float32, device=self.dev)
         if idx.size == 0:
             return out

@@ -253,3 +253,54 @@ def test_preconditioner_is_built_once_per_fitter(monkeypatch):
     assert passed[2] is None
     fitter.close()
     assert fitter.precond_conf is None
+
+
+def test_partition_checks_follow_the_reference(fakes):
+    """reml_model.py:464-512: one dense source split into components."""
+    with pytest.raises(ValueError, match="either vc_block_sizes or component_variant_indices"):
+        InfinitesimalREMLFitter(FitConfig(sources=["a"], vc_block_sizes=[2],
+                                          component_variant_indices=[[0, 1]]))
+    with pytest.raises(ValueError, match="only for dense-only fits"):
+        InfinitesimalREMLFitter(FitConfig(sources=["a"], vc_block_sizes=[2], rare_sources=["r"]))
+    with pytest.raises(ValueError, match="exactly one dense source"):
+        InfinitesimalREMLFitter(FitConfig(sources=["a", "b"], vc_block_sizes=[2]))
+    with pytest.raises(ValueError, match="exactly one dense BED prefix"):
+        InfinitesimalREMLFitter(FitConfig(bed_prefix=["a", "b"], component_variant_indices=[[0]]))
+    f = InfinitesimalREMLFitter(FitConfig(sources=["a"], vc_block_sizes=[3, 7]))
+    assert f.streamers[0].kw["component_block_sizes"] == [3, 7]
+
+
+def test_prediction_geometry_checks():
+    """reml_model.py:223-272 (without the variant-metadata files)."""
+    import types
+
+    import numpy as np
+
+    def geo(m=10, starts=(0, 5), widths=(5, 5), part=False, cts=None, offs=(0, 10)):
+        return types.SimpleNamespace(m=m, _n_calls=len(starts), _call_snp_starts=np.array(starts),
+                                     _call_true_widths=np.array(widths),
+                                     has_component_partition=part,
+                                     _cache_to_source_variant_indices=cts,
+                                     _component_snp_offsets=np.array(offs))
+
+    check = reml_model._validate_dense_prediction_streamers
+    check([geo()], [geo()])
+    cases = [
+        ([geo(), geo()], [geo()], "component count mismatch"),
+        ([geo()], [geo(m=11)], "SNP count mismatch"),
+        ([geo()], [geo(starts=(0,), widths=(10,))], "call geometry mismatch"),
+        ([geo()], [geo(starts=(0, 4))], "SNP call starts mismatch"),
+        ([geo()], [geo(widths=(5, 6))], "call widths mismatch"),
+        ([geo(part=True)], [geo()], "partitioning mode mismatch"),
+        ([geo(cts=np.arange(10))], [geo()], "variant-order mapping mismatch"),
+        ([geo(cts=np.arange(10))], [geo(cts=np.arange(10)[::-1])], "source-variant order"),
+        ([geo(part=True, offs=(0, 4, 10))], [geo(part=True, offs=(0, 5, 10))],
+         "component block layout mismatch"),
+    ]
+    for train, test, match in cases:
+        with pytest.raises(ValueError, match=match):
+            check(train, test)
+    with pytest.raises(FloatingPointError, match="Failed to stabilize GLS"):
+        import torch
+
+        reml_model._solve_small_spd(torch.tensor([[0.0, 1e3], [1e3, 0.0]]), torch.ones(2))
