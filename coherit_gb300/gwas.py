@@ -72,9 +72,14 @@ def marginal_scan(streamer, y, covar=None) -> dict:
     if n != int(streamer.n):
         raise ValueError(f"Sample-size mismatch between phenotype (n={n}) and streamer "
                          f"(n={int(streamer.n)}).")
+    if getattr(streamer, "_means_host", None) is None or \
+            getattr(streamer, "_inv_sds_host", None) is None:
+        raise ValueError("GWAS requires keep_host_stats=True on dense streamers.")
     if getattr(streamer, "_count_host", None) is None:
         raise ValueError("GWAS requires per-SNP non-missing counts; rebuild streamers without "
                          "standardization_override or with host stats retained.")
+    if np.asarray(streamer._count_host).size != int(streamer.m):
+        raise RuntimeError("Internal GWAS count vector length mismatch.")
     if covar is None or np.size(covar) == 0:
         X = np.ones((n, 1), dtype=np.float32)
     else:

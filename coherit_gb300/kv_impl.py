@@ -206,6 +206,17 @@ def zxb_impl_streamed(b_by_call, true_widths, means_by_call, inv_by_call, *, n: 
         raise ValueError(
             f"zxb_impl_streamed b_by_call row mismatch: expected n_calls={int(n_calls)}, "
             f"got {int(bb.shape[0])}.")
+    tws, mbs, ibs = (tuple(torch.as_tensor(x).shape)
+                     for x in (true_widths, means_by_call, inv_by_call))
+    if len(tws) != 1 or tws[0] != int(n_calls):
+        raise ValueError(f"zxb_impl_streamed true_widths must have shape ({int(n_calls)},), "
+                         f"got {tws}.")
+    if len(mbs) != 2 or mbs[0] != int(n_calls):
+        raise ValueError("zxb_impl_streamed means_by_call must have shape "
+                         f"(n_calls, max_unpack_width), got {mbs}.")
+    if ibs != mbs:
+        raise ValueError(f"zxb_impl_streamed inv_by_call shape mismatch: expected {mbs}, "
+                         f"got {ibs}.")
     tw, _, _ = _flat_stats(true_widths, means_by_call, inv_by_call)
     if component_ids is not None:
         component_ids = np.asarray(component_ids, dtype=np.int32).reshape(-1)

@@ -586,7 +586,7 @@ class SmileMultiBlockWeightedOperator:
         tg = np.asarray(theta_g, dtype=np.float64).reshape(-1)
         if tg.size != len(self.operators):
             raise ValueError(
-                f"theta_g must have length {len(self.operators)} for SMILE multi-GRM.")
+                f"theta_g must be a length-{len(self.operators)} array for SMILE multi-GRM.")
         Vm, squeeze = as_rhs(V, self.streamer.dev)
         XtV = self.streamer.xtv(Vm, normalize=False)
         scores = torch.zeros((int(self.streamer.m), Vm.shape[1]), dtype=torch.float32,
@@ -602,7 +602,7 @@ class SmileMultiBlockWeightedOperator:
         tg = np.asarray(theta_g, dtype=np.float64).reshape(-1)
         if tg.size != len(self.operators):
             raise ValueError(
-                f"theta_g must have length {len(self.operators)} for SMILE multi-GRM.")
+                f"theta_g must be a length-{len(self.operators)} array for SMILE multi-GRM.")
         return tuple(op.snp_effects(alpha, tg[i]) for i, op in enumerate(self.operators))
 
 

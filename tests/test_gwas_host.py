@@ -150,3 +150,15 @@ def test_run_continuous_gwas_metadata_errors(tmp_path):
         f.write("1 rs0 0\n")
     with pytest.raises(ValueError, match="fewer than 6"):
         gwas.run_continuous_gwas(fitter, np.arange(16.0), out_prefix=str(tmp_path / "c"))
+
+
+def test_marginal_scan_requires_host_statistics():
+    """gwas.py:92-93, :163-164 of the reference."""
+    st = _DenseStreamer(_codes(4, 12, 6))
+    st._means_host = None
+    with pytest.raises(ValueError, match="keep_host_stats=True"):
+        gwas.marginal_scan(st, np.arange(12.0))
+    st = _DenseStreamer(_codes(4, 12, 6))
+    st._count_host = st._count_host[:5]
+    with pytest.raises(RuntimeError, match="count vector length"):
+        gwas.marginal_scan(st, np.arange(12.0))

@@ -55,3 +55,18 @@ def test_multi_streamed_argument_checks():
         f([np.zeros(4)], [st], [])
     with pytest.raises(ValueError, match="expected n_calls=2, got 3"):
         f([np.zeros((3, 4))], [st], [])
+
+
+def test_zxb_streamed_shape_checks():
+    """kv_impl.py:538-571 of the reference."""
+    f = kv_impl.zxb_impl_streamed
+    b = np.zeros((2, 8), np.float32)
+    ok = dict(true_widths=np.array([8, 8]), means_by_call=np.zeros((2, 8)),
+              inv_by_call=np.zeros((2, 8)))
+    for bad, match in ((dict(true_widths=np.array([8])), "true_widths must have shape"),
+                       (dict(means_by_call=np.zeros(8)), "means_by_call must have shape"),
+                       (dict(inv_by_call=np.zeros((2, 7))), "inv_by_call shape mismatch")):
+        args = {**ok, **bad}
+        with pytest.raises(ValueError, match=match):
+            f(b, args["true_widths"], args["means_by_call"], args["inv_by_call"], n=3, n_calls=2,
+              pop_block=None)
