@@ -202,3 +202,45 @@ def test_fit_infinitesimal_matches_oracle_fit(monkeypatch, comps):
     assert abs(res.heritability - h2_ref) < 1e-3, (res.heritability, h2_ref)
     assert abs(res.final_loglik - cur["ll"]) <= 1e-4 * abs(cur["ll"])
     assert res.final_ai.shape == (G + 1, G + 1) and len(res.history) >= 1
+
+
+def test_dense_plus_rare_streamer_fit_matches_oracle(monkeypatch):
+    """A dense GRM and a rare-variant GRM as two streamers (reml_model.py:611-666,
+    :1196-1290): per-streamer operators, the summed preconditioner kernel and
+    its refresh, against the oracle's two-GRM fit.  Prediction refuses
+    rare-variant streamers."""
+    from coherit_gb300 import reml, synth
+    from oracle import sparse12 as osp
+
+    class _Rare(_HostGeno):
+        has_sparse_backend = True
+
+    monkeypatch.setattr(reml, "pcg_solve", _exact_solve)
+    n = 200
+    dense = _HostGeno(og.synth_codes(91, n, np.arange(600)))
+    lo, hi = synth.maf_range_q24(0.0005, 0.01)
+    rare = _Rare(osp.synth_rare_codes(92, n, np.arange(900), lo, hi))
+    rng = np.random.default_rng(9)
+    g = dense.Z @ rng.normal(size=600) + rare.Z @ rng.normal(size=900)
+    X = np.column_stack([np.ones(n), rng.normal(size=n)])
+    y = (g / g.std() * np.sqrt(0.5) + rng.normal(scale=np.sqrt(0.5), size=n)).astype(np.float32)
+    probes = rng.choice([-1.0, 1.0], size=(n, 16))
+    cfg = FitConfig(slq_samples=16, slq_m=16, precond_rank=12, reml_pcg_tol=1e-5, minq_iter=15,
+                    slq_mode="raw", verbose=False)
+    fitter = InfinitesimalREMLFitter(cfg, [dense, rare])
+    assert fitter._has_sparse and fitter._n_dense_streamers == 1
+    res = fitter.fit_infinitesimal(y, X, slq_probes=torch.as_tensor(probes, dtype=torch.float32))
+    Ks = [s.Z @ s.Z.T / s._eff_m_host for s in (dense, rare)]
+    atoms = np.asarray([dense._mean_diag_atom_host, rare._mean_diag_atom_host], np.float32)
+    atoms = atoms.astype(np.float64)
+    yo, _, _ = oreml.standardize(y)
+    ctx = oreml.Context(yo, [(lambda v, K=K: K @ v) for K in Ks], X, diag_atoms=atoms,
+                        slq_probes=probes, slq_m=16, pcg_tol=1e-6, maxiter=1000)
+    po, _, cur = oreml.fit(ctx, minq_iter=15)
+    h2_ref = oreml.heritability(po, 2, atoms)
+    assert abs(res.heritability - h2_ref) < 1e-3, (res.heritability, h2_ref)
+    assert abs(res.final_loglik - cur["ll"]) <= 1e-4 * abs(cur["ll"])
+    monkeypatch.setattr(pcg, "pcg_solve", _exact_solve)
+    eff = fitter.estimate_effects(y, var_components=res.var_components, covar=X)
+    with pytest.raises(NotImplementedError, match="dense genotype paths only"):
+        fitter.predict(eff, test_fitter=fitter, test_covar=X)
