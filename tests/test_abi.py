@@ -64,6 +64,16 @@ def test_package_exports_resolve():
     assert hot_path <= set(coherit_gb300.__all__)
 
 
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No CPU fallback: without the built library every entry point refuses."""
+    import pytest
+
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(build_ext, "LIB_PATH", tmp_path / "libcoherit_gpu.so")
+    with pytest.raises(RuntimeError, match="CUDA library not found"):
+        _lib.load(build_if_missing=False)
+
+
 def test_null_handle_is_rejected_without_gpu():
     lib = _lib.load()
     assert lib.coherit_geno_info(None, None, None, None, None, None, None, None) == _lib.E_CLOSED
