@@ -739,8 +739,18 @@ class GenoBlockStreamer:
 class BedBlockStreamer(GenoBlockStreamer):
     """``BedBlockStreamer(bed_prefix, ...)`` alias (geno_stream.py:2867-2896)."""
 
-    def __init__(self, bed_prefix: str, call_width: int = 131072, **kwargs):
-        super().__init__(bed_prefix=bed_prefix, call_width=call_width, **kwargs)
+    def __init__(self, bed_prefix: str, call_width: int = 131072, component_block_sizes=None,
+                 component_variant_indices=None, standardization_override=None, device=None,
+                 keep_host_stats: bool = True, build_threads: int | None = None,
+                 sample_mask: np.ndarray | None = None, ring_depth: int | None = None,
+                 source_build_chunk_width: int | None = None, *, precision: str | None = None):
+        super().__init__(bed_prefix=bed_prefix, call_width=call_width,
+                         component_block_sizes=component_block_sizes,
+                         component_variant_indices=component_variant_indices,
+                         standardization_override=standardization_override, device=device,
+                         keep_host_stats=keep_host_stats, build_threads=build_threads,
+                         sample_mask=sample_mask, ring_depth=ring_depth,
+                         source_build_chunk_width=source_build_chunk_width, precision=precision)
 
 
 __all__ = [
