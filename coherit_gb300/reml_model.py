@@ -555,8 +555,9 @@ class InfinitesimalREMLFitter:
                 slq_probes=slq_probes, trace_probes=trace_probes,
             ))
         param, history, diag = reps[0]
-        ga = np.asarray(diag.get("genetic_trace_atoms"), np.float64)
-        ra = np.asarray(diag.get("residual_trace_atoms"), np.float64)
+        # Unit-variance components report no trace atoms (reml_model.py:1876-1889).
+        ga, ra = (None if diag.get(k) is None else np.asarray(diag[k], np.float64)
+                  for k in ("genetic_trace_atoms", "residual_trace_atoms"))
 
         def reported_h2(theta):
             theta = np.asarray(theta, np.float64)

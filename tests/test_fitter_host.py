@@ -304,3 +304,18 @@ def test_prediction_geometry_checks():
         import torch
 
         reml_model._solve_small_spd(torch.tensor([[0.0, 1e3], [1e3, 0.0]]), torch.ones(2))
+
+
+def test_unit_variance_components_report_no_atoms(monkeypatch):
+    import numpy as np
+
+    def fit(**kwargs):
+        assert kwargs["unit_variance_components"] is True
+        diag = {"loglik": -1.0, "ai": np.eye(2), "grad": np.zeros(2)}
+        return np.array([0.6, 0.2]), [], diag
+
+    monkeypatch.setattr(reml_model, "fit_reml", fit)
+    cfg = FitConfig(precond_rank=0, unit_variance_components=True)
+    res = InfinitesimalREMLFitter(cfg, [_Operator()]).fit_infinitesimal(np.ones(8))
+    assert res.genetic_trace_atoms is None and res.residual_trace_atoms is None
+    assert res.heritability == pytest.approx(0.75)
