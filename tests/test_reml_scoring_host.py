@@ -126,3 +126,39 @@ def test_scoring_driver_takes_single_trials_and_expands_small_steps():
     if hist[-1]["stop_reason"] == "scoring_step":
         assert hist[-1]["max_rel_dp"] < 1e-4
     assert np.all(np.isfinite(param)) and np.isfinite(diag["loglik"])
+
+
+def test_taylor_logdet_is_the_first_order_expansion(monkeypatch):
+    """logdet(theta + d) ~ logdet(theta) + sum_i d_i tr(H^-1 M_i), the traces
+    taken at the last full evaluation (reml.py:1800-1829)."""
+    Ks, X, y, Z, _ = _problem(n=80, R=32)
+    Kt = [torch.as_tensor(K, dtype=torch.float32) for K in Ks]
+    calls = []
+    original = reml._eval_once
+
+    def recording(ctx, pvec, *a, taylor_logdet=None, **kw):
+        out = original(ctx, pvec, *a, taylor_logdet=taylor_logdet, **kw)
+        calls.append((np.array(pvec, np.float64), None if taylor_logdet is None
+                      else float(taylor_logdet), float(out[8])))
+        return out
+
+    monkeypatch.setattr(reml, "_eval_once", recording)
+    probes = np.random.default_rng(5).choice([-1.0, 1.0], size=(80, 12))
+    reml.fit_reml(y.astype(np.float32), tuple(lambda v, k=k: k @ v for k in Kt),
+                  [torch.diagonal(k) for k in Kt], X, n_rand_vec=32, maxiter=300, minq_iter=12,
+                  slq_samples=12, slq_m=10, slq_mode="raw", pcg_tol=1e-5, verbose=False,
+                  device="cpu", optimizer="smile_scoring",
+                  slq_probes=torch.as_tensor(probes, dtype=torch.float32),
+                  trace_probes=torch.as_tensor(Z, dtype=torch.float32), taylor_threshold=0.05)
+    R = Z.shape[1]
+    expansions = 0
+    anchor_theta, anchor_logdet = calls[0][0], calls[0][2]
+    for theta, taylor, logdet in calls[1:]:
+        if taylor is not None:
+            Hi, _, mats, _ = _dense(anchor_theta, Ks, X, None)
+            tr = np.array([np.sum((Hi @ Z) * (M @ Z)) / R for M in mats])
+            expected = anchor_logdet + (theta - anchor_theta) @ tr
+            assert taylor == pytest.approx(expected, rel=1e-5, abs=1e-6)
+            expansions += 1
+        anchor_theta, anchor_logdet = theta, logdet     # every scoring step is accepted
+    assert expansions >= 1
