@@ -784,3 +784,44 @@ def test_driver_steps_equal_oracle_on_analytic_objective(monkeypatch, G, E):
                 "frozen_genetic", "ai_pcg_iters", "ws_trace"):
         assert key in last, key
     assert diag["loglik"] == pytest.approx(ll_of(param))
+
+
+def test_preconditioner_refresh_follows_accepted_non_final_steps(monkeypatch):
+    """reml.py:1922-1940 of the reference: after an accepted step that does not
+    end the fit (and is not the last allowed iteration) the PCG
+    preconditioner is rebuilt at the accepted parameters."""
+    ll_of, grad_of, ai = _quadratic(2, 1)
+    seen_conf = []
+
+    def package_eval(ctx, pvec, warm_all, warm_ai=None, *, min_loglik=None, **kw):
+        seen_conf.append(ctx.precond_conf)
+        t = np.asarray(pvec, np.float64)
+        ll = float(ll_of(t))
+        if min_loglik is not None and not ll >= min_loglik:
+            return (ll, None, None, 3, warm_all, None, None, None, None)
+        FI = reml.AverageInfoMatrix(mat=ai.copy(), stats=reml.FisherSolveStats(ai_pcg_iters=4))
+        return (ll, grad_of(t), FI, 7, warm_all, warm_ai, None, None, None)
+
+    monkeypatch.setattr(reml, "_eval_once", package_eval)
+    refreshes = []
+
+    def refresh(theta):
+        refreshes.append(np.array(theta))
+        return ("conf", len(refreshes))
+
+    K_mvs, _ = _kernels(2)
+    diags = [torch.tensor(0.9), torch.tensor(1.1)]
+    y = np.random.default_rng(1).normal(size=24).astype(np.float32)
+    args = (y, K_mvs, diags, None)
+    kw = dict(n_rand_vec=3, maxiter=50, minq_iter=30, slq_samples=3, slq_m=4, verbose=False,
+              device="cpu")
+    param, hist = reml.fit_reml(*args, **kw, precond_refresh_fn=refresh)
+    flagged = [h for h in hist if h["pcg_precond_refreshed"]]
+    assert len(flagged) == len(refreshes) == sum(
+        1 for h in hist if h["accepted"] and not h["converged"])
+    for h, theta in zip(flagged, refreshes):
+        np.testing.assert_array_equal(h["params"], theta)
+    # The evaluations after a refresh see the rebuilt configuration.
+    assert refreshes and ("conf", len(refreshes)) in seen_conf
+    with pytest.raises(RuntimeError, match="returned no configuration"):
+        reml.fit_reml(*args, **kw, precond_refresh_fn=lambda theta: None)
