@@ -40,6 +40,13 @@ def test_status_mapping():
         _lib.check(_lib.E_NONFINITE)
     with pytest.raises(RuntimeError):
         _lib.check(_lib.E_CLOSED)
+    with pytest.raises(FloatingPointError):
+        _lib.check(_lib.E_NOT_CONVERGED)
+    with pytest.raises(MemoryError):
+        _lib.check(_lib.E_OOM)
+    for code in (_lib.E_TIMEOUT, _lib.E_CUDA, _lib.E_UNSUPPORTED):
+        with pytest.raises(RuntimeError, match=f"status {code}"):
+            _lib.check(code, "op")
     _lib.check(_lib.OK)
 
 
