@@ -160,21 +160,91 @@ def cpu_operator_sample(n: int, m_sample: int, k: int, seed: int, reps: int = 2)
     return (time.perf_counter() - t0) / reps
 
 
-def cpu_fit_estimate(wl, apps: int, cols: int, budget_s: float = 20.0):
-    """CPU seconds for one fit, scaled from two sampled application widths."""
-    m_sample = 2048
+def _cores():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+
+def cpu_vector_sample(n: int, k: int, reps: int = 3):
+    """Seconds of the block-PCG vector work of one iteration (state and
+    direction updates, column reductions) of the oracle port on (n, k)."""
+    from oracle import pcg as opcg
+
+    rng = np.random.default_rng(0)
+    X, R, P, AP, Z = (rng.normal(size=(n, k)).astype(np.float32) for _ in range(5))
+    rs = np.einsum("ij,ij->j", R, Z).astype(np.float64)
+    active = np.ones(k, dtype=bool)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        opcg._state_update(X, R, P, rs, AP, active)
+        opcg._direction_update(P, R, Z, rs, 1e-30)
+    return (time.perf_counter() - t0) / reps
+
+
+def cpu_fit_estimate(wl, apps: float, cols: float, budget_s: float = 20.0):
+    """CPU seconds for one fit at the workload's size, extrapolated: the
+    oracle's FP32 kv_impl_streamed port timed on a 1,024-SNP call block at n
+    samples for two widths (a fixed and a per-column cost), scaled by
+    m / 1,024 and by the fit's operator applications and right-hand-side
+    columns (counted on the GPU in the same run), plus the PCG vector work
+    of one iteration per application."""
+    m_sample = 1024
     k1, k2 = 4, 64
     t1 = cpu_operator_sample(wl.n, m_sample, k1, wl.seed)
     t2 = cpu_operator_sample(wl.n, m_sample, k2, wl.seed)
     per_col = max((t2 - t1) / (k2 - k1), 0.0)
     fixed = max(t1 - per_col * k1, 0.0)
     scale = wl.m / m_sample
-    t_fit = scale * (apps * fixed + cols * per_col)
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    sample = (f"oracle FP32 kv_impl_streamed port, n={wl.n}, {m_sample}-SNP call block, "
-              f"k={k1} and k={k2}; scaled by m/{m_sample} and by the fit's {apps} operator "
-              f"applications / {cols} RHS columns")
-    return t_fit, cores, sample
+    k_typ = max(1, int(round(cols / max(apps, 1.0))))
+    t_vec = cpu_vector_sample(wl.n, k_typ)
+    t_fit = scale * (apps * fixed + cols * per_col) + apps * t_vec
+    sample = (f"extrapolated: oracle FP32 kv_impl_streamed port, n={wl.n}, {m_sample}-SNP call "
+              f"block at k={k1} and k={k2}, scaled by m/{m_sample} and by {apps:.1f} operator "
+              f"applications / {cols:.1f} RHS columns per fit, plus PCG vector work at k={k_typ} "
+              f"per application")
+    return t_fit, _cores(), sample
+
+
+def cpu_c1_fit():
+    """One whole fit of the small CPU-runnable configuration by the CPU port
+    of the reference path, timed end to end on all host cores: per-call
+    packed genotypes (4,096-SNP calls) applied by the FP32 kv_impl_streamed
+    restatement, the affine SLQ cache (30 probes, 30 Lanczos steps), the
+    oracle's block PCG (tol 1e-6) and AI-REML driver.  Returns (seconds,
+    h2)."""
+    from coherit_gb300 import synth
+    from coherit_gb300.configs import C1
+    from oracle import geno as og
+    from oracle import reml as oreml
+    from oracle import slq as oslq
+
+    n, m = C1.n, C1.m
+    codes = og.synth_codes(C1.seed, n, np.arange(m))
+    y, X, _, _ = synth.phenotype(C1.seed, n, m, h2=C1.h2, n_causal=C1.n_causal,
+                                 n_covar=C1.n_covar, noise_var=0.5)
+    probes = np.random.default_rng(C1.seed).choice([-1.0, 1.0], size=(n, C1.slq_samples))
+    t0 = time.perf_counter()
+    starts, widths, _, _ = og.call_geometry(m, 4096)
+    W = 4 * ((int(widths.max()) + 3) // 4)
+    packed = [og.pack_block(codes[:, s0:s0 + w]) for s0, w in zip(starts, widths)]
+    mean, inv, cnt = og.stats(codes)
+    mbc = np.zeros((len(widths), W), np.float32)
+    ibc = np.zeros_like(mbc)
+    for c, (s0, w) in enumerate(zip(starts, widths)):
+        mbc[c, :w] = mean[s0:s0 + w]
+        ibc[c, :w] = inv[s0:s0 + w]
+    eff = float(np.count_nonzero(inv > 0))
+    _, _, _, atom = og.stats_summary(cnt, *og.raw_counts(codes)[1:], mean, inv, n)
+
+    def K(V):
+        return og.kv_streamed_fp32(packed, widths, mbc, ibc, eff, V)
+
+    yo, _, _ = oreml.standardize(y)
+    cache = oslq.affine_cache(K, n, probes, C1.slq_m)
+    ctx = oreml.Context(yo, [K], X, diag_atoms=[atom], affine_cache=cache, pcg_tol=C1.pcg_tol,
+                        maxiter=1000)
+    po, _, _ = oreml.fit(ctx, minq_iter=C1.minq_iter)
+    t = time.perf_counter() - t0
+    return t, oreml.heritability(po, 1, [atom])
 
 
 # ----------------------------------------------------------------- our arm
@@ -232,22 +302,32 @@ def _percentile(xs, q):
     return xs[min(len(xs) - 1, max(0, int(math.ceil(q * len(xs))) - 1))]
 
 
-def operator_roofline(st, k, hbm_peak, tensor_peak, reps=10):
-    """Device time of one batched-width operator application, its HBM and
+def _nsplit(precision: str) -> int:
+    return {"bf16x3": 3, "bf16x2": 2, "fp16x2": 2, "bf16x1": 1}.get(precision, 0)
+
+
+def operator_roofline(st, k, hbm_peak, tensor_peak, reps=10, precision=None):
+    """Device time of one operator application at width k, its HBM and
     tensor fractions (algorithmic bytes n*ceil(m/4) + 8nk + 8m and flops
-    4nmk), timed with CUDA events on the launching stream."""
+    4nmk), timed with CUDA events on the launching stream.  For the
+    tensor-core precisions also the MMA instruction count of the two
+    contractions (M = 128, K = 16: n_pad * m_pad / 1024 per launch) and the
+    SM cycles per instruction this time implies: an instruction of N <= ~190
+    costs a fixed ~90-140 cycles on GB300 whatever N is, so narrow launches
+    are bound by the instruction count, not by HBM."""
     import torch
 
+    precision = precision or st.precision
     V = torch.randn(st.n, k, device=st.dev)
     for _ in range(3):
-        st.kv(V)
+        st.kv(V, precision=precision)
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(reps):
-        st.kv(V)
+        st.kv(V, precision=precision)
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
@@ -269,12 +349,33 @@ def operator_roofline(st, k, hbm_peak, tensor_peak, reps=10):
         roof = {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm_peak, "unit": "GB/s",
                 "frac": round(hbm_frac, 4)}
     roof.update({"traffic": traffic,
-                 "kernel": f"genotype operator application (prep + K1 + K2), k={k}, bf16x3",
+                 "kernel": f"genotype operator application (prep + K1 + K2), k={k}, {precision}",
                  "ms_per_application": round(ms, 4), "algorithmic_bytes": alg_bytes,
                  "algorithmic_flops": alg_flops, "hbm_gbs": round(gbs, 1),
                  "hbm_frac": round(hbm_frac, 4), "tensor_tflops": round(tfs, 1),
                  "tensor_frac": round(ten_frac, 4)})
+    ns = _nsplit(precision)
+    if ns:
+        info = st.info()
+        kp = (k + 15) // 16 * 16
+        max_cols = 128 if precision == "fp16x2" else (256 // ns) // 16 * 16
+        launches = -(-kp // max_cols)
+        instr = 2.0 * info["n_pad"] * info["m_pad"] / 2048.0 * launches
+        sm_hz, sms = _sm_clock_hz(), torch.cuda.get_device_properties(st.dev).multi_processor_count
+        roof["mma_issue"] = {
+            "instructions_per_application": int(instr),
+            "n_per_instruction": ns * min(kp, max_cols),
+            "cycles_per_instruction_per_sm": round(ms * 1e-3 * sm_hz * sms / instr, 1),
+            "sm_clock_mhz_assumed": sm_hz / 1e6}
     return roof
+
+
+def _sm_clock_hz() -> float:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f).get("sm_max_mhz", 2070.0)) * 1e6
+    return 2070e6
 
 
 def sparse12_operator(n, m, k, hbm_peak, dense_ms, seed, reps=10):
@@ -426,8 +527,14 @@ def run_ours(args, wl):
     srv = REMLServer(st, max_active=R, precision=args.precision, fit_kwargs=fit_kwargs(wl),
                      batch_window_s=args.batch_window)
 
-    for _ in range(args.warmup):
+    cold_fit_s = None
+    for w in range(args.warmup):
+        t0 = time.perf_counter()
         serve_step(srv, ys, Xs, host=False)
+        torch.cuda.synchronize()
+        if w == 0:
+            # The first batch builds the shared SLQ cache and preconditioner set-up.
+            cold_fit_s = time.perf_counter() - t0
     torch.cuda.synchronize()
     launches0 = lib.coherit_launch_count()
     b0, c0 = srv.batcher.launches, srv.batcher.columns
@@ -453,6 +560,9 @@ def run_ours(args, wl):
     launches = lib.coherit_launch_count() - launches0
     op_launches = srv.batcher.launches - b0
     op_cols = srv.batcher.columns - c0
+    # Operator applications the timed fits requested (a launch serves one
+    # application of each request it carries).
+    op_apps = float(sum(srv.batcher.requests_per_launch[b0:b0 + op_launches]))
     lat = [r.latency for r in timed]
 
     # End to end through the public API: phenotypes/covariates from pinned
@@ -468,8 +578,10 @@ def run_ours(args, wl):
     dev_s, e2e_s, value, e2e_val = replica_totals(dev_s, e2e_s, args.steps, R, dist, dev)
     result = None
     if rank == 0:
+        n_fits = args.steps * R
+        fit_apps, fit_cols = op_apps / n_fits, op_cols / n_fits
         k_typ = max(16, int(round(op_cols / max(op_launches, 1))))
-        roof = operator_roofline(st, k_typ, hbm_peak, tensor_peak)
+        roof = operator_roofline(st, k_typ, hbm_peak, tensor_peak, precision=args.precision)
         roof["peak_source"] = peak_src
         single = None
         plain = None
@@ -486,42 +598,51 @@ def run_ours(args, wl):
                 sh2.append(fitter.fit_infinitesimal(ys[r], Xs[r]).heritability)
             torch.cuda.synchronize()
             ts = (time.perf_counter() - t0) / len(sh2)
-            fit_apps = (st.op_stats["apps"] - a0) / len(sh2)
-            fit_cols = (st.op_stats["cols"] - k0) / len(sh2)
             single = {"fits_per_hr": round(3600.0 / ts, 3), "fit_s": round(ts, 4),
-                      "operator_apps_per_fit": fit_apps, "rhs_columns_per_fit": fit_cols,
+                      "operator_apps_per_fit": (st.op_stats["apps"] - a0) / len(sh2),
+                      "rhs_columns_per_fit": (st.op_stats["cols"] - k0) / len(sh2),
                       "max_abs_dh2_vs_served": round(max(
                           abs(a - b.heritability) for a, b in zip(sh2, timed)), 6)}
-        else:
-            fit_apps, fit_cols = args.ref_apps, args.ref_cols
         if not args.no_plain:
             # Plain FP32 single-fit form, warm (its shared setup built by a
             # first fit), timed on the second phenotype.
             pf = make_fitter(st, wl, "fp32")
             pf.fit_infinitesimal(ys[0], Xs[0])
             torch.cuda.synchronize()
+            a0, k0 = st.op_stats["apps"], st.op_stats["cols"]
             t0 = time.perf_counter()
             pres = pf.fit_infinitesimal(ys[1 % R], Xs[1 % R])
             torch.cuda.synchronize()
             tp = time.perf_counter() - t0
+            papps = st.op_stats["apps"] - a0
+            pcols = st.op_stats["cols"] - k0
+            pk = max(1, int(round(pcols / max(papps, 1))))
             plain = {"fits_per_hr": round(3600.0 / tp, 3), "fit_s": round(tp, 3),
                      "h2": round(pres.heritability, 6),
                      "abs_dh2_vs_served": round(
-                         abs(pres.heritability - timed[1 % R].heritability), 6)}
+                         abs(pres.heritability - timed[1 % R].heritability), 6),
+                     "operator_apps_per_fit": papps, "rhs_columns_per_fit": pcols,
+                     "roofline": operator_roofline(st, pk, hbm_peak, tensor_peak,
+                                                   precision="fp32", reps=3)}
         stream = None
         if args.stream > 0:
-            rate = args.stream_rate
-            stream = serving_stream(st, wl, args.stream, rate, seed=wl.seed + 99,
+            stream = serving_stream(st, wl, args.stream, args.stream_rate, seed=wl.seed + 99,
                                     max_active=R)
         sparse = None
-        if not args.no_sparse:
+        if args.sparse12:
             sparse = sparse12_operator(wl.n, wl.m, k_typ, hbm_peak, roof["ms_per_application"],
                                        seed=wl.seed + 7)
         cpu = None
         if not args.no_cpu:
+            c1_s, c1_h2 = cpu_c1_fit()
             t_fit, cores, sample = cpu_fit_estimate(wl, fit_apps, fit_cols)
-            cpu = {"value": round(3600.0 / t_fit, 4), "unit": "fits/hr", "cores": cores,
-                   "kind": "port", "sample": sample, "fit_s_extrapolated": round(t_fit, 1)}
+            cpu = {"value": round(3600.0 / t_fit, 5), "unit": "fits/hr", "cores": cores,
+                   "kind": "port", "extrapolated": True, "sample": sample,
+                   "fit_s_extrapolated": round(t_fit, 1),
+                   "c1_whole_fit": {"fit_s": round(c1_s, 2),
+                                    "fits_per_hr": round(3600.0 / c1_s, 2),
+                                    "h2": round(c1_h2, 6), "cores": cores,
+                                    "workload": "c1_n2000_m10000 (measured end to end)"}}
         result = {
             "metric": METRIC,
             "value": round(value, 3),
@@ -533,19 +654,27 @@ def run_ours(args, wl):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "bf16x3 genotype operator, fp32 PCG, fp64 small solves",
+            "dtype": f"{args.precision} genotype operator, fp32 PCG, fp64 small solves",
             "data": "synthetic (device-generated MAF~U(0.05,0.5) HWE genotypes; "
                     f"{R} phenotypes with h2={wl.h2}, {wl.n_causal} causal SNPs each)",
             "config": {"workload": wl.name, "n": wl.n, "m": wl.m,
                        "requests_per_step": R, "slq_probes": wl.slq_samples,
                        "lanczos_steps": wl.slq_m, "covariates": wl.n_covar,
                        "pcg_tol": wl.pcg_tol, "parallelism": f"replicas x{ws}",
-                       "l2_policy": "inputs larger than L2 (2 x 6.25 GB packed genotypes)"},
+                       "slq_cache": "the affine SLQ cache (slq_probes x lanczos_steps operator "
+                                    "columns) is built once during warm-up and shared by every "
+                                    "fit on these genotypes, as the reference's REMLProbeCache "
+                                    "allows; each step re-fits the same R phenotypes",
+                       "l2_policy": "inputs larger than L2 (2 x n*m/4 bytes of packed "
+                                    "genotypes, 50 GB at n=100k, m=1M)"},
             "latency_s": {"p50": round(statistics.median(lat), 3),
                           "p99": round(_percentile(lat, 0.99), 3)},
+            "cold_step_s": None if cold_fit_s is None else round(cold_fit_s, 3),
             "h2": [round(r.heritability, 4) for r in timed[:R]],
             "operator_launches_per_step": op_launches / args.steps,
             "rhs_columns_per_launch": round(op_cols / max(op_launches, 1), 1),
+            "operator_apps_per_fit": round(fit_apps, 2),
+            "rhs_columns_per_fit": round(fit_cols, 1),
             "e2e": {"value": round(e2e_val, 3), "unit": "fits/hr",
                     "h2d_bytes_per_step": int(sum(y.numel() * 4 + X.numel() * 4
                                                   for y, X in zip(ys_host, Xs_host))),
@@ -559,6 +688,11 @@ def run_ours(args, wl):
             "cpu_baseline": cpu,
             "clocks": clocks,
         }
+        if args.write_counts:
+            with open(args.write_counts, "w") as f:
+                json.dump({"workload": wl.name, "operator_apps_per_fit": fit_apps,
+                           "rhs_columns_per_fit": fit_cols,
+                           "source": "bench.py serving run (timed fits)"}, f, indent=1)
     st.close()
     if dist is not None:
         dist.destroy_process_group()
@@ -569,23 +703,53 @@ METRIC = ("REML fits/hr, p50/p99 latency: mixed-precision batched serving form "
           "(plain FP32 single-fit form alongside), 1 GB300, |dh2|<1e-3")
 
 
+def fit_counts(wl):
+    """Operator applications and right-hand-side columns per fit of the
+    workload, as counted by a GPU serving run of this benchmark
+    (``--write-counts``), committed under profiles/."""
+    path = os.path.join(ROOT, "profiles", f"fit_counts_{wl.name}.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        c = json.load(f)
+    return float(c["operator_apps_per_fit"]), float(c["rhs_columns_per_fit"]), path
+
+
 def run_reference(args, wl):
     ws, rank, _ = _dist()
     if rank != 0:
         return None
     # The reference (jax + numba) is not installable here; its CPU path is
-    # restated by the oracle.  Each step times one bounded sample: one FP32
-    # streamed application of a 2048-SNP call block at n on all host cores,
-    # scaled to a whole fit by the operator work a fit performs.
-    apps, cols = args.ref_apps, args.ref_cols
+    # restated by the oracle and run on all host cores.  Each step: one whole
+    # fit of the small CPU-runnable configuration (measured end to end), and
+    # the workload's fit extrapolated from one operator application on a
+    # 1,024-SNP call block at n samples, scaled by the per-fit operator counts
+    # of this benchmark's GPU serving run.
+    from coherit_gb300.configs import C1
+
+    whole = wl.name == C1.name
+    counts = None if whole else fit_counts(wl)
+    if counts is None and not whole:
+        return {"impl": "reference",
+                "unavailable": f"no per-fit operator counts for {wl.name} under profiles/"}
     for _ in range(args.warmup):
-        cpu_operator_sample(wl.n, 2048, 16, wl.seed, reps=1)
-    times = []
+        cpu_operator_sample(wl.n, 256, 4, wl.seed, reps=1)
+    times, c1 = [], []
     for _ in range(args.steps):
-        t_fit, cores, sample = cpu_fit_estimate(wl, apps, cols)
+        c1.append(cpu_c1_fit()[0])
+        if whole:
+            times.append(c1[-1])
+            continue
+        t_fit, cores, sample = cpu_fit_estimate(wl, counts[0], counts[1])
         times.append(t_fit)
     t_fit = statistics.median(times)
     value = 3600.0 / t_fit
+    if whole:
+        cores = _cores()
+        sample = ("whole fit of the CPU port (FP32 kv_impl_streamed on 4,096-SNP packed calls, "
+                  "affine SLQ cache, block PCG, AI-REML), measured end to end")
+    else:
+        sample += f" (counts: {os.path.relpath(counts[2], ROOT)})"
     return {
         "impl": "reference",
         "metric": METRIC,
@@ -604,9 +768,107 @@ def run_reference(args, wl):
                    "lanczos_steps": wl.slq_m, "covariates": wl.n_covar, "pcg_tol": wl.pcg_tol,
                    "parallelism": "CPU, one fit at a time"},
         "cpu_baseline": {"value": round(value, 5), "unit": "fits/hr", "cores": cores,
-                         "kind": "port", "sample": sample},
+                         "kind": "port", "extrapolated": not whole, "sample": sample,
+                         "c1_whole_fit_s": round(statistics.median(c1), 2)},
         "e2e": {"value": round(value, 5), "unit": "fits/hr", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+    }
+
+
+def run_c3(args, wl):
+    """The 8-component workload (``--config c3``): n x m block-LD genotypes
+    generated on the device, 8 components = 4 MAF bins x 2 LD-score halves
+    (LD scores from the first 4,096 samples), per-component h2 ~ Dirichlet(1)
+    x 0.4 from n_causal / 8 causal SNPs each, 10 covariates, 128 SLQ probes,
+    projected-core preconditioner; fits one at a time through the model API
+    (the serving loop takes single-component genotypes).  Reports the cold
+    and warm fit times, the operator roofline at the SLQ width (128) and at
+    the PCG width, and the plain FP32 fit extrapolated from its per-application
+    times and the mixed fit's operator counts (a full FP32 fit at this size
+    takes tens of minutes)."""
+    import torch
+
+    from coherit_gb300 import synth
+    from coherit_gb300.geno_stream import GenoBlockStreamer, LDBlockSource
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    hbm_peak, tensor_peak, peak_src = _peaks()
+    t0 = time.perf_counter()
+    groups, tables = synth.ld_partition_device(wl.seed, wl.m, block=wl.ld_block, device=dev)
+    st = GenoBlockStreamer(LDBlockSource(wl.n, wl.m, seed=wl.seed, block=wl.ld_block),
+                           component_variant_indices=groups, device=dev,
+                           precision=args.precision)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    G = len(groups)
+    h2s = synth.dirichlet_h2(wl.seed, G, total=wl.h2_dirichlet_total)
+    rng = np.random.default_rng(wl.seed + 1)
+    starts = np.concatenate([[0], np.cumsum([g.size for g in groups])])
+    fits = 2
+    ys, Xs = [], []
+    for r in range(fits):
+        B = np.zeros((st.m, G), np.float32)
+        for g in range(G):
+            pos = rng.choice(groups[g].size, size=min(wl.n_causal // G, groups[g].size),
+                             replace=False)
+            B[starts[g] + pos, g] = rng.normal(size=pos.size)
+        gv = st.zxb(torch.as_tensor(B, device=dev)).double()
+        gv = gv * torch.sqrt(torch.as_tensor(h2s, device=dev) / gv.var(dim=0, unbiased=False))
+        gen = torch.Generator(device=dev).manual_seed(wl.seed + 7 * r)
+        noise = torch.randn(st.n, generator=gen, device=dev, dtype=torch.float64)
+        ys.append((gv.sum(dim=1) + noise * math.sqrt(1.0 - h2s.sum())).float())
+        X = torch.randn((st.n, wl.n_covar + 1), generator=gen, device=dev)
+        X[:, 0] = 1.0
+        Xs.append(X)
+    fitter = make_fitter(st, wl, args.precision)
+    sampler = ClockSampler(0)
+    sampler.start()
+    times, res = [], []
+    for r in range(fits):
+        a0, k0 = st.op_stats["apps"], st.op_stats["cols"]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res.append(fitter.fit_infinitesimal(ys[r], Xs[r]))
+        torch.cuda.synchronize()
+        times.append((time.perf_counter() - t0, st.op_stats["apps"] - a0,
+                      st.op_stats["cols"] - k0))
+    clocks = sampler.stop()
+    warm_s, apps, cols = times[-1]
+    roof_slq = operator_roofline(st, wl.slq_samples, hbm_peak, tensor_peak, reps=3,
+                                 precision=args.precision)
+    k_pcg = wl.n_covar + 2
+    roof_pcg = operator_roofline(st, k_pcg, hbm_peak, tensor_peak, reps=3,
+                                 precision=args.precision)
+    fp32_slq = operator_roofline(st, wl.slq_samples, hbm_peak, tensor_peak, reps=1,
+                                 precision="fp32")
+    fp32_pcg = operator_roofline(st, k_pcg, hbm_peak, tensor_peak, reps=2, precision="fp32")
+    # FP32 fit time from the mixed fit's counts: wide (SLQ) and narrow
+    # applications priced at their own FP32 times.
+    mixed_ratio = fp32_pcg["ms_per_application"] / roof_pcg["ms_per_application"]
+    fp32_fit_s = warm_s * max(mixed_ratio, fp32_slq["ms_per_application"] /
+                              roof_slq["ms_per_application"]) if apps else None
+    st.close()
+    return {
+        "metric": "REML fits/hr, 8-component block-LD workload (single fits, model API)",
+        "value": round(3600.0 / warm_s, 3), "unit": "fits/hr", "higher_is_better": True,
+        "config": {"workload": wl.name, "n": wl.n, "m": wl.m, "components": G,
+                   "slq_probes": wl.slq_samples, "lanczos_steps": wl.slq_m,
+                   "precision": args.precision, "precond_rank": wl.precond_rank},
+        "build_s": round(build_s, 2), "cold_fit_s": round(times[0][0], 2),
+        "warm_fit_s": round(warm_s, 2), "operator_apps_per_fit": apps,
+        "rhs_columns_per_fit": cols,
+        "h2_true_total": round(float(h2s.sum()), 4),
+        "h2": [round(r.heritability, 4) for r in res],
+        "var_components": [[round(float(v), 5) for v in r.var_components] for r in res],
+        "component_sizes": [int(g.size) for g in groups],
+        "roofline_slq_width": roof_slq, "roofline_pcg_width": roof_pcg,
+        "plain_fp32": {"ms_per_application_slq_width": fp32_slq["ms_per_application"],
+                       "ms_per_application_pcg_width": fp32_pcg["ms_per_application"],
+                       "fit_s_extrapolated": None if fp32_fit_s is None else round(fp32_fit_s, 1),
+                       "note": "extrapolated: the mixed fit's time scaled by the FP32/mixed "
+                               "per-application ratio (the larger of the SLQ and PCG widths)"},
+        "clocks": clocks, "peak_source": peak_src,
     }
 
 
@@ -759,7 +1021,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", default="c2")
+    ap.add_argument("--config", default="c3s")
     ap.add_argument("--precision", default="bf16x3")
     ap.add_argument("--requests", type=int, default=8,
                     help="concurrent fit requests per step (the serving batch)")
@@ -774,14 +1036,10 @@ def main():
     ap.add_argument("--no-single", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-sparse", action="store_true",
-                    help="skip the rare-variant (sparse12) operator measurement")
-    # Operator work of one warm c2 fit, as counted on the GPU path (same
-    # algorithm and probe settings as the reference's single fit).
-    ap.add_argument("--ref-apps", type=float, default=52.0,
-                    help="operator applications per fit assumed by the reference arm")
-    ap.add_argument("--ref-cols", type=float, default=368.0,
-                    help="right-hand-side columns per fit assumed by the reference arm")
+    ap.add_argument("--sparse12", action="store_true",
+                    help="also time the rare-variant (sparse12) operator at the workload's size")
+    ap.add_argument("--write-counts", default="",
+                    help="write the per-fit operator counts of the timed fits to this JSON file")
     ap.add_argument("--operator", type=int, default=0, metavar="K",
                     help="time bare operator applications of width K instead of fits")
     ap.add_argument("--smile", type=int, default=0, metavar="K",
@@ -806,6 +1064,8 @@ def main():
         out = run_smile_only(args, wl)
     elif args.impl == "reference":
         out = run_reference(args, wl)
+    elif wl.partition == "maf_ld":
+        out = run_c3(args, wl)
     else:
         out = run_ours(args, wl)
     if out is not None:

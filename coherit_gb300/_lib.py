@@ -30,6 +30,7 @@ PREC_FP32 = 0
 PREC_BF16X3 = 1
 PREC_BF16X2 = 2
 PREC_BF16X1 = 3
+PREC_FP16X2 = 4
 
 MODE_SUM = 0
 MODE_STACKED = 1
@@ -39,6 +40,7 @@ PRECISIONS = {
     "bf16x3": PREC_BF16X3,
     "bf16x2": PREC_BF16X2,
     "bf16x1": PREC_BF16X1,
+    "fp16x2": PREC_FP16X2,
 }
 
 _lock = threading.Lock()
@@ -67,6 +69,11 @@ _SIGNATURES = {
     "coherit_geno_create_bed": (
         C.c_int,
         [_p, _i64, _i64, _i64, _p, _i64, _p, _i32, C.c_int, _p, _p],
+    ),
+    "coherit_ldblock_records": (C.c_int, [_i64, _i64, _i32, _u64, _p, _p, _p, _p, _p, _p]),
+    "coherit_geno_create_ldblock": (
+        C.c_int,
+        [_i64, _i64, _i32, _u64, _p, _p, _p, _p, _p, _p, _i32, C.c_int, _p, _p],
     ),
     "coherit_geno_destroy": (C.c_int, [_p]),
     "coherit_geno_info": (C.c_int, [_p, _p, _p, _p, _p, _p, _p, _p]),

@@ -19,6 +19,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -37,6 +38,12 @@ constexpr int kTile = 128;                           // rows per block
 // kMaxStageBlocks * 64, so that every launch's stage size divides them.
 constexpr int kMaxStageBlocks = 4;
 constexpr int kAlign = kPanel * kMaxStageBlocks;  // 256, a multiple of kTile
+// Centring segments of the operator's first contraction: the right-hand side
+// is shifted by its mean over each segment of kSegChunks sample chunks
+// (4,096 samples), so the FP32 tensor-core accumulator never carries the
+// running sum of a trend or an offset.
+constexpr int kSegChunks = 64;
+inline int64_t n_segments(int64_t n_chunks) { return (n_chunks + kSegChunks - 1) / kSegChunks; }
 static_assert(kAlign % kTile == 0, "padding must hold whole 128-row tiles");
 
 // -------------------------------------------------------------- status
@@ -142,6 +149,14 @@ struct StatsSlot {
   bool used = false;
   float* mean = nullptr;        // m_pad, device
   float* inv = nullptr;         // m_pad, device
+  // m_pad, device: sum over all the slot's samples of diff_ij = s1_j - cnt_j
+  // * mean_j (observed allele sum minus observed count times the FP32 mean;
+  // zero up to the rounding of mean_j; 0 for padding slots).
+  float* dsum = nullptr;
+  // m_pad x n_seg, device, slot-major: the same sum over the samples of each
+  // centring segment z (4,096 samples).
+  float* dseg = nullptr;
+  float* nseg = nullptr;  // n_seg, device: samples of the slot in each segment
   uint8_t* row_mask = nullptr;  // n_pad bytes, device; nullptr = all samples
   uint32_t* tmask = nullptr;    // n_chunks * 4 words: sample mask in row order (2 bits/sample)
   int64_t n_sub = 0;
@@ -231,12 +246,17 @@ int run_operator_fp32(coherit_geno* h, const OpDesc& d, cudaStream_t st);
 // (`bytes` long); never allocates; rejects shapes whose workspace is larger.
 int run_operator_in_scratch(coherit_geno* h, const OpDesc& d, void* scratch, size_t bytes,
                             cudaStream_t st);
-int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t nsplit);
+int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t nsplit, bool f16);
 int ensure_ws_bytes(coherit_geno* h, size_t bytes);
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 inline int nsplit_of(int precision) {
-  return precision == COHERIT_PREC_BF16X3 ? 3 : precision == COHERIT_PREC_BF16X2 ? 2 : 1;
+  return precision == COHERIT_PREC_BF16X3 ? 3
+         : (precision == COHERIT_PREC_BF16X2 || precision == COHERIT_PREC_FP16X2) ? 2 : 1;
+}
+inline bool is_f16(int precision) { return precision == COHERIT_PREC_FP16X2; }
+inline bool is_tc_precision(int precision) {
+  return precision >= COHERIT_PREC_BF16X3 && precision <= COHERIT_PREC_FP16X2;
 }
 
 }  // namespace coherit

@@ -102,6 +102,59 @@ __global__ void k_build_s_from_bed(uint8_t* __restrict__ geno_s, int64_t n, int6
   *dst = make_uint4(old.x | w[0], old.y | w[1], old.z | w[2], old.w | w[3]);
 }
 
+// Block-LD generator (genotypes with linkage disequilibrium, for the
+// 8-component benchmark workload).  SNPs come in blocks of `block`; every
+// sample carries two latent haplotype chains per block,
+//   x_0 = e_0,  x_p = rho_b x_{p-1} + s_b e_p   (FP32, each operation rounded),
+// with e drawn from a 4096-entry table of standard-normal quantiles indexed
+// by the top 12 bits of a counter-based hash of (seed, SNP, sample,
+// haplotype); allele = [x_p < thr_j], genotype = sum of the two alleles, so
+// every allele is Bernoulli(Phi(thr_j)) and neighbouring SNPs share rho_b.
+// The tables (thr, rho, s, quantiles) come from the host, where a numpy
+// twin of the same arithmetic reproduces every code.  One thread per (4
+// consecutive samples, LD block) writes SNP-major PLINK BED records (byte q
+// of the record of SNP j holds samples 4q..4q+3; count 2, 1, 0 -> BED code
+// 0, 2, 3) at record record_of_snp[j] (identity when null).
+__global__ void __launch_bounds__(256) k_ldblock_records(
+    uint8_t* __restrict__ out, int64_t n_rows, int64_t bps, int64_t m, int32_t block,
+    uint64_t seed, const float* __restrict__ thr, const float* __restrict__ rho,
+    const float* __restrict__ sfac, const float* __restrict__ qtab,
+    const int64_t* __restrict__ record_of_snp) {
+  __shared__ float q[4096];
+  for (int t = threadIdx.x; t < 4096; t += blockDim.x) q[t] = qtab[t];
+  __syncthreads();
+  const int64_t nb = (m + block - 1) / block;
+  const int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (idx >= bps * nb) return;
+  const int64_t qg = idx % bps;
+  const int64_t b = idx / bps;
+  const float r = rho[b], sf = sfac[b];
+  float x[8];
+  const int64_t j0 = b * block, j1 = min(m, j0 + static_cast<int64_t>(block));
+  for (int64_t j = j0; j < j1; ++j) {
+    const uint64_t ks = synth_snp_key(seed, j);
+    const float tj = thr[j];
+    uint32_t byte = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int64_t i = qg * 4 + t;
+      uint32_t cnt = 0;
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        const uint64_t hh =
+            splitmix64(ks ^ (static_cast<uint64_t>(2 * i + a) * 0x9E3779B97F4A7C15ull));
+        const float e = q[hh >> 52];
+        x[2 * t + a] = (j == j0) ? e : __fadd_rn(__fmul_rn(r, x[2 * t + a]), __fmul_rn(sf, e));
+        cnt += x[2 * t + a] < tj ? 1u : 0u;
+      }
+      const uint32_t bed = cnt == 2 ? 0u : (cnt == 1 ? 2u : 3u);
+      if (i < n_rows) byte |= bed << (2 * t);
+    }
+    const int64_t rec = record_of_snp ? record_of_snp[j] : j;
+    out[rec * bps + qg] = static_cast<uint8_t>(byte);
+  }
+}
+
 // copy S from the synthetic generator.
 __global__ void k_build_s_synth(uint8_t* __restrict__ geno_s, int64_t n, int64_t n_pad,
                                 int64_t n_panels, const int32_t* __restrict__ snp_of_slot,
@@ -253,6 +306,44 @@ __global__ void k_slot_counts(const uint8_t* __restrict__ geno_t, int64_t m_pad,
   n1o[j] = a1;
   n2o[j] = a2;
   n3o[j] = a3;
+}
+
+// Sums of diff per slot: dseg[j, z] = s1_jz - cnt_jz mu_j over segment z
+// (chunks [64 z, 64 z + 64)) and dsum[j] = s1_j - cnt_j mu_j over all the
+// slot's samples, each in FP64 from integer counts, stored in FP32.
+// nseg[z] = samples of the slot in segment z.
+__global__ void k_slot_seg_dsum(const uint8_t* __restrict__ geno_t, int64_t m_pad,
+                                int64_t n_chunks, const uint32_t* __restrict__ tmask,
+                                const float* __restrict__ mean, const float* __restrict__ nseg,
+                                const int32_t* __restrict__ snp_of_slot, int n_seg,
+                                float* __restrict__ dseg, float* __restrict__ dsum) {
+  const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (j >= m_pad) return;
+  const int64_t tt = j / kTile;
+  const int row = static_cast<int>(j % kTile);
+  const bool pad = snp_of_slot[j] < 0;
+  const double mu = static_cast<double>(mean[j]);
+  double s1_all = 0.0, cnt_all = 0.0;
+  for (int z = 0; z < n_seg; ++z) {
+    int n1 = 0, n2 = 0, n3 = 0;
+    const int64_t q1 = min(n_chunks, static_cast<int64_t>(z + 1) * kSegChunks);
+    for (int64_t q = static_cast<int64_t>(z) * kSegChunks; q < q1; ++q) {
+      const uint4 v = *reinterpret_cast<const uint4*>(
+          geno_t + ((tt * n_chunks + q) * kTile + row) * kRowBytes);
+      uint4 mk = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+      if (tmask != nullptr) mk = reinterpret_cast<const uint4*>(tmask)[q];
+      count_codes(v.x, mk.x, n1, n2, n3);
+      count_codes(v.y, mk.y, n1, n2, n3);
+      count_codes(v.z, mk.z, n1, n2, n3);
+      count_codes(v.w, mk.w, n1, n2, n3);
+    }
+    const double cnt = static_cast<double>(nseg[z]) - static_cast<double>(n3);
+    const double s1 = static_cast<double>(n1 + 2 * n2);
+    dseg[j * n_seg + z] = pad ? 0.f : static_cast<float>(s1 - cnt * mu);
+    s1_all += s1;
+    cnt_all += cnt;
+  }
+  dsum[j] = pad ? 0.f : static_cast<float>(s1_all - cnt_all * mu);
 }
 
 // Reference FP32 standardisation of every slot (padding slots get 0, 0).
@@ -541,6 +632,20 @@ int compute_slot_stats(coherit_geno* h, StatsSlot& s, const float* override_mean
     CO_CUDA(cudaMemcpyAsync(s.inv, inv.data(), sizeof(float) * mp, cudaMemcpyHostToDevice, st));
     CO_CUDA(cudaStreamSynchronize(st));
   }
+  {
+    // Segment sums of diff over the slot's samples, exact in FP64 from the
+    // integer counts and the installed FP32 mean.  The operator's first
+    // contraction shifts V by its mean over each segment and adds
+    // sum_z shift_z * dsum_z back, so no large FP32 running sums occur for
+    // columns with an offset or a trend.
+    const int ns = static_cast<int>(n_segments(h->n_chunks));
+    k_slot_seg_dsum<<<grid_of(mp, 128), 128, 0, st>>>(h->geno_t, mp, h->n_chunks, s.tmask, s.mean,
+                                                      s.nseg, h->d_snp_of_slot, ns, s.dseg,
+                                                      s.dsum);
+    note_launch();
+    CO_CUDA(cudaGetLastError());
+    CO_CUDA(cudaStreamSynchronize(st));
+  }
   // Summaries: m_eff and mean-diagonal atoms per component (FP64 host sums).
   s.comp_eff.assign(h->G, 0.0);
   s.comp_atom.assign(h->G, 0.0);
@@ -657,17 +762,26 @@ static int init_slot(coherit_geno* h, int32_t slot, const uint8_t* sample_mask, 
   if (!s.used) {
     CO_CUDA(cudaMalloc(&s.mean, sizeof(float) * h->m_pad));
     CO_CUDA(cudaMalloc(&s.inv, sizeof(float) * h->m_pad));
+    const int64_t ns = n_segments(h->n_chunks);
+    CO_CUDA(cudaMalloc(&s.dsum, sizeof(float) * h->m_pad));
+    CO_CUDA(cudaMalloc(&s.dseg, sizeof(float) * h->m_pad * ns));
+    CO_CUDA(cudaMalloc(&s.nseg, sizeof(float) * ns));
     s.used = true;
   }
   if (s.row_mask) { cudaFree(s.row_mask); s.row_mask = nullptr; }
   if (s.tmask) { cudaFree(s.tmask); s.tmask = nullptr; }
   s.n_sub = h->n;
+  const int64_t seg_len = static_cast<int64_t>(kSegChunks) * kPanel;
+  std::vector<float> nseg(n_segments(h->n_chunks), 0.f);
+  if (sample_mask == nullptr)
+    for (int64_t i = 0; i < h->n; ++i) nseg[i / seg_len] += 1.f;
   if (sample_mask != nullptr) {
     std::vector<uint8_t> rm(h->n_pad, 0);
     int64_t cnt = 0;
     for (int64_t i = 0; i < h->n; ++i) {
       rm[i] = sample_mask[i] ? 1 : 0;
       cnt += rm[i];
+      nseg[i / seg_len] += rm[i];
     }
     CO_CHECK(cnt > 0, COHERIT_E_SHAPE, "sample_mask selects no samples");
     s.n_sub = cnt;
@@ -678,12 +792,19 @@ static int init_slot(coherit_geno* h, int32_t slot, const uint8_t* sample_mask, 
                                                              s.tmask); note_launch();
     CO_CUDA(cudaGetLastError());
   }
+  // Segment sample counts (exact integers in FP32: a segment holds 4,096).
+  CO_CUDA(cudaMemcpyAsync(s.nseg, nseg.data(), sizeof(float) * nseg.size(),
+                          cudaMemcpyHostToDevice, st));
+  CO_CUDA(cudaStreamSynchronize(st));
   return COHERIT_OK;
 }
 
 static void free_slot(StatsSlot& s) {
   if (s.mean) cudaFree(s.mean);
   if (s.inv) cudaFree(s.inv);
+  if (s.dsum) cudaFree(s.dsum);
+  if (s.dseg) cudaFree(s.dseg);
+  if (s.nseg) cudaFree(s.nseg);
   if (s.row_mask) cudaFree(s.row_mask);
   if (s.tmask) cudaFree(s.tmask);
   s = StatsSlot();
@@ -906,6 +1027,108 @@ int coherit_geno_create_bed(const uint8_t* bed, int64_t bed_bytes, int64_t n_ful
     cudaStreamSynchronize(st);
     cudaFree(d_keep);
   }
+  if (rc == COHERIT_OK) rc = finish_create(h, st);
+  if (rc != COHERIT_OK) { free_handle(h); return rc; }
+  *out = h;
+  return COHERIT_OK;
+}
+
+int coherit_ldblock_records(int64_t n_rows, int64_t m, int32_t block, uint64_t seed,
+                            const float* thresholds, const float* rho, const float* sfac,
+                            const float* quantiles, uint8_t* out, void* stream) {
+  CO_CHECK(n_rows > 0 && m > 0 && block > 0, COHERIT_E_SHAPE,
+           "LD-block records need n_rows > 0, m > 0 and block > 0");
+  CO_CHECK(thresholds && rho && sfac && quantiles && out, COHERIT_E_SHAPE,
+           "LD-block records need device tables and an output buffer");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int64_t bps = (n_rows + 3) / 4;
+  const int64_t work = bps * ((m + block - 1) / block);
+  k_ldblock_records<<<grid_of(work, 256), 256, 0, st>>>(out, n_rows, bps, m, block, seed,
+                                                        thresholds, rho, sfac, quantiles,
+                                                        nullptr); note_launch();
+  CO_CUDA(cudaGetLastError());
+  return COHERIT_OK;
+}
+
+int coherit_geno_create_ldblock(int64_t n, int64_t m, int32_t block, uint64_t seed,
+                                const float* thresholds, const float* rho, const float* sfac,
+                                const float* quantiles, const int64_t* cache_to_source,
+                                const int32_t* component_sizes, int32_t n_components, int device,
+                                void* stream, coherit_geno_t** out) {
+  CO_CHECK(out != nullptr, COHERIT_E_SHAPE, "out handle pointer is NULL");
+  *out = nullptr;
+  CO_CHECK(n > 0 && m > 0 && block > 0, COHERIT_E_SHAPE,
+           "LD-block genotypes need n > 0, m > 0 and block > 0");
+  CO_CHECK(n < (int64_t(1) << 31) && m < (int64_t(1) << 31), COHERIT_E_SHAPE,
+           "n and m must be below 2^31");
+  CO_CHECK(thresholds && rho && sfac && quantiles, COHERIT_E_SHAPE, "generator tables missing");
+  std::vector<int64_t> comp_m;
+  if (component_sizes == nullptr || n_components <= 1) {
+    comp_m.push_back(m);
+  } else {
+    int64_t tot = 0;
+    for (int g = 0; g < n_components; ++g) {
+      CO_CHECK(component_sizes[g] > 0, COHERIT_E_SHAPE, "component %d has no SNPs", g);
+      comp_m.push_back(component_sizes[g]);
+      tot += component_sizes[g];
+    }
+    CO_CHECK(tot == m, COHERIT_E_SHAPE, "component sizes sum to %lld, expected m=%lld",
+             (long long)tot, (long long)m);
+  }
+  // Record (= cache position) of every source SNP.
+  std::vector<int64_t> rec(m);
+  if (cache_to_source) {
+    std::vector<uint8_t> seen(m, 0);
+    for (int64_t c = 0; c < m; ++c) {
+      const int64_t j = cache_to_source[c];
+      CO_CHECK(j >= 0 && j < m && !seen[j], COHERIT_E_SHAPE,
+               "cache_to_source must be a permutation of 0..m-1");
+      seen[j] = 1;
+      rec[j] = c;
+    }
+  } else {
+    for (int64_t j = 0; j < m; ++j) rec[j] = j;
+  }
+  coherit_geno* h = new coherit_geno();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = alloc_common(h, n, comp_m, device);
+  if (rc != COHERIT_OK) { free_handle(h); return rc; }
+  const int64_t nb = (m + block - 1) / block;
+  const int64_t bps = (n + 3) / 4;
+  float *d_thr = nullptr, *d_rho = nullptr, *d_s = nullptr, *d_q = nullptr;
+  int64_t* d_rec = nullptr;
+  uint8_t* d_bed = nullptr;
+  cudaError_t e = cudaMalloc(&d_thr, sizeof(float) * m);
+  if (e == cudaSuccess) e = cudaMalloc(&d_rho, sizeof(float) * nb);
+  if (e == cudaSuccess) e = cudaMalloc(&d_s, sizeof(float) * nb);
+  if (e == cudaSuccess) e = cudaMalloc(&d_q, sizeof(float) * 4096);
+  if (e == cudaSuccess) e = cudaMalloc(&d_rec, sizeof(int64_t) * m);
+  if (e == cudaSuccess) e = cudaMalloc(&d_bed, static_cast<size_t>(m) * bps);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_thr, thresholds, sizeof(float) * m, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_rho, rho, sizeof(float) * nb, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_s, sfac, sizeof(float) * nb, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_q, quantiles, sizeof(float) * 4096, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_rec, rec.data(), sizeof(int64_t) * m, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    k_ldblock_records<<<grid_of(bps * nb, 256), 256, 0, st>>>(d_bed, n, bps, m, block, seed, d_thr,
+                                                             d_rho, d_s, d_q, d_rec); note_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->geno_s, 0, static_cast<size_t>(h->n_pad) * h->m_pad / 4, st);
+  if (e == cudaSuccess && h->n_panels > 0) {
+    k_build_s_from_bed<<<grid_of(n * h->n_panels, 256), 256, 0, st>>>(
+        h->geno_s, n, h->n_pad, h->n_panels, d_bed, bps, 0, m, nullptr, h->d_snp_of_slot, 0,
+        h->n_panels); note_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_thr); cudaFree(d_rho); cudaFree(d_s); cudaFree(d_q); cudaFree(d_rec); cudaFree(d_bed);
+  if (e != cudaSuccess) { free_handle(h); return cuda_status(e, "LD-block genotypes"); }
+  rc = build_copy_t(h, st);
   if (rc == COHERIT_OK) rc = finish_create(h, st);
   if (rc != COHERIT_OK) { free_handle(h); return rc; }
   *out = h;

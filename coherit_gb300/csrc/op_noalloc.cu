@@ -8,20 +8,23 @@
 // runs the same launches with the workspace in `g_scratch` below instead.
 //
 // Setup: the first call on each device, with that device current, resolves
-// the array's address with cudaGetSymbolAddress (this loads the module that
-// holds it and commits its 64 MiB) and caches it; later calls only read the
-// cache.  Make that first call before any stream capture begins.
+// the array's address with cudaGetSymbolAddress and caches it; later calls
+// only read the cache.  Make that first call before any stream capture
+// begins.  Under lazy module loading (the CUDA default) that first call loads
+// the module holding the array and commits its 64 MiB; with eager loading
+// (CUDA_MODULE_LOADING=EAGER) every context that loads this library commits
+// 64 MiB on each device it uses, whether or not this entry point is called.
 //
 // Limits: single request, tensor-core precisions; the workspace of one
 // launch (about 2*nsplit*kp*(n_pad + m_pad) bytes, plus 8*kp*m_pad with
 // missing genotypes, plus the split-K partials) must fit kScratchBytes, else
 // COHERIT_E_SHAPE.
 //
-// What must start at zero: only the FP64 rank-one accumulators, cleared by
-// the launch sequence on every call; every other region is written before it
-// is read.  Calls on one device share the array: calls issued on one stream
-// (or otherwise ordered) are safe, calls in flight at the same time on
-// different streams race on it.
+// What must start at zero: the FP64 rank-one accumulators and the FP16X2
+// column maxima, cleared by the launch sequence on every call; every other
+// region is written before it is read.  Calls on one device share the array:
+// calls issued on one stream (or otherwise ordered, e.g. with events) are
+// safe, calls in flight at the same time on different streams race on it.
 #include <mutex>
 
 #include "coherit_internal.cuh"

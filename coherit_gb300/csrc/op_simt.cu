@@ -8,13 +8,17 @@
 // launch.
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 #include "coherit_internal.cuh"
 
 namespace coherit {
 
-constexpr int kSimtCols = 32;  // columns per CTA
-constexpr int kSimtRows = 64;  // slots (K1) or samples (K2) per CTA
+// Tiles: COLS right-hand-side columns (8, 16 or 32, the narrowest that
+// holds the block's columns in few launches) x ROWS = 2048 / COLS slots (K1)
+// or samples (K2) per CTA of 256 threads; every thread owns one row and 8
+// columns.  Narrow PCG blocks then do no work for padding columns.
+constexpr int kSimtOut = 2048;  // outputs per CTA
 
 struct SimtParams {
   int64_t n, n_pad, m_pad, n_chunks, n_panels;
@@ -36,46 +40,69 @@ struct SimtParams {
   float* out;   // K2 output or X^T V output
 };
 
-// T block rows -> diff[sample r][slot jj] in shared memory.
+template <int COLS>
+constexpr int simt_rows() { return kSimtOut / COLS; }
+template <int COLS>
+constexpr size_t simt_smem() {
+  return sizeof(float) * (static_cast<size_t>(kPanel) * (simt_rows<COLS>() + 1) + kPanel * COLS +
+                          kPanel);
+}
+
+// K1: T = diff^T V for ROWS slots; the T block rows of a chunk are decoded to
+// diff[sample][slot] in shared memory (4 threads per slot row, one 32-bit
+// word = 16 samples each).
+template <int COLS>
 __global__ void __launch_bounds__(256) k_simt_k1(const __grid_constant__ SimtParams p) {
-  __shared__ float D[kPanel][kSimtRows + 1];
-  __shared__ float Vs[kPanel][kSimtCols];
+  constexpr int ROWS = simt_rows<COLS>();
+  extern __shared__ float sm[];
+  float* D = sm;                               // [64][ROWS + 1]
+  float* Vs = sm + kPanel * (ROWS + 1);        // [64][COLS]
   const int t = threadIdx.x;
-  const int64_t slot0 = static_cast<int64_t>(blockIdx.x) * kSimtRows;
-  const int c0 = blockIdx.y * kSimtCols;
-  const int64_t tt = slot0 / kTile;
-  const int rbase = static_cast<int>(slot0 % kTile);
-  const int jj = t % kSimtRows;
-  const int cg = t / kSimtRows;  // 0..3 -> 8 columns each
+  const int64_t slot0 = static_cast<int64_t>(blockIdx.x) * ROWS;
+  const int c0 = blockIdx.y * COLS;
+  const int jj = t % ROWS;
+  const int cg = t / ROWS;  // column group of 8
   float acc[8];
 #pragma unroll
   for (int u = 0; u < 8; ++u) acc[u] = 0.f;
-  // decode role: 4 threads per slot row, one 32-bit word (16 samples) each
-  const int drow = t / 4, dword = t % 4;
-  const float mu = p.mean[slot0 + drow];
-  for (int64_t q = 0; q < p.n_chunks; ++q) {
-    const uint32_t w = reinterpret_cast<const uint32_t*>(
-        p.geno_t + ((tt * p.n_chunks + q) * kTile + rbase + drow) * kRowBytes)[dword];
+  constexpr int kWords = 4 * ROWS / 256;  // decode words per thread and chunk
+  float mu[kWords];
+  const uint8_t* rowp[kWords];
 #pragma unroll
-    for (int r = 0; r < 16; ++r) {
-      const int e = dword * 16 + r;
-      const uint32_t code = (w >> row_shift(e)) & 3u;
-      D[e][drow] = code == 3u ? 0.f : (static_cast<float>(code) - mu);
+  for (int x = 0; x < kWords; ++x) {
+    const int widx = t + 256 * x;
+    const int64_t slot = slot0 + widx / 4;
+    mu[x] = p.mean[slot];
+    rowp[x] = p.geno_t + ((slot / kTile) * p.n_chunks * kTile + slot % kTile) * kRowBytes +
+              4 * (widx % 4);
+  }
+  for (int64_t q = 0; q < p.n_chunks; ++q) {
+#pragma unroll
+    for (int x = 0; x < kWords; ++x) {
+      const int widx = t + 256 * x;
+      const int drow = widx / 4, dword = widx % 4;
+      const uint32_t w = *reinterpret_cast<const uint32_t*>(rowp[x] + q * kTile * kRowBytes);
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        const int e = dword * 16 + r;
+        const uint32_t code = (w >> row_shift(e)) & 3u;
+        D[e * (ROWS + 1) + drow] = code == 3u ? 0.f : (static_cast<float>(code) - mu[x]);
+      }
     }
-    for (int idx = t; idx < kPanel * kSimtCols; idx += 256) {
-      const int r = idx / kSimtCols, c = idx % kSimtCols;
+    for (int idx = t; idx < kPanel * COLS; idx += 256) {
+      const int r = idx / COLS, c = idx % COLS;
       const int64_t i = q * kPanel + r;
       float v = 0.f;
       if (i < p.n && c0 + c < p.k && (p.mask == nullptr || p.mask[i] != 0))
         v = p.V[i * p.ldv + c0 + c];
-      Vs[r][c] = v;
+      Vs[r * COLS + c] = v;
     }
     __syncthreads();
 #pragma unroll 8
     for (int r = 0; r < kPanel; ++r) {
-      const float d = D[r][jj];
+      const float d = D[r * (ROWS + 1) + jj];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) acc[u] = fmaf(d, Vs[r][cg * 8 + u], acc[u]);
+      for (int u = 0; u < 8; ++u) acc[u] = fmaf(d, Vs[r * COLS + cg * 8 + u], acc[u]);
     }
     __syncthreads();
   }
@@ -97,48 +124,63 @@ __global__ void __launch_bounds__(256) k_simt_k1(const __grid_constant__ SimtPar
   }
 }
 
+// K2: out = diff S for ROWS samples; the S block rows of a panel are decoded
+// to diff[slot][sample] in shared memory.
+template <int COLS>
 __global__ void __launch_bounds__(256) k_simt_k2(const __grid_constant__ SimtParams p) {
-  __shared__ float D[kPanel][kSimtRows + 1];  // [slot jj][sample r]
-  __shared__ float Ss[kPanel][kSimtCols];
-  __shared__ float mus[kPanel];
+  constexpr int ROWS = simt_rows<COLS>();
+  extern __shared__ float sm[];
+  float* D = sm;                          // [64 slots][ROWS + 1]
+  float* Ss = sm + kPanel * (ROWS + 1);   // [64][COLS]
+  float* mus = Ss + kPanel * COLS;        // [64]
   const int t = threadIdx.x;
-  const int64_t i0 = static_cast<int64_t>(blockIdx.x) * kSimtRows;
-  const int c0 = blockIdx.y * kSimtCols;
+  const int64_t i0 = static_cast<int64_t>(blockIdx.x) * ROWS;
+  const int c0 = blockIdx.y * COLS;
   const int comp = blockIdx.z;
-  const int64_t st = i0 / kTile;
-  const int rbase = static_cast<int>(i0 % kTile);
   int64_t p0 = 0, p1 = p.n_panels;
   if (p.stacked) {
     p0 = p.comp_slot_start[comp] / kPanel;
     p1 = p.comp_slot_start[comp + 1] / kPanel;
   }
-  const int r_own = t % kSimtRows;
-  const int cg = t / kSimtRows;
+  const int r_own = t % ROWS;
+  const int cg = t / ROWS;
   float acc[8];
 #pragma unroll
   for (int u = 0; u < 8; ++u) acc[u] = 0.f;
-  const int drow = t / 4, dword = t % 4;
+  constexpr int kWords = 4 * ROWS / 256;
+  const uint8_t* rowp[kWords];
+#pragma unroll
+  for (int x = 0; x < kWords; ++x) {
+    const int widx = t + 256 * x;
+    const int64_t i = i0 + widx / 4;
+    rowp[x] = p.geno_s + ((i / kTile) * p.n_panels * kTile + i % kTile) * kRowBytes +
+              4 * (widx % 4);
+  }
   for (int64_t pn = p0; pn < p1; ++pn) {
     if (t < kPanel) mus[t] = p.mean[pn * kPanel + t];
     __syncthreads();
-    const uint32_t w = reinterpret_cast<const uint32_t*>(
-        p.geno_s + ((st * p.n_panels + pn) * kTile + rbase + drow) * kRowBytes)[dword];
 #pragma unroll
-    for (int r = 0; r < 16; ++r) {
-      const int e = dword * 16 + r;
-      const uint32_t code = (w >> row_shift(e)) & 3u;
-      D[e][drow] = code == 3u ? 0.f : (static_cast<float>(code) - mus[e]);
+    for (int x = 0; x < kWords; ++x) {
+      const int widx = t + 256 * x;
+      const int drow = widx / 4, dword = widx % 4;
+      const uint32_t w = *reinterpret_cast<const uint32_t*>(rowp[x] + pn * kTile * kRowBytes);
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        const int e = dword * 16 + r;
+        const uint32_t code = (w >> row_shift(e)) & 3u;
+        D[e * (ROWS + 1) + drow] = code == 3u ? 0.f : (static_cast<float>(code) - mus[e]);
+      }
     }
-    for (int idx = t; idx < kPanel * kSimtCols; idx += 256) {
-      const int r = idx / kSimtCols, c = idx % kSimtCols;
-      Ss[r][c] = (c0 + c < p.kp) ? p.sf[(pn * kPanel + r) * p.kp + c0 + c] : 0.f;
+    for (int idx = t; idx < kPanel * COLS; idx += 256) {
+      const int r = idx / COLS, c = idx % COLS;
+      Ss[r * COLS + c] = (c0 + c < p.kp) ? p.sf[(pn * kPanel + r) * p.kp + c0 + c] : 0.f;
     }
     __syncthreads();
 #pragma unroll 8
     for (int e = 0; e < kPanel; ++e) {
-      const float d = D[e][r_own];
+      const float d = D[e * (ROWS + 1) + r_own];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) acc[u] = fmaf(d, Ss[e][cg * 8 + u], acc[u]);
+      for (int u = 0; u < 8; ++u) acc[u] = fmaf(d, Ss[e * COLS + cg * 8 + u], acc[u]);
     }
     __syncthreads();
   }
@@ -209,19 +251,37 @@ int run_operator_fp32(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
   p.out = d.out;
   // S in FP32 (m_pad x kp) at the start of the workspace.
   p.sf = static_cast<float*>(h->ws.base);
-  const unsigned cblocks = static_cast<unsigned>((kp + kSimtCols - 1) / kSimtCols);
   if (d.zxb) {
     k_simt_prep_b<<<static_cast<unsigned>((h->m_pad + 127) / 128), 128, 0, st>>>(p, d.V, d.ldv); note_launch();
     p.use_theta_e = 0;
-  } else {
-    k_simt_k1<<<dim3(static_cast<unsigned>(h->m_pad / kSimtRows), cblocks), 256, 0, st>>>(p); note_launch();
+    CO_CUDA(cudaGetLastError());
   }
-  CO_CUDA(cudaGetLastError());
-  if (d.xtv) return COHERIT_OK;
-  const unsigned nz = p.stacked ? static_cast<unsigned>(h->G) : 1u;
-  k_simt_k2<<<dim3(static_cast<unsigned>(h->n_pad / kSimtRows), cblocks, nz), 256, 0, st>>>(p); note_launch();
-  CO_CUDA(cudaGetLastError());
-  return COHERIT_OK;
+  // Narrowest tile that holds the block (kp is a multiple of 16; 8 only for
+  // one-column blocks padded to 16 would waste half the CTA).
+  const int cols = kp <= 16 ? 16 : 32;
+  auto run = [&](auto cols_tag) -> int {
+    constexpr int COLS = decltype(cols_tag)::value;
+    constexpr int ROWS = simt_rows<COLS>();
+    const unsigned cblocks = static_cast<unsigned>((kp + COLS - 1) / COLS);
+    const size_t smem = simt_smem<COLS>();
+    if (!d.zxb) {
+      CO_CUDA(cudaFuncSetAttribute(k_simt_k1<COLS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(smem)));
+      k_simt_k1<COLS><<<dim3(static_cast<unsigned>(h->m_pad / ROWS), cblocks), 256, smem, st>>>(p);
+      note_launch();
+      CO_CUDA(cudaGetLastError());
+    }
+    if (d.xtv) return COHERIT_OK;
+    const unsigned nz = p.stacked ? static_cast<unsigned>(h->G) : 1u;
+    CO_CUDA(cudaFuncSetAttribute(k_simt_k2<COLS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem)));
+    k_simt_k2<COLS><<<dim3(static_cast<unsigned>(h->n_pad / ROWS), cblocks, nz), 256, smem, st>>>(p);
+    note_launch();
+    CO_CUDA(cudaGetLastError());
+    return COHERIT_OK;
+  };
+  if (cols == 16) return run(std::integral_constant<int, 16>());
+  return run(std::integral_constant<int, 32>());
 }
 
 }  // namespace coherit

@@ -4,8 +4,16 @@
 // the resident 2-bit genotypes (kv_impl.py:94-113 computes the same pair per
 // call block, with diff materialised in FP32):
 //
-//   K1 (slot tiles of 128 SNPs):  T = G0^T V            (K = samples)
-//       epilogue  S_j = w_j (T_j - mu_j 1^T V + mu_j sum_{i missing} V_i)
+//   K1 (slot tiles of 128 SNPs):  T = G0^T V'           (K = samples)
+//       V' = V - a_z is V shifted by its column means a_z over the request's
+//       samples in each segment z of 4,096 samples, so the FP32 accumulator
+//       never carries the running sum of an offset or a trend; the shift comes
+//       back through the sums of diff over all samples (dsum_j, zero up to
+//       the rounding of mu_j) and over each segment (dseg_jz), with a_z
+//       written as the column mean abar plus d_z = a_z - abar so that a
+//       constant column (d_z = 0) needs only the exact dsum_j:
+//       epilogue  S_j = w_j (T_j - mu_j 1^T V' + mu_j sum_{i missing} V'_i
+//                            + abar dsum_j + sum_z d_z dseg_jz)
 //                 w_j = inv_sd_j^2 * s_g(j) [* snp weight]
 //                 S is split into BF16 terms in the B-tile layout of K2 and
 //                 r = sum_j mu_j S_j is accumulated in FP64.
@@ -31,7 +39,7 @@ namespace coherit {
 // Pipeline configurations of the tensor-core operator, chosen per launch:
 //  * StageCfg<2, 3> ("narrow"): stages of 2 blocks (K = 128), 3 decoder warp
 //    sets, a 9-deep genotype ring, an A ring of 3..6 slots of 64 columns;
-//    two CTAs per SM for blocks of <= 16 columns, one CTA otherwise.
+//    one CTA per SM.
 //  * StageCfg<4, 2> ("wide"): stages of 4 blocks (K = 256), 2 decoder sets,
 //    an 8-deep genotype ring, an A ring of 2..3 slots of 128 columns; half
 //    the barrier round trips per K of the narrow form (at n = 50,000,
@@ -48,13 +56,19 @@ struct StageCfg {
   static constexpr int SETS = SETS_;    // decoder warp sets
   static constexpr int RG = SETS_ == 3 ? 9 : 8;  // genotype ring depth
   static constexpr int MIN_RA = SETS_ >= 3 ? 3 : SETS_;
-  static constexpr int THREADS = 32 * (3 + 4 * SETS_);
+  // Whole warpgroups: warps 0-2 copy genotypes / issue MMAs / copy B tiles,
+  // warp 3 idles, warps 4.. decode.  A warp reaches only the tensor-memory
+  // lanes of its SM sub-partition, which follows the hardware warp slot; a
+  // CTA of whole warpgroups keeps threadIdx-derived warp % 4 equal to that
+  // sub-partition even when a second CTA shares the SM.
+  static constexpr int THREADS = 32 * (4 + 4 * SETS_);
   static_assert(RG % SETS_ == 0, "genotype ring depth must be a multiple of the decoder sets");
   static_assert(SB_ <= kMaxStageBlocks, "stage larger than the layout padding");
 };
 using CfgNarrow = StageCfg<2, 3>;
 using CfgWide = StageCfg<4, 2>;
-constexpr int kWarpG = 0, kWarpMMA = 1, kWarpB = 2, kWarpDec0 = 3;
+constexpr int kWarpG = 0, kWarpMMA = 1, kWarpB = 2, kWarpIdle = 3, kWarpDec0 = 4;
+static_assert(kWarpDec0 % 4 == 0, "decoder sets must start on a warpgroup boundary");
 // Tensor-memory A ring depth limit.  Depths up to 6 (64-column slots) are
 // the configurations exercised on GB300; a 7-slot ring with a 64-column
 // accumulator raised an illegal-instruction fault whose cause was not found,
@@ -67,20 +81,31 @@ constexpr int kBarrierBytes = 1024;
 
 struct EpiParams {
   int n_groups, G, k, kp, nsplit, stacked, xtv, use_theta_e;
+  int f16;  // FP16X2: V' and S carry per-column power-of-two scales
   int64_t n, m_pad, ldv, ldo;
   int32_t col_start[kMaxGroups + 1];
   const float* gmean[kMaxGroups];
   const float* ginv[kMaxGroups];
+  const float* gdsum[kMaxGroups];  // m_pad sums of diff over the group slot's samples
+  const float* gdseg[kMaxGroups];  // m_pad x n_seg segment sums of diff
+  const float* gnseg[kMaxGroups];  // n_seg samples per segment of the group's slot
+  int n_seg;                       // centring segments
   const uint8_t* gmask[kMaxGroups];
   float cscale[kMaxScale];
   float theta_e[kMaxGroups];
   const int32_t* comp_of_slot;
   const int32_t* snp_of_slot;
   const float* snpw;   // cache order or nullptr
-  const float* cs;     // kp column sums of V
-  const float* vmiss;  // m_pad x kp or nullptr
-  __nv_bfloat16* sbuf; // K1 output: S split tiles
-  float* sf32;         // m_pad x kp or nullptr
+  // (2 n_seg + 1) x kp: rows [0, n_seg) the segment means a_z of V over the
+  // group's samples, row n_seg the column mean abar, rows n_seg + 1 + z the
+  // deviations d_z = a_z - abar.
+  const float* shift;
+  const float* vscale; // kp: power-of-two scale of V' in K1's B tiles (1 unless f16)
+  unsigned* smax;      // kp: max |S| per column (float bits), f16 only
+  const float* cs;     // kp column sums of the shifted V
+  const float* vmiss;  // m_pad x kp (shifted V over missing genotypes) or nullptr
+  __nv_bfloat16* sbuf; // K1 output: S split tiles (16-bit terms, BF16 or FP16 bits)
+  float* sf32;         // m_pad x kp FP32 S (missing genotypes or f16), else nullptr
   double* rbuf;        // (stacked ? G : 1) x kp
   float* xout;         // X^T V output (m x ldo) when xtv
   const float* V;      // K2: residual term
@@ -120,10 +145,13 @@ __device__ __forceinline__ int group_of(const EpiParams& e, int c) {
 // L = {0x00, 0x80, 0x00, 0x00}, H = {0x00, 0x3F, 0x40, 0x00}, i.e. the low and
 // high bytes of bf16(0), bf16(1), bf16(2) and bf16(0) for code 3 (missing).
 // 16 bytes = 64 codes -> 32 words of BF16 pairs in K order (word t =
-// elements 2t, 2t+1).
+// elements 2t, 2t+1).  With F16 the table holds the FP16 bytes instead:
+// L = {0, 0, 0, 0}, H = {0x00, 0x3C, 0x40, 0x00} (fp16(1) = 0x3C00,
+// fp16(2) = 0x4000).
+template <bool F16>
 __device__ __forceinline__ void decode_row(const uint4 raw, uint32_t (&a)[32]) {
-  const uint32_t L = 0x00008000u;
-  const uint32_t H = 0x00403F00u;
+  const uint32_t L = F16 ? 0u : 0x00008000u;
+  const uint32_t H = F16 ? 0x00403C00u : 0x00403F00u;
   const uint32_t ws[4] = {raw.x, raw.y, raw.z, raw.w};
 #pragma unroll
   for (int w = 0; w < 4; ++w) {
@@ -146,14 +174,33 @@ __device__ __forceinline__ void split3(float v, __nv_bfloat16& hi, __nv_bfloat16
   lo = __float2bfloat16_rn(r2);
 }
 
+// Two FP16 terms of v (already scaled into FP16's range): hi + lo carries
+// 22 significant bits.
+__device__ __forceinline__ void split2h(float v, __half& hi, __half& lo) {
+  hi = __float2half_rn(v);
+  lo = __float2half_rn(v - __half2float(hi));
+}
+
+// Power-of-two scale that maps a column whose largest magnitude is `mx` into
+// [2^13, 2^14): the FP16 terms then stay normal and far below 65504.  Zero or
+// non-finite maxima give 1.
+__device__ __forceinline__ float pow2_scale(float mx) {
+  if (!(mx > 0.f) || !isfinite(mx)) return 1.f;
+  int ex;
+  frexpf(mx, &ex);  // mx = f 2^ex, f in [0.5, 1)
+  const int e = max(-100, min(100, 14 - ex));
+  return ldexpf(1.f, e);
+}
+
 // Offset (elements) of (column c, K index kk) inside one split term of a B
 // tile: K-major canonical layout, core matrices of 8 columns x 8 K values.
 __host__ __device__ __forceinline__ int64_t btile_off(int c, int kk) {
   return ((c >> 3) * 8 + (kk >> 3)) * 64 + (c & 7) * 8 + (kk & 7);
 }
 
-// K1 epilogue for one 16-column chunk of slot j: S = w (T - mu 1^T V + mu vmiss)
-// split into BF16 terms (K2's B tiles), r += mu S; or the X^T V output.
+// K1 epilogue for one 16-column chunk of slot j:
+// S = w (T - mu 1^T V' + mu vmiss' + a dsum) split into BF16 terms (K2's B
+// tiles), r += mu S; or the X^T V output.
 __device__ __forceinline__ void epilogue_k1(const EpiParams& e, int64_t j, int c0,
                                             const float (&T)[16], int lane) {
   const int g = e.comp_of_slot[j];
@@ -166,6 +213,20 @@ __device__ __forceinline__ void epilogue_k1(const EpiParams& e, int64_t j, int c
   const int g0 = __shfl_sync(0xffffffffu, gi, 0);
   const bool uniform = __all_sync(0xffffffffu, gi == g0);
   const int64_t term = static_cast<int64_t>(e.kp) * kPanel;
+  // abar dsum_j + sum_z d_z dseg_jz for the 16 columns (shifts are 0 beyond k).
+  float seg[16];
+  const float* dev_rows = e.shift + static_cast<int64_t>(e.n_seg + 1) * e.kp;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    seg[i] = 0.f;
+    const int c = c0 + i;
+    if (c >= e.k) continue;
+    const int grp = group_of(e, c);
+    const float* ds = e.gdseg[grp] + j * e.n_seg;
+    float acc = 0.f;
+    for (int z = 0; z < e.n_seg; ++z) acc = fmaf(dev_rows[z * e.kp + c], ds[z], acc);
+    seg[i] = fmaf(e.shift[e.n_seg * e.kp + c], e.gdsum[grp][j], acc);
+  }
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
     const int c = c0 + i;
@@ -175,12 +236,24 @@ __device__ __forceinline__ void epilogue_k1(const EpiParams& e, int64_t j, int c
       mu = e.gmean[grp][j];
       const float iv = e.ginv[grp][j];
       const float w = (e.xtv ? iv : iv * iv) * e.cscale[grp * e.G + g] * wsnp;
-      float corr = mu * e.cs[c];
+      float corr = mu * e.cs[c] - seg[i];
       if (e.vmiss != nullptr) corr -= mu * e.vmiss[j * e.kp + c];
-      sval = w * (T[i] - corr);
+      // The B tiles held V' * vscale (a power of two): undo it exactly.
+      sval = w * (T[i] * (1.f / e.vscale[c]) - corr);
     }
     if (e.xtv) {
       if (snp >= 0 && c < e.k) e.xout[static_cast<int64_t>(snp) * e.ldo + c] = sval;
+      continue;
+    }
+    if (e.f16) {
+      // FP16 terms need the column's largest |S| first: keep S in FP32 and
+      // its maximum (float bits order like unsigned for |S|; NaN wins);
+      // k_split_s writes the B tiles and r afterwards.
+      if (c < e.k) e.sf32[j * e.kp + c] = sval;
+      unsigned u = __float_as_uint(fabsf(sval));
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) u = max(u, __shfl_xor_sync(0xffffffffu, u, off));
+      if (lane == 0 && c < e.k) atomicMax(&e.smax[c], u);
       continue;
     }
     const int64_t base = pnl * (e.nsplit * term) + btile_off(c, kk);
@@ -213,7 +286,9 @@ __device__ __forceinline__ void epilogue_k2(const EpiParams& e, int64_t i, int c
     const int c = c0 + t;
     if (c >= e.k) break;
     const int grp = group_of(e, c);
-    float v = T[t] - static_cast<float>(e.rbuf[gi * e.kp + c]);
+    float acc = T[t];
+    if (e.f16) acc *= 1.f / pow2_scale(__uint_as_float(e.smax[c]));
+    float v = acc - static_cast<float>(e.rbuf[gi * e.kp + c]);
     if (e.use_theta_e) v += e.theta_e[grp] * e.V[i * e.ldv + c];
     if (e.gmask[grp] != nullptr && e.gmask[grp][i] == 0) v = 0.f;
     outb[i * e.ldo + c] = v;
@@ -268,11 +343,16 @@ __global__ void __launch_bounds__(128) k_k2_finish(const float* __restrict__ par
 
 // ------------------------------------------------------------ helper kernels
 
-// V (n x k, fp32) -> split BF16 B tiles for K1 + per-chunk FP64 column sums.
-// Rows outside a request's sample subset are read as zero.
+// V (n x k, fp32) -> per-chunk FP64 column sums of V (SPLIT = false), or of
+// the shifted V' = V - a (SPLIT = true) together with V' split into BF16 B
+// tiles for K1.  Rows outside a request's sample subset are read as zero
+// (and are not shifted).
+// Pass 1 also writes the per-chunk column maxima of |V| to mx_part (f16).
+// Pass 2 splits V' * vscale into three BF16 or two FP16 terms.
+template <bool SPLIT>
 __global__ void k_prep_v(const float* __restrict__ V, int64_t ldv, int64_t n, int k, int kp,
                          int nsplit, __nv_bfloat16* __restrict__ vt, double* __restrict__ cs_part,
-                         const __grid_constant__ EpiParams e) {
+                         float* __restrict__ mx_part, const __grid_constant__ EpiParams e) {
   extern __shared__ float tile[];  // [64][kp + 1]
   const int64_t q = blockIdx.x;
   const int ld = kp + 1;
@@ -282,16 +362,23 @@ __global__ void k_prep_v(const float* __restrict__ V, int64_t ldv, int64_t n, in
     float v = 0.f;
     if (i < n && c < k) {
       const uint8_t* mk = e.gmask[group_of(e, c)];
-      if (mk == nullptr || mk[i] != 0) v = V[i * ldv + c];
+      if (mk == nullptr || mk[i] != 0)
+        v = SPLIT ? V[i * ldv + c] - e.shift[(q / kSegChunks) * kp + c] : V[i * ldv + c];
     }
     tile[r * ld + c] = v;
   }
   __syncthreads();
   for (int c = threadIdx.x; c < kp; c += blockDim.x) {
     double s = 0.0;
-    for (int r = 0; r < kPanel; ++r) s += static_cast<double>(tile[r * ld + c]);
+    float mx = 0.f;
+    for (int r = 0; r < kPanel; ++r) {
+      s += static_cast<double>(tile[r * ld + c]);
+      mx = fmaxf(mx, fabsf(tile[r * ld + c]));
+    }
     cs_part[q * kp + c] = s;
+    if (!SPLIT && mx_part != nullptr) mx_part[q * kp + c] = mx;
   }
+  if (!SPLIT) return;
   const int cg_n = kp / 8;
   const int64_t chunk_elems = static_cast<int64_t>(nsplit) * kp * kPanel;
   for (int idx = threadIdx.x; idx < chunk_elems; idx += blockDim.x) {
@@ -299,9 +386,15 @@ __global__ void k_prep_v(const float* __restrict__ V, int64_t ldv, int64_t n, in
     const int rest = idx >> 9;
     const int cg = rest % cg_n, t = rest / cg_n;
     const int c = cg * 8 + cr, kk = kg * 8 + kr;
-    __nv_bfloat16 hi, mid, lo;
-    split3(tile[kk * ld + c], hi, mid, lo);
-    vt[q * chunk_elems + idx] = t == 0 ? hi : (t == 1 ? mid : lo);
+    if (e.f16) {
+      __half hi, lo;
+      split2h(tile[kk * ld + c] * e.vscale[c], hi, lo);
+      reinterpret_cast<__half*>(vt)[q * chunk_elems + idx] = t == 0 ? hi : lo;
+    } else {
+      __nv_bfloat16 hi, mid, lo;
+      split3(tile[kk * ld + c], hi, mid, lo);
+      vt[q * chunk_elems + idx] = t == 0 ? hi : (t == 1 ? mid : lo);
+    }
   }
 }
 
@@ -322,7 +415,80 @@ __global__ void __launch_bounds__(256) k_colsum_finish(const double* __restrict_
   if (threadIdx.x == 0) cs[c] = static_cast<float>(red[0]);
 }
 
-// vmiss[j, c] = sum over samples i with a missing genotype at slot j of V[i, c].
+// Segment shifts: a_zc = (sum of column c over its group's samples in
+// segment z) / those samples, rounded to FP32 (any FP32 value is exact for
+// the identity the K1 epilogue uses; the local mean keeps the shifted column
+// and its running sums small).  One CTA per column; each segment's chunk
+// partials are added in chunk order.
+// With f16 it also sets vscale_c = pow2_scale(max |V_c| + max_z |a_zc|), a
+// bound on max |V'_c|, so that V' * vscale fits FP16's range.
+__global__ void __launch_bounds__(256) k_shift_finish(const double* __restrict__ cs_part,
+                                                      const float* __restrict__ mx_part,
+                                                      int64_t n_parts, int kp,
+                                                      float* __restrict__ shift,
+                                                      float* __restrict__ vscale,
+                                                      const __grid_constant__ EpiParams e) {
+  __shared__ float redm[256];
+  __shared__ double red[256];
+  __shared__ double redn[256];
+  const int c = blockIdx.x;
+  const float* nseg = c < e.k ? e.gnseg[group_of(e, c)] : nullptr;
+  // Column total and sample count (fixed-order tree), then abar.
+  double tot = 0.0, cnt = 0.0;
+  for (int z = threadIdx.x; z < e.n_seg; z += 256) {
+    const int64_t q1 = min(n_parts, static_cast<int64_t>(z + 1) * kSegChunks);
+    for (int64_t q = static_cast<int64_t>(z) * kSegChunks; q < q1; ++q) tot += cs_part[q * kp + c];
+    if (nseg != nullptr) cnt += static_cast<double>(nseg[z]);
+  }
+  red[threadIdx.x] = tot;
+  redn[threadIdx.x] = cnt;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      red[threadIdx.x] += red[threadIdx.x + w];
+      redn[threadIdx.x] += redn[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  const float abar = redn[0] > 0.0 ? static_cast<float>(red[0] / redn[0]) : 0.f;
+  if (threadIdx.x == 0) shift[static_cast<int64_t>(e.n_seg) * kp + c] = abar;
+  float mx = fabsf(abar);
+  for (int z = threadIdx.x; z < e.n_seg; z += 256) {
+    double s = 0.0;
+    const int64_t q1 = min(n_parts, static_cast<int64_t>(z + 1) * kSegChunks);
+    for (int64_t q = static_cast<int64_t>(z) * kSegChunks; q < q1; ++q) s += cs_part[q * kp + c];
+    float a = abar;
+    if (nseg != nullptr && nseg[z] > 0.f) a = static_cast<float>(s / static_cast<double>(nseg[z]));
+    if (nseg == nullptr) a = 0.f;
+    shift[z * kp + c] = a;
+    shift[(static_cast<int64_t>(e.n_seg) + 1 + z) * kp + c] = a - abar;
+    mx = fmaxf(mx, fabsf(a));
+  }
+  if (e.f16) {
+    float vm = 0.f;
+    for (int64_t q = threadIdx.x; q < n_parts; q += 256) vm = fmaxf(vm, mx_part[q * kp + c]);
+    redm[threadIdx.x] = vm;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (threadIdx.x < w) redm[threadIdx.x] = fmaxf(redm[threadIdx.x], redm[threadIdx.x + w]);
+      __syncthreads();
+    }
+    const float vmax = redm[0];
+    __syncthreads();
+    redm[threadIdx.x] = mx;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (threadIdx.x < w) redm[threadIdx.x] = fmaxf(redm[threadIdx.x], redm[threadIdx.x + w]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) vscale[c] = pow2_scale(vmax + redm[0]);
+  } else if (threadIdx.x == 0) {
+    vscale[c] = 1.f;
+  }
+}
+
+// vmiss[j, c] = sum over samples i with a missing genotype at slot j of the
+// shifted V'[i, c] = V[i, c] - a_c.
 __global__ void k_vmiss(const int64_t* __restrict__ off, const int32_t* __restrict__ idx,
                         int64_t m_pad, const float* __restrict__ V, int64_t ldv, int64_t n, int k,
                         int kp, float* __restrict__ vmiss, const __grid_constant__ EpiParams e) {
@@ -335,7 +501,9 @@ __global__ void k_vmiss(const int64_t* __restrict__ off, const int32_t* __restri
       const uint8_t* mk = e.gmask[group_of(e, c)];
       for (int64_t t = off[j]; t < off[j + 1]; ++t) {
         const int64_t i = idx[t];
-        if (i < n && (mk == nullptr || mk[i] != 0)) s += static_cast<double>(V[i * ldv + c]);
+        if (i < n && (mk == nullptr || mk[i] != 0))
+          s += static_cast<double>(V[i * ldv + c] -
+                                   e.shift[(i / (kSegChunks * kPanel)) * kp + c]);
       }
     }
     vmiss[j * kp + c] = static_cast<float>(s);
@@ -377,6 +545,15 @@ __global__ void k_prep_s_from_b(const float* __restrict__ b, int64_t ldb,
   for (int c = 0; c < e.kp; ++c) {
     float sval = 0.f;
     if (c < e.k && snp >= 0) sval = iv * b[static_cast<int64_t>(snp) * ldb + c];
+    if (e.f16) {
+      // FP32 S and its column maximum; k_split_s forms the FP16 tiles and r.
+      if (active && c < e.k) e.sf32[j * e.kp + c] = sval;
+      unsigned u = __float_as_uint(fabsf(sval));
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) u = max(u, __shfl_xor_sync(0xffffffffu, u, off));
+      if (lane == 0 && c < e.k) atomicMax(&e.smax[c], u);
+      continue;
+    }
     if (active) {
       const int64_t base =
           pnl * (static_cast<int64_t>(e.nsplit) * e.kp * kPanel) + btile_off(c, kk);
@@ -392,6 +569,49 @@ __global__ void k_prep_s_from_b(const float* __restrict__ b, int64_t ldb,
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
       if (lane == 0 && v != 0.0) atomicAdd(&e.rbuf[c], v);
+    }
+  }
+}
+
+// FP16X2: S (FP32, m_pad x kp) -> K2's B tiles of S * tau_c in two FP16
+// terms, tau_c = pow2_scale(max_j |S_jc|), and r = sum_j mu_j S_j in FP64
+// (per component when stacked).  One thread per slot; a warp's 32 slots lie
+// in one component (components start on multiples of 256 slots), checked
+// before the warp reduction.
+__global__ void k_split_s(const __grid_constant__ EpiParams e) {
+  const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const bool active = j < e.m_pad;
+  const int lane = threadIdx.x & 31;
+  const int g = active ? e.comp_of_slot[j] : 0;
+  const int gi = e.stacked ? g : 0;
+  const int g0 = __shfl_sync(0xffffffffu, gi, 0);
+  const bool uniform = __all_sync(0xffffffffu, gi == g0);
+  const int64_t pnl = j / kPanel;
+  const int kk = static_cast<int>(j % kPanel);
+  const int64_t term = static_cast<int64_t>(e.kp) * kPanel;
+  __half* sb = reinterpret_cast<__half*>(e.sbuf);
+  for (int c = 0; c < e.kp; ++c) {
+    float sval = 0.f, mu = 0.f;
+    if (active && c < e.k) {
+      sval = e.sf32[j * e.kp + c];
+      mu = e.gmean[group_of(e, c)][j];
+    }
+    if (active) {
+      const float tau = c < e.k ? pow2_scale(__uint_as_float(e.smax[c])) : 1.f;
+      __half hi, lo;
+      split2h(sval * tau, hi, lo);
+      const int64_t base = pnl * (2 * term) + btile_off(c, kk);
+      sb[base] = hi;
+      sb[base + term] = lo;
+    }
+    if (c >= e.k) continue;
+    double v = static_cast<double>(mu) * static_cast<double>(sval);
+    if (uniform) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      if (lane == 0 && v != 0.0) atomicAdd(&e.rbuf[gi * e.kp + c], v);
+    } else if (v != 0.0) {
+      atomicAdd(&e.rbuf[gi * e.kp + c], v);
     }
   }
 }
@@ -457,7 +677,7 @@ static SplitPlan split_plan(const coherit_geno* h, bool stacked, int64_t target_
 static int64_t target_ctas(const coherit_geno* h) { return 4LL * std::max(h->sm_count, 1); }
 
 struct WsLayout {
-  size_t vt, sbuf, cs_part, cs, rbuf, vmiss, sf32, part, total;
+  size_t vt, sbuf, cs_part, mx_part, cs, shift, vscale, smax, rbuf, vmiss, sf32, part, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
@@ -476,7 +696,7 @@ static int64_t part_rows_needed(const coherit_geno* h) {
   return rows;
 }
 
-static WsLayout ws_layout(const coherit_geno* h, int kp, int nsplit) {
+static WsLayout ws_layout(const coherit_geno* h, int kp, int nsplit, bool f16) {
   WsLayout L;
   size_t off = 0;
   L.vt = off;
@@ -485,17 +705,23 @@ static WsLayout ws_layout(const coherit_geno* h, int kp, int nsplit) {
   off = align256(off + static_cast<size_t>(h->n_panels) * nsplit * kp * kPanel * 2);
   L.cs_part = off;
   off = align256(off + static_cast<size_t>(h->n_chunks) * kp * 8);
+  L.mx_part = off;
+  if (f16) off = align256(off + static_cast<size_t>(h->n_chunks) * kp * 4);
   L.cs = off;
+  off = align256(off + static_cast<size_t>(kp) * 4);
+  L.shift = off;
+  off = align256(off + static_cast<size_t>(2 * n_segments(h->n_chunks) + 1) * kp * 4);
+  L.vscale = off;
+  off = align256(off + static_cast<size_t>(kp) * 4);
+  L.smax = off;
   off = align256(off + static_cast<size_t>(kp) * 4);
   L.rbuf = off;
   off = align256(off + static_cast<size_t>(h->G) * kp * 8);
   L.vmiss = off;
   L.sf32 = off;
-  if (h->n_missing > 0) {
-    off = align256(off + static_cast<size_t>(h->m_pad) * kp * 4);
-    L.sf32 = off;
-    off = align256(off + static_cast<size_t>(h->m_pad) * kp * 4);
-  }
+  if (h->n_missing > 0) off = align256(off + static_cast<size_t>(h->m_pad) * kp * 4);
+  L.sf32 = off;
+  if (h->n_missing > 0 || f16) off = align256(off + static_cast<size_t>(h->m_pad) * kp * 4);
   L.part = off;
   off = align256(off + static_cast<size_t>(part_rows_needed(h)) * kp * 4);
   L.total = off;
@@ -515,9 +741,9 @@ int ensure_ws_bytes(coherit_geno* h, size_t bytes) {
   return COHERIT_OK;
 }
 
-int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t nsplit) {
+int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t nsplit, bool f16) {
   const int kp = static_cast<int>(round_up(std::max(k_max, 1), 16));
-  const WsLayout L = ws_layout(h, kp, nsplit);
+  const WsLayout L = ws_layout(h, kp, nsplit, f16);
   return ensure_ws_bytes(h, L.total);
 }
 
@@ -534,8 +760,10 @@ static int fill_epi(coherit_geno* h, const OpDesc& d, int kp, int nsplit, EpiPar
   e.nsplit = nsplit;
   e.stacked = d.mode == COHERIT_MODE_STACKED ? 1 : 0;
   e.xtv = d.xtv ? 1 : 0;
+  e.f16 = is_f16(d.precision) ? 1 : 0;
   e.n = h->n;
   e.m_pad = h->m_pad;
+  e.n_seg = static_cast<int>(n_segments(h->n_chunks));
   e.ldv = d.ldv;
   e.ldo = d.ldo;
   for (int r = 0; r <= d.n_groups; ++r) e.col_start[r] = d.col_start[r];
@@ -545,6 +773,9 @@ static int fill_epi(coherit_geno* h, const OpDesc& d, int kp, int nsplit, EpiPar
              COHERIT_E_INDEX, "stats slot %d is not initialised", s);
     e.gmean[r] = h->slots[s].mean;
     e.ginv[r] = h->slots[s].inv;
+    e.gdsum[r] = h->slots[s].dsum;
+    e.gdseg[r] = h->slots[s].dseg;
+    e.gnseg[r] = h->slots[s].nseg;
     e.gmask[r] = h->slots[s].row_mask;
     for (int g = 0; g < h->G; ++g) e.cscale[r * h->G + g] = d.comp_scale[r * h->G + g];
     e.theta_e[r] = d.theta_e.empty() ? 0.f : d.theta_e[r];
@@ -571,13 +802,10 @@ struct TcLaunchCfg {
 
 // Accumulator: NSPLIT*kp columns, the split terms side by side in N (one MMA
 // per K step, N <= 256).  The A ring takes the remaining tensor-memory
-// columns.  Blocks of <= 16 columns use the narrow form at two CTAs per SM;
-// wider blocks use the wide form where its B ring (>= 2 stages) fits shared
-// memory, else the narrow form, always at one CTA per SM: two-CTA layouts
-// of wider blocks returned wrong lane quarters when K was split (bf16x1 and
-// bf16x2 at 32-48 columns, 3e-2 to 1e-1 off at n = 20,000, m = 30,000), and
-// one CTA per SM allocates all 512 tensor-memory columns so no second CTA
-// can share the SM.
+// columns.  Blocks of <= 16 columns use the narrow form; wider blocks use the
+// wide form where its B ring (>= 2 stages) fits shared memory, else the
+// narrow form; always one CTA per SM, which allocates all 512 tensor-memory
+// columns so no second CTA can share the SM.
 static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
   TcLaunchCfg c;
   c.side = nsplit > 1 && nsplit * kp <= 256;
@@ -605,12 +833,11 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
   c.wide = false;
   c.sb = CfgNarrow::SB;
   const uint32_t slot_cols = 32u * CfgNarrow::SB;
-  uint32_t cols = 512;
-  if (kp <= 16) {
-    const uint32_t need = c.acc_cols + CfgNarrow::MIN_RA * slot_cols;
-    cols = 32;
-    while (cols < need) cols <<= 1;
-  }
+  // One CTA per SM for every width: all 512 tensor-memory columns.  Layouts
+  // with two CTAs per SM returned a few wrong rows under split K (a whole
+  // lane quarter of a tile) even with CTAs of whole warpgroups, and they buy
+  // little: the SM's tensor pipe runs the two CTAs' MMAs one after the other.
+  const uint32_t cols = 512;
   c.tmem_cols = cols;
   c.RA = std::min<int>(kMaxRA, static_cast<int>((cols - c.acc_cols) / slot_cols));
   c.bslot = static_cast<uint32_t>(CfgNarrow::SB) * nsplit * kp * kPanel * 2;
@@ -632,8 +859,8 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
 }
 
 template <bool IS_K1, class Cfg>
-static int launch_tc_cfg(int nsplit, bool side, dim3 grid, size_t smem, cudaStream_t st,
-                         const TcParams& p) {
+static int launch_tc_cfg(int nsplit, bool f16, bool side, dim3 grid, size_t smem,
+                         cudaStream_t st, const TcParams& p) {
   auto go = [&](auto kern) -> int {
     CO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));
@@ -641,17 +868,22 @@ static int launch_tc_cfg(int nsplit, bool side, dim3 grid, size_t smem, cudaStre
     CO_CUDA(cudaGetLastError());
     return COHERIT_OK;
   };
-  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false, Cfg>);
+  if (f16) {
+    CO_CHECK(nsplit == 2 && side, COHERIT_E_SHAPE, "FP16 terms must fit side by side (2 kp <= 256)");
+    return go(k_tc_op<IS_K1, 2, true, Cfg, true>);
+  }
+  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false, Cfg, false>);
   CO_CHECK(side, COHERIT_E_SHAPE, "split terms must fit side by side (nsplit * kp <= 256)");
-  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true, Cfg>);
-  return go(k_tc_op<IS_K1, 3, true, Cfg>);
+  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true, Cfg, false>);
+  return go(k_tc_op<IS_K1, 3, true, Cfg, false>);
 }
 
 template <bool IS_K1>
-static int launch_tc(const TcLaunchCfg& cfg, int nsplit, dim3 grid, cudaStream_t st,
+static int launch_tc(const TcLaunchCfg& cfg, int nsplit, bool f16, dim3 grid, cudaStream_t st,
                      const TcParams& p) {
-  if (cfg.wide) return launch_tc_cfg<IS_K1, CfgWide>(nsplit, cfg.side, grid, cfg.smem, st, p);
-  return launch_tc_cfg<IS_K1, CfgNarrow>(nsplit, cfg.side, grid, cfg.smem, st, p);
+  if (cfg.wide)
+    return launch_tc_cfg<IS_K1, CfgWide>(nsplit, f16, cfg.side, grid, cfg.smem, st, p);
+  return launch_tc_cfg<IS_K1, CfgNarrow>(nsplit, f16, cfg.side, grid, cfg.smem, st, p);
 }
 
 // Column-block width when k exceeds what one launch holds (each block
@@ -667,6 +899,7 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
 
 int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
   if (d.precision == COHERIT_PREC_FP32) return run_operator_fp32(h, d, st);
+  CO_CHECK(is_tc_precision(d.precision), COHERIT_E_SHAPE, "unknown precision %d", d.precision);
   const int nsplit = nsplit_of(d.precision);
   const int kmax = max_kp_for(h, nsplit);
   if (d.k > kmax) {
@@ -686,7 +919,7 @@ int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
     return COHERIT_OK;
   }
   const int kp = static_cast<int>(round_up(std::max(d.k, 1), 16));
-  int rc = ensure_workspace(h, kp, nsplit);
+  int rc = ensure_workspace(h, kp, nsplit, is_f16(d.precision));
   if (rc != COHERIT_OK) return rc;
   return launch_operator(h, d, kp, nsplit, static_cast<uint8_t*>(h->ws.base), st);
 }
@@ -695,13 +928,12 @@ int run_operator_in_scratch(coherit_geno* h, const OpDesc& d, void* scratch, siz
                             cudaStream_t st) {
   CO_CHECK(d.precision != COHERIT_PREC_FP32, COHERIT_E_UNSUPPORTED,
            "the fixed-scratch operator runs the tensor-core precisions only");
-  CO_CHECK(d.precision >= COHERIT_PREC_BF16X3 && d.precision <= COHERIT_PREC_BF16X1,
-           COHERIT_E_SHAPE, "unknown precision %d", d.precision);
+  CO_CHECK(is_tc_precision(d.precision), COHERIT_E_SHAPE, "unknown precision %d", d.precision);
   CO_CHECK(d.n_groups == 1, COHERIT_E_SHAPE, "the fixed-scratch operator takes one request");
   const int nsplit = nsplit_of(d.precision);
   const int step = column_step(d.k, max_kp_for(h, nsplit));
   const int kp = static_cast<int>(round_up(std::max(step, 1), 16));
-  const size_t need = ws_layout(h, kp, nsplit).total;
+  const size_t need = ws_layout(h, kp, nsplit, is_f16(d.precision)).total;
   CO_CHECK(need <= bytes, COHERIT_E_SHAPE,
            "operator needs %zu bytes of scratch for n=%lld, m_pad=%lld, %d columns per launch; "
            "the fixed scratch holds %zu bytes (use coherit_geno_kv)",
@@ -723,7 +955,8 @@ int run_operator_in_scratch(coherit_geno* h, const OpDesc& d, void* scratch, siz
 // with the workspace at `ws` (laid out by ws_layout(h, kp, nsplit)).
 static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit, uint8_t* ws,
                            cudaStream_t st) {
-  const WsLayout L = ws_layout(h, kp, nsplit);
+  const bool f16 = is_f16(d.precision);
+  const WsLayout L = ws_layout(h, kp, nsplit, f16);
   EpiParams e;
   int rc = fill_epi(h, d, kp, nsplit, e);
   if (rc != COHERIT_OK) return rc;
@@ -731,16 +964,24 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   auto* sbuf = reinterpret_cast<__nv_bfloat16*>(ws + L.sbuf);
   auto* cs_part = reinterpret_cast<double*>(ws + L.cs_part);
   auto* cs = reinterpret_cast<float*>(ws + L.cs);
+  auto* shift = reinterpret_cast<float*>(ws + L.shift);
+  auto* vscale = reinterpret_cast<float*>(ws + L.vscale);
+  auto* smax = reinterpret_cast<unsigned*>(ws + L.smax);
+  float* mx_part = f16 ? reinterpret_cast<float*>(ws + L.mx_part) : nullptr;
   auto* rbuf = reinterpret_cast<double*>(ws + L.rbuf);
   float* vmiss = h->n_missing > 0 ? reinterpret_cast<float*>(ws + L.vmiss) : nullptr;
-  float* sf32 = h->n_missing > 0 ? reinterpret_cast<float*>(ws + L.sf32) : nullptr;
+  float* sf32 = (h->n_missing > 0 || f16) ? reinterpret_cast<float*>(ws + L.sf32) : nullptr;
   e.cs = cs;
+  e.shift = shift;
+  e.vscale = vscale;
+  e.smax = smax;
   e.vmiss = vmiss;
   e.sbuf = sbuf;
   e.sf32 = sf32;
   e.rbuf = rbuf;
   const int nr = e.stacked ? h->G : 1;
   CO_CUDA(cudaMemsetAsync(rbuf, 0, sizeof(double) * nr * kp, st));
+  if (f16) CO_CUDA(cudaMemsetAsync(smax, 0, sizeof(unsigned) * kp, st));
   const TcLaunchCfg cfg = tc_config(h, kp, nsplit);
   const SplitPlan sp = split_plan(h, e.stacked != 0, target_ctas(h), cfg.sb);
   float* part = reinterpret_cast<float*>(ws + L.part);
@@ -759,11 +1000,22 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   p.b_chunk_bytes = static_cast<int64_t>(nsplit) * kp * kPanel * 2;
 
   if (!d.zxb) {
+    // Column means a of V, then V' = V - a split into K1's B tiles and the
+    // column sums of V'.
     const int prep_smem = kPanel * (kp + 1) * static_cast<int>(sizeof(float));
-    CO_CUDA(cudaFuncSetAttribute(k_prep_v, cudaFuncAttributeMaxDynamicSharedMemorySize, prep_smem));
-    k_prep_v<<<static_cast<unsigned>(h->n_chunks), 256, prep_smem, st>>>(
-        d.V, d.ldv, h->n, d.k, kp, nsplit, vt, cs_part, e); note_launch();
+    CO_CUDA(cudaFuncSetAttribute(k_prep_v<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 prep_smem));
+    CO_CUDA(cudaFuncSetAttribute(k_prep_v<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 prep_smem));
+    k_prep_v<false><<<static_cast<unsigned>(h->n_chunks), 256, prep_smem, st>>>(
+        d.V, d.ldv, h->n, d.k, kp, nsplit, vt, cs_part, mx_part, e); note_launch();
+    k_shift_finish<<<kp, 256, 0, st>>>(cs_part, mx_part, h->n_chunks, kp, shift, vscale, e);
+    note_launch();
+    k_prep_v<true><<<static_cast<unsigned>(h->n_chunks), 256, prep_smem, st>>>(
+        d.V, d.ldv, h->n, d.k, kp, nsplit, vt, cs_part, nullptr, e); note_launch();
     k_colsum_finish<<<kp, 256, 0, st>>>(cs_part, h->n_chunks, kp, cs); note_launch();
+    CO_CHECK(vmiss == nullptr || (h->d_csc_off != nullptr && h->d_csc_idx != nullptr),
+             COHERIT_E_SHAPE, "missing-genotype lists absent");
     if (vmiss != nullptr)
       k_vmiss<<<static_cast<unsigned>((h->m_pad + 7) / 8), 256, 0, st>>>(
           h->d_csc_off, h->d_csc_idx, h->m_pad, d.V, d.ldv, h->n, d.k, kp, vmiss, e); note_launch();
@@ -775,7 +1027,7 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
     p.part = sp.k1 > 1 ? part : nullptr;
     p.part_stride = h->m_pad * kp;
     p.part_rows = h->m_pad;
-    rc = launch_tc<true>(cfg, nsplit,
+    rc = launch_tc<true>(cfg, nsplit, f16,
                          dim3(static_cast<unsigned>(h->n_ttiles), 1, static_cast<unsigned>(sp.k1)),
                          st, p);
     if (rc != COHERIT_OK) return rc;
@@ -786,9 +1038,14 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
     }
     if (d.xtv) return COHERIT_OK;
   } else {
-    // Z b: S = inv_sd * b computed directly.
+    // Z b: S = inv_sd * b computed directly.  vscale is never read here.
     CO_CHECK(h->n_missing == 0 || sf32 != nullptr, COHERIT_E_SHAPE, "workspace missing");
     k_prep_s_from_b<<<static_cast<unsigned>((h->m_pad + 127) / 128), 128, 0, st>>>(d.V, d.ldv, e); note_launch();
+    CO_CUDA(cudaGetLastError());
+  }
+  if (f16) {
+    // S's column maxima are known once every slot tile is done: FP16 tiles now.
+    k_split_s<<<static_cast<unsigned>((h->m_pad + 127) / 128), 128, 0, st>>>(e); note_launch();
     CO_CUDA(cudaGetLastError());
   }
   p.geno = h->geno_s;
@@ -799,7 +1056,7 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   p.part = sp.k2 > 1 ? part : nullptr;
   p.part_stride = static_cast<int64_t>(nr) * h->n_pad * kp;
   p.part_rows = h->n_pad;
-  rc = launch_tc<false>(cfg, nsplit,
+  rc = launch_tc<false>(cfg, nsplit, f16,
                         dim3(static_cast<unsigned>(h->n_stiles), static_cast<unsigned>(nr),
                              static_cast<unsigned>(sp.k2)),
                         st, p);
@@ -809,7 +1066,11 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
                   dim3(32, 4), 0, st>>>(part, sp.k2, p.part_stride, h->n_pad, e); note_launch();
     CO_CUDA(cudaGetLastError());
   }
-  if (sf32 != nullptr) {
+  // Missing-genotype correction: only when the handle holds missing
+  // genotypes (and so the CSR lists); the FP32 S buffer also exists for FP16X2.
+  if (h->n_missing > 0) {
+    CO_CHECK(sf32 != nullptr && h->d_csr_off != nullptr && h->d_csr_idx != nullptr,
+             COHERIT_E_SHAPE, "missing-genotype lists or FP32 S buffer absent");
     k_rowcorr<<<static_cast<unsigned>((h->n + 7) / 8), 256, 0, st>>>(h->d_csr_off, h->d_csr_idx,
                                                                       h->n, e); note_launch();
     CO_CUDA(cudaGetLastError());
@@ -844,8 +1105,9 @@ int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision) {
   const int kp = static_cast<int>(round_up(std::max(k_max, 1), 16));
   if (precision == COHERIT_PREC_FP32)
     return ensure_ws_bytes(h, static_cast<size_t>(h->m_pad) * kp * sizeof(float));
+  CO_CHECK(is_tc_precision(precision), COHERIT_E_SHAPE, "unknown precision %d", precision);
   const int ns = nsplit_of(precision);
-  return ensure_workspace(h, std::min(kp, max_kp_for(h, ns)), ns);
+  return ensure_workspace(h, std::min(kp, max_kp_for(h, ns)), ns, is_f16(precision));
 }
 
 int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t precision,
@@ -925,3 +1187,6 @@ int coherit_geno_zxb(coherit_geno_t* h, int32_t slot, int32_t precision, const f
 }
 
 }  // extern "C"
+
+// Kernel parameters stay within the classic 4 KB limit.
+static_assert(sizeof(coherit::TcParams) <= 4000, "operator kernel parameters exceed 4 KB");

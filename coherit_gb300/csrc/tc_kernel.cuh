@@ -6,7 +6,8 @@
 //            a shared ring;
 //   warp 2   bulk-copies the B tile (all split terms of V or S for these 64
 //            K values) into a shared ring;
-//   warps 3.. decode in Cfg::SETS sets of 4 warps (one per tensor-memory lane
+//   warp 3   idles (the CTA is a whole number of warpgroups);
+//   warps 4.. decode in Cfg::SETS sets of 4 warps (one per tensor-memory lane
 //            quarter); a set turns the 16-byte rows (64 codes) of one chunk
 //            into 32 BF16 pairs per row stored with tcgen05.st into an A ring
 //            in tensor memory, and the sets take successive chunks so that
@@ -24,7 +25,7 @@
 // with the number of MMAs into one accumulator), so the host bounds every
 // chain this way.
 
-template <bool IS_K1, int NSPLIT, bool SIDE, class Cfg>
+template <bool IS_K1, int NSPLIT, bool SIDE, class Cfg, bool F16>
 __global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant__ TcParams p) {
   constexpr int kStageBlocks = Cfg::SB;
   constexpr int kSets = Cfg::SETS;
@@ -175,7 +176,8 @@ __global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant
   } else if (warp == kWarpMMA) {
     // ------------------------------------------------------------ MMA issue
     if (lane == 0) {
-      const uint32_t idesc = ptx::idesc_bf16_f32(128, SIDE ? NSPLIT * kp : kp);
+      const uint32_t idesc = F16 ? ptx::idesc_f16_f32(128, SIDE ? NSPLIT * kp : kp)
+                                 : ptx::idesc_bf16_f32(128, SIDE ? NSPLIT * kp : kp);
       const uint64_t bdesc0 = ptx::smem_desc(ptx::smem_addr(bring), 128u, 1024u);
       const uint32_t term_off = static_cast<uint32_t>(kp * 128) >> 4;
       int as = 0, bs = 0;
@@ -220,6 +222,8 @@ __global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant
         ptx::mbar_wait(done, 0, p.err, 20, &no_abort);
       }
     }
+  } else if (warp == kWarpIdle) {
+    // Pads the CTA to whole warpgroups (see StageCfg::THREADS).
   } else {
     // --------------------------------------------- decoders, then epilogue
     // Decoder warp sets: set s handles chunks s, s + kSets, ...; within a set
@@ -252,7 +256,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant
 #pragma unroll
       for (int b = 0; b < kStageBlocks; ++b) {
         uint32_t a[32];
-        decode_row(raw[b], a);
+        decode_row<F16>(raw[b], a);
         ptx::tmem_st32(tmem + lane_base + p.acc_cols +
                            static_cast<uint32_t>(as * kStageBlocks + b) * 32u, a);
       }

@@ -136,6 +136,13 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
          | (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(M >> 4) << 24);
 }
 
+// Instruction descriptor for kind::f16: FP16 x FP16 -> FP32 (A and B both
+// FP16: format code 0), both operands K-major, dense.
+__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
+  return (1u << 4)  // D format: F32
+         | (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(M >> 4) << 24);
+}
+
 // D[tmem] (+)= A[tmem] * B[smem]  (A from tensor memory)
 __device__ __forceinline__ void mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc,
                                        uint32_t idesc, uint32_t accumulate) {

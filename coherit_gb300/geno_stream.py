@@ -75,6 +75,33 @@ class SyntheticSource:
         return out
 
 
+class LDBlockSource:
+    """Generator-backed source with linkage disequilibrium (synth.ld_tables):
+    SNPs in blocks of ``block`` with AR(1) latent haplotypes, rho ~
+    U(rho_range), MAF ~ U(0.05, 0.5).  The streamer builds its resident
+    matrix on the device (coherit_geno_create_ldblock); host reads give the
+    same codes from the numpy twin (small sizes)."""
+
+    def __init__(self, n: int, m: int, seed: int = 0, block: int = 200, rho_range=(0.0, 0.9)):
+        from .synth import ld_tables
+
+        self.n = int(n)
+        self.m = int(m)
+        self.seed = int(seed)
+        self.block = int(block)
+        self.tables = ld_tables(self.seed, self.m, block=self.block, rho_range=rho_range)
+        self.missing_val = -127
+        self.sample_ids = None
+
+    def read_block_variant_major(self, start: int, count: int) -> np.ndarray:
+        from .synth import ld_block_codes
+
+        if start % self.block:
+            raise ValueError("host reads of the LD-block source start on a block boundary")
+        codes = ld_block_codes(self.seed, self.n, self.m, block=self.block, tables=self.tables)
+        return np.ascontiguousarray(codes[:, start:start + count].T.astype(np.int8))
+
+
 def _normalize_component_block_sizes(m: int, component_block_sizes) -> list[int]:
     """Contiguous component sizes: positive, summing to m (geno_stream.py:371-392)."""
     if component_block_sizes is None:
@@ -309,8 +336,25 @@ class GenoBlockStreamer:
         from .bed import BedSource
 
         bed_direct = isinstance(source, BedSource) and cache_to_source is None
+        ld_direct = isinstance(source, LDBlockSource) and self._sample_mask is None
         with torch.cuda.device(self.dev):
-            if bed_direct:
+            if ld_direct:
+                # LD-block genotypes generated on the device, permuted into
+                # cache order there.
+                thr, rho, sfac, quant, _ = source.tables
+                sizes_arr = np.asarray(sizes, dtype=np.int32)
+                c2s = (None if cache_to_source is None
+                       else np.ascontiguousarray(cache_to_source, dtype=np.int64))
+                _lib.check(
+                    self._lib.coherit_geno_create_ldblock(
+                        self.n, self.m, source.block, source.seed, thr.ctypes.data,
+                        rho.ctypes.data, sfac.ctypes.data, quant.ctypes.data,
+                        None if c2s is None else c2s.ctypes.data, sizes_arr.ctypes.data,
+                        len(sizes), self.dev.index, stream, C.byref(self._handle),
+                    ),
+                    "create LD-block genotypes",
+                )
+            elif bed_direct:
                 # PLINK BED bytes go to the device as they are and are
                 # transcoded there (no host repacking).
                 sizes_arr = np.asarray(sizes, dtype=np.int32)

@@ -116,6 +116,14 @@ def _device(V) -> torch.device:
     return torch.device("cuda", torch.cuda.current_device())
 
 
+def _zero_rhs(V) -> torch.Tensor:
+    """Zero result of V's shape on V's device (no call blocks to apply)."""
+    V2 = V if isinstance(V, torch.Tensor) else torch.as_tensor(np.asarray(V, dtype=np.float32))
+    if V2.ndim not in (1, 2):
+        raise ValueError(f"right-hand side must be 1-D or 2-D, got shape {tuple(V2.shape)}")
+    return torch.zeros(V2.shape, dtype=torch.float32, device=V2.device)
+
+
 def _eff(eff_m) -> float:
     return float(torch.as_tensor(eff_m).reshape(()).item())
 
@@ -132,9 +140,7 @@ def kv_impl_streamed(V, true_widths, means_by_call, inv_by_call, eff_m, *, n: in
     if st is not None and means_by_call is st._means_by_call and inv_by_call is st._inv_by_call:
         return st._kv_raw(V, comp_scale=np.full(st.n_components, scale))
     if n_calls == 0:
-        V2, squeeze = as_rhs(V, _device(V))
-        out = torch.zeros_like(V2)
-        return out[:, 0] if squeeze else out
+        return _zero_rhs(V)
     tg = _TransientGeno(n, n_calls, pop_block, true_widths, means_by_call, inv_by_call, _device(V))
     try:
         return tg.kv(V, scale)
@@ -145,6 +151,11 @@ def kv_impl_streamed(V, true_widths, means_by_call, inv_by_call, eff_m, *, n: in
 def kv_impl_snp_weighted_streamed(V, true_widths, means_by_call, inv_by_call, weights_by_call,
                                   denom, *, n: int, n_calls: int, pop_block, missing_val: int = 3):
     """Z diag(w) Z^T V / denom for per-SNP weights (kv_impl.py:329-379)."""
+    if int(missing_val) != 3:
+        raise ValueError("packed genotypes use code 3 for missing values")
+    if n_calls == 0:
+        # No call blocks: the accumulator stays zero (kv_impl.py:358-359).
+        return _zero_rhs(V)
     tw, _, _ = _flat_stats(true_widths, means_by_call, inv_by_call)
     wb = np.asarray(torch.as_tensor(weights_by_call).cpu(), dtype=np.float32)
     w = np.concatenate([wb[c, : tw[c]] for c in range(tw.size)]) if tw.size else np.zeros(0, np.float32)

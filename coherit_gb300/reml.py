@@ -1120,7 +1120,12 @@ def fit_reml(
     if return_diagnostics:
         diag = {"theta": param, "grad": grad, "ai": FI.mat, "loglik": ll,
                 "stop_reason": stop_reason, "y_mean": y_mean, "y_scale": y_scale,
-                "n_evals": n_evals}
+                "n_evals": n_evals,
+                "logdet": None if logdet_c is None else float(logdet_c)}
+        if use_trace_probes and trK is not None:
+            # Hutchinson traces tr(H^-1 K_i), tr(H^-1 R_j) of the last accepted solve.
+            diag["trace_K"] = torch.as_tensor(trK).double().cpu().numpy()
+            diag["trace_R"] = torch.as_tensor(trR).double().cpu().numpy()
         if not unit_variance_components:
             diag["genetic_trace_atoms"] = genetic_atoms
             diag["residual_trace_atoms"] = residual_atoms

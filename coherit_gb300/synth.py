@@ -103,41 +103,134 @@ def phenotype(seed: int, n: int, m: int, *, h2: float, n_causal: int, missing_q2
 
 # ------------------------------------------------- block-LD genotypes (8-GRM workload)
 
-def ld_block_genotypes(seed: int, n: int, m: int, *, block: int = 200, rho_range=(0.0, 0.9),
-                       maf_range=(0.05, 0.5)):
-    """Genotypes with linkage disequilibrium inside blocks of ``block`` SNPs.
+_Q_BITS = 12
 
-    Each block draws rho ~ U(rho_range); every sample carries two latent
-    haplotype chains h_0 ~ N(0, 1), h_j = rho h_{j-1} + sqrt(1 - rho^2) e_j,
-    and allele j is 1[h_j < Phi^-1(p_j)] with p_j ~ U(maf_range).  Each allele
-    is Bernoulli(p_j), so genotypes (two alleles) are in Hardy-Weinberg
-    equilibrium, and neighbouring SNPs are correlated through rho; blocks are
-    independent.  Host-side, for test-sized matrices.
 
-    Returns (codes (n, m) uint8 in {0, 1, 2}, maf (m,), rho per block).
-    """
-    from scipy.stats import norm
+def _snp_keys(seed: int, snps) -> np.ndarray:
+    s = np.asarray(snps, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        return _splitmix64(np.full(s.shape, seed, dtype=np.uint64) ^ (s * _U(0x8CB92BA72F3D8DD7)))
+
+
+def ld_tables(seed: int, m: int, *, block: int = 200, rho_range=(0.0, 0.9),
+              maf_range_q24=COMMON_MAF_Q24):
+    """Tables of the block-LD generator: per-SNP thresholds Phi^-1(maf_j) and
+    the population MAF, per-block rho_b ~ U(rho_range) and s_b = sqrt(1 -
+    rho_b^2), and the 4096 standard-normal quantiles Phi^-1((k + 1/2) / 4096)
+    the draws come from.  Returns float32 (thr, rho, s, quantiles) and the
+    float64 MAF."""
+    from scipy.special import ndtri
 
     if block < 1:
         raise ValueError("block must be positive")
     lo, hi = (float(x) for x in rho_range)
     if not 0.0 <= lo <= hi < 1.0:
         raise ValueError("rho_range must satisfy 0 <= lo <= hi < 1")
-    rng = np.random.default_rng(seed)
-    maf = rng.uniform(maf_range[0], maf_range[1], size=m)
-    thr = norm.ppf(maf)
-    n_blocks = (m + block - 1) // block
-    rho = rng.uniform(lo, hi, size=n_blocks)
-    codes = np.zeros((n, m), dtype=np.uint8)
-    for b in range(n_blocks):
-        j0, j1 = b * block, min((b + 1) * block, m)
-        r, s = rho[b], np.sqrt(1.0 - rho[b] ** 2)
-        h = rng.normal(size=(2, n))
-        for j in range(j0, j1):
-            if j > j0:
-                h = r * h + s * rng.normal(size=(2, n))
-            codes[:, j] = (h[0] < thr[j]).astype(np.uint8) + (h[1] < thr[j]).astype(np.uint8)
-    return codes, maf, rho
+    maf = maf_q24(seed, np.arange(m), maf_range_q24).astype(np.float64) / float(1 << 24)
+    thr = ndtri(maf).astype(np.float32)
+    nb = (m + block - 1) // block
+    b = np.arange(nb, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        h = _splitmix64(np.full(b.shape, seed, dtype=np.uint64) * _U(0xA24BAED4963EE407)
+                        ^ (b * _U(0x9FB21C651E98DF25)))
+    u = (h >> _U(40)).astype(np.float64) / float(1 << 24)
+    rho = (lo + (hi - lo) * u).astype(np.float32)
+    sfac = np.sqrt(1.0 - rho.astype(np.float64) ** 2).astype(np.float32)
+    quant = ndtri((np.arange(1 << _Q_BITS) + 0.5) / float(1 << _Q_BITS)).astype(np.float32)
+    return thr, rho, sfac, quant, maf
+
+
+def ld_block_codes(seed: int, n: int, m: int, *, block: int = 200, tables=None,
+                   samples=None) -> np.ndarray:
+    """Codes (n x m, uint8 in {0, 1, 2}) of the block-LD generator, with the
+    arithmetic of the device generator (coherit_ldblock_records): per sample,
+    haplotype a and block, x_0 = e_0 and x_p = rho_b x_{p-1} + s_b e_p in
+    float32 with separately rounded products and sum, e = quantiles[top 12
+    bits of splitmix64(key_j ^ (2i + a) C)], allele = [x_p < thr_j].  Host
+    scale (tests and small fits)."""
+    thr, rho, sfac, quant, _ = tables if tables is not None else ld_tables(seed, m, block=block)
+    i = np.arange(n, dtype=np.uint64) if samples is None else np.asarray(samples, np.uint64)
+    codes = np.zeros((i.size, m), dtype=np.uint8)
+    keys = _snp_keys(seed, np.arange(m))
+    for b in range((m + block - 1) // block):
+        r, sf = np.float32(rho[b]), np.float32(sfac[b])
+        x = np.zeros((2, i.size), np.float32)
+        for j in range(b * block, min(m, (b + 1) * block)):
+            for a in range(2):
+                with np.errstate(over="ignore"):
+                    hh = _splitmix64(keys[j] ^ ((_U(2) * i + _U(a)) * _U(0x9E3779B97F4A7C15)))
+                e = quant[(hh >> _U(64 - _Q_BITS)).astype(np.int64)]
+                if j == b * block:
+                    x[a] = e
+                else:
+                    x[a] = np.float32(r * x[a]) + np.float32(sf * e)
+            codes[:, j] = (x[0] < thr[j]).astype(np.uint8) + (x[1] < thr[j]).astype(np.uint8)
+    return codes
+
+
+def ld_block_genotypes(seed: int, n: int, m: int, *, block: int = 200, rho_range=(0.0, 0.9),
+                       maf_range=(0.05, 0.5)):
+    """Genotypes with linkage disequilibrium inside blocks of ``block`` SNPs
+    (the generator the device builds the 8-component workload with).
+
+    Each block has rho_b ~ U(rho_range); every sample carries two latent
+    haplotype chains x_0 ~ N(0, 1), x_p = rho_b x_{p-1} + sqrt(1 - rho_b^2)
+    e_p, and allele j is 1[x_j < Phi^-1(p_j)] with p_j ~ U(maf_range).  Each
+    allele is Bernoulli(p_j), so genotypes (two alleles) are in
+    Hardy-Weinberg equilibrium and neighbouring SNPs correlate through rho_b;
+    blocks are independent.
+
+    Returns (codes (n, m) uint8 in {0, 1, 2}, maf (m,), rho per block).
+    """
+    q24 = maf_range_q24(*maf_range)
+    tables = ld_tables(seed, m, block=block, rho_range=rho_range, maf_range_q24=q24)
+    codes = ld_block_codes(seed, n, m, block=block, tables=tables)
+    return codes, tables[4], tables[1].astype(np.float64)
+
+
+def ld_partition_device(seed: int, m: int, *, block: int = 200, n_ld: int = 4096,
+                        n_maf_bins: int = 4, device=None, rho_range=(0.0, 0.9)):
+    """The 4 MAF bins x 2 LD-score halves partition of the block-LD generator
+    at full size, built on the device: codes of the first ``n_ld`` samples
+    from coherit_ldblock_records, LD scores (sum of r^2 within each block) by
+    batched FP32 Gram products, MAF = the generator's population MAF.
+    Returns (groups, tables)."""
+    import torch
+
+    from . import _lib
+
+    lib = _lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+    tables = ld_tables(seed, m, block=block, rho_range=rho_range)
+    thr, rho, sfac, quant, maf = tables
+    td = [torch.as_tensor(a, device=dev).contiguous() for a in (thr, rho, sfac, quant)]
+    bps = (n_ld + 3) // 4
+    rec = torch.empty((m, bps), dtype=torch.uint8, device=dev)
+    _lib.check(lib.coherit_ldblock_records(n_ld, m, block, seed, *(t.data_ptr() for t in td),
+                                           rec.data_ptr(), _lib.stream_ptr()), "LD-block records")
+    lut = torch.tensor([2.0, 0.0, 1.0, 0.0], device=dev)  # BED 0,1,2,3 -> count (no missing)
+    ld = torch.empty(m, dtype=torch.float64, device=dev)
+    nb = (m + block - 1) // block
+    per = max(1, (1 << 28) // (block * n_ld))
+    for b0 in range(0, nb, per):
+        j0, j1 = b0 * block, min(m, (b0 + per) * block)
+        r = rec[j0:j1]
+        g = torch.stack([lut[((r >> (2 * t)) & 3).long()] for t in range(4)], dim=2)
+        g = g.reshape(j1 - j0, 4 * bps)[:, :n_ld]
+        g = g - g.mean(dim=1, keepdim=True)
+        sd = g.std(dim=1, unbiased=False, keepdim=True)
+        g = torch.where(sd > 0, g / torch.where(sd > 0, sd, torch.ones_like(sd)), torch.zeros_like(g))
+        full = (j1 - j0) // block * block
+        if full:
+            zb = g[:full].reshape(-1, block, n_ld)
+            cor = torch.bmm(zb, zb.transpose(1, 2)) / n_ld
+            ld[j0:j0 + full] = (cor * cor).sum(dim=2).reshape(-1).double()
+        if full < j1 - j0:
+            zt = g[full:]
+            cor = zt @ zt.T / n_ld
+            ld[j0 + full:j1] = (cor * cor).sum(dim=1).double()
+    groups = maf_ld_partition(maf, ld.cpu().numpy(), n_maf_bins=n_maf_bins)
+    return groups, tables
 
 
 def block_ld_scores(codes: np.ndarray, block: int = 200) -> np.ndarray:

@@ -49,11 +49,17 @@ extern "C" {
  *            form of the reference's Precision.HIGHEST matmuls (kv_impl.py:107-113).
  *  BF16X3  : tcgen05 tensor cores, genotypes exact in BF16, right-hand sides
  *            split into three BF16 terms (~FP32 accuracy), FP32 accumulation.
- *  BF16X2 / BF16X1 : fewer split terms (faster, less accurate; for sketches). */
+ *  BF16X2 / BF16X1 : fewer split terms (faster, less accurate; for sketches).
+ *  FP16X2  : tcgen05 tensor cores, genotypes exact in FP16, right-hand sides
+ *            (and the intermediate S) scaled per column by a power of two and
+ *            split into two FP16 terms (22 significant bits), FP32
+ *            accumulation; two terms instead of three, so one instruction of
+ *            N = 256 carries 128 columns. */
 #define COHERIT_PREC_FP32 0
 #define COHERIT_PREC_BF16X3 1
 #define COHERIT_PREC_BF16X2 2
 #define COHERIT_PREC_BF16X1 3
+#define COHERIT_PREC_FP16X2 4
 
 /* Operator output forms. */
 #define COHERIT_MODE_SUM 0      /* out = sum_g scale_g K_g V (+ theta_e V)         */
@@ -100,6 +106,33 @@ int coherit_geno_create_bed(const uint8_t* bed, int64_t bed_bytes, int64_t n_ful
                             const int32_t* keep, int64_t n_keep, const int32_t* component_sizes,
                             int32_t n_components, int device, void* stream,
                             coherit_geno_t** out);
+
+/* Benchmark genotypes with linkage disequilibrium, generated on the device
+ * (no counterpart in the reference, which reads real genotype files; this
+ * builds the synthetic 8-component workload: SNPs in blocks of `block`, two
+ * latent AR(1) haplotype chains per sample and block,
+ * x_p = rho_b x_{p-1} + s_b e_p in FP32, allele = [x_p < thresholds[j]],
+ * e from the 4096-entry standard-normal quantile table `quantiles` indexed
+ * by a counter-based hash of (seed, SNP, sample, haplotype)).
+ *
+ * coherit_ldblock_records writes SNP-major PLINK BED records (m records of
+ * ceil(n_rows/4) bytes) for samples 0..n_rows-1 into the device buffer
+ * `out`; the tables are device arrays (thresholds: m, rho and sfac:
+ * ceil(m/block), quantiles: 4096).  Used for LD scores on a sample prefix.
+ *
+ * coherit_geno_create_ldblock builds the resident matrix of n samples from
+ * the same generator with host tables; cache_to_source (host, m entries,
+ * NULL = identity) places source SNP cache_to_source[c] at cache position c,
+ * so arbitrary variant groups become contiguous components of
+ * component_sizes.  Synchronises `stream`.                                    */
+int coherit_ldblock_records(int64_t n_rows, int64_t m, int32_t block, uint64_t seed,
+                            const float* thresholds, const float* rho, const float* sfac,
+                            const float* quantiles, uint8_t* out, void* stream);
+int coherit_geno_create_ldblock(int64_t n, int64_t m, int32_t block, uint64_t seed,
+                                const float* thresholds, const float* rho, const float* sfac,
+                                const float* quantiles, const int64_t* cache_to_source,
+                                const int32_t* component_sizes, int32_t n_components, int device,
+                                void* stream, coherit_geno_t** out);
 
 /* Build a synthetic resident matrix (no host copy): per-SNP MAF ~ U(0.05, 0.5)
  * and genotypes ~ Binomial(2, MAF) drawn from a counter-based hash of
@@ -195,7 +228,8 @@ int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t preci
  * For callers that cannot allocate or free during a solve: the per-handle
  * buffer grows with cudaMalloc on the first wider call, and growing it runs
  * cudaFree after a device-wide synchronisation, which stalls every other
- * stream of a process that runs several solves at once.
+ * stream of the process.  Several solvers sharing a device must order their
+ * calls (one stream, or events between streams): they share the array.
  *   - tensor-core precisions only (COHERIT_PREC_FP32 -> COHERIT_E_UNSUPPORTED);
  *   - the workspace of one launch, about 2*nsplit*kp*(n_pad + m_pad) bytes
  *     (+ 8*kp*m_pad with missing genotypes, + the split-K partials; kp =
@@ -203,7 +237,9 @@ int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t preci
  *     COHERIT_E_SHAPE;
  *   - the handle's device must be current; the first call on a device
  *     resolves the array's address (cudaGetSymbolAddress), so make it before
- *     any stream capture;
+ *     any stream capture; with lazy module loading (the default) that call
+ *     commits the 64 MiB, with CUDA_MODULE_LOADING=EAGER every context that
+ *     loads the library commits it on each device it uses;
  *   - calls on one device share the array: calls in flight at the same time
  *     on different streams race; calls ordered on one stream are safe.     */
 int coherit_geno_kv_noalloc(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t precision,

@@ -4,8 +4,10 @@ Follows reml.py of the reference: response standardisation (:151-163),
 _eval_once (:685-971) with the affine single-GRM SLQ (:367-486) or the
 multi-component SLQ with its exact score (:489-540), the fixed-effect
 projection through the Cholesky of X^T H^-1 X (:780-801), the bounded Fisher
-step by NNLS + KKT polish (:979-1247) and the strict line search of fit_reml
-(:1695-1880).  Operators are numpy callables; vectors are FP64.
+step by NNLS + KKT polish (:979-1247), the strict line search of fit_reml
+(:1695-1880) and its one-trial scoring optimizer with Hutchinson traces
+(:608-649, :1798-1808, :1909-1911).  Operators are numpy callables; vectors
+are FP64.
 """
 from __future__ import annotations
 
@@ -252,6 +254,57 @@ def fit(ctx: Context, *, h2_init=0.5, minq_iter=50, trials=3, rel_dll_tol=1e-3, 
         param, cur = cand, res
         history.append(dict(iter=it + 1, accepted=True, loglik=cur["ll"], params=list(param)))
         if rel < rel_dll_tol:
+            break
+    return param, history, cur
+
+
+def hutchinson_traces(ctx: Context, sol):
+    """tr(H^-1 K_i) and tr(H^-1 R_j) estimated from the trace-probe columns of
+    a solve, (1/R) sum_r (H^-1 z_r)^T (K_i z_r) (reml.py:608-649)."""
+    Z = np.asarray(ctx.trace_probes, np.float64)
+    R = Z.shape[1]
+    a = ctx.y_col + 1
+    HZ = np.asarray(sol, np.float64)[:, a:a + R]
+    trK = np.asarray([np.sum(HZ * K(Z)) for K in ctx.K]) / R
+    trR = np.asarray([np.sum(Z * P) for P in ctx.residual_products(HZ)]) / R
+    return trK, trR
+
+
+def fit_scoring(ctx: Context, *, h2_init=0.5, minq_iter=50, taylor_threshold=0.01,
+                scoring_step_tol=1e-4, floor=1e-2):
+    """The ``smile_scoring`` optimizer of fit_reml (reml.py:1760-1911): one
+    trial per iteration at alpha = 1, every step accepted; when the largest
+    relative parameter change is below ``taylor_threshold`` the trial's
+    log-determinant is the first-order expansion logdet + dtheta . traces
+    (traces from the trace-probe columns of the last accepted solve) and its
+    score comes from the Hutchinson traces of the projected probes; stop when
+    that change is below ``scoring_step_tol``.  Needs ``ctx.trace_probes``."""
+    if ctx.trace_probes is None:
+        raise ValueError("the scoring optimizer needs trace probes")
+    G, E = ctx.G, ctx.E
+    ra = np.ones(E) if ctx.R is None else ctx.R.mean(axis=1)
+    param = np.concatenate([np.where(ctx.diag_atoms > 0, h2_init / np.sum(ctx.diag_atoms), 0.0),
+                            np.maximum(np.full(E, (1 - h2_init) / np.sum(ra)), floor)])
+    cur = evaluate(ctx, param)
+    trK, trR = hutchinson_traces(ctx, cur["sol"])
+    logdet_c = cur["logdet"]
+    history = []
+    for it in range(minq_iter):
+        d = fisher_step(param, cur["grad"], cur["ai"], G=G, floor=floor, alpha=1.0)
+        cand = apply_step(param, d, 1.0, G=G, floor=floor)
+        delta = cand - param
+        max_rel_dp = float(np.max(np.abs(delta) / np.maximum(np.abs(param), 1e-8)))
+        taylor = None
+        if max_rel_dp < taylor_threshold:
+            taylor = float(logdet_c + delta[:G] @ trK + delta[G:] @ trR)
+        res = evaluate(ctx, cand, warm=cur["sol"], taylor=taylor)
+        rel = (res["ll"] - cur["ll"]) / max(abs(cur["ll"]), 1e-12)
+        trK, trR = hutchinson_traces(ctx, res["sol"])
+        logdet_c = res["logdet"]
+        param, cur = cand, res
+        history.append(dict(iter=it + 1, loglik=cur["ll"], params=list(param),
+                            taylor=taylor is not None, max_rel_dp=max_rel_dp))
+        if not math.isfinite(rel) or max_rel_dp < scoring_step_tol:
             break
     return param, history, cur
 

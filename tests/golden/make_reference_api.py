@@ -1,10 +1,10 @@
 """Write reference_api.json: the public call surface of the reference modules
 this package replaces, read from their sources with ast (no import).
 
-Run from the repository root, with the reference checked out at
-/root/reference:
+Run from the repository root, giving the reference checkout as the argument
+or in COHERIT_REFERENCE_ROOT:
 
-    python tests/golden/make_reference_api.py [/root/reference]
+    python tests/golden/make_reference_api.py <reference checkout>
 
 Recorded per module: the parameter names of every public top-level function
 and of every public method (and __init__) of every public class, split into
@@ -75,4 +75,8 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("COHERIT_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_reference_api.py <reference checkout> "
+                 "(or set COHERIT_REFERENCE_ROOT)")
+    main(root)

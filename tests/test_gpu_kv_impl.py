@@ -127,3 +127,34 @@ def test_zxb_same_stream_multi_and_multi_streamed(cuda):
     only0[int(st._call_true_widths[0]):] = 0.0
     ref0 = og.zxb_f64(codes, st._means_host, st._inv_sds_host, only0)
     assert rel(part.cpu()[:, None], ref0[:, None]) < TOL
+
+
+def test_snp_weighted_resident_foreign_and_streamer(cuda):
+    """Z diag(w) Z^T V / denom (kv_impl.py:139-160, :329-379) through the
+    streamer's resident path, a foreign pop_block and the streamer method,
+    against the FP64 oracle with the same per-SNP weights."""
+    st, codes = _setup(seed=59)
+    rng = np.random.default_rng(11)
+    w = rng.uniform(0.05, 2.0, size=st.m).astype(np.float32)
+    w[::7] = 0.0
+    wb = _b_rows(st, w)
+    denom = 137.25
+    V = torch.randn(st.n, 5, device=cuda)
+    ref = og.kv_f64(codes, st._means_host, st._inv_sds_host, V.cpu().numpy(),
+                    comp_scale=[1.0 / denom], snp_weight=w)
+    args = (st._true_widths_dev, st._means_by_call, st._inv_by_call, torch.as_tensor(wb), denom)
+    kw = dict(n=st.n, n_calls=st._n_calls)
+    a = kv_impl.kv_impl_snp_weighted_streamed(V, *args, pop_block=st._pop_cached, **kw)
+    blocks = [st._pop_cached(c) for c in range(st._n_calls)]
+    b = kv_impl.kv_impl_snp_weighted_streamed(V, *args, pop_block=lambda c: blocks[c], **kw)
+    c = st.snp_weighted_kv(V, w, denom)
+    for out in (a, b, c):
+        assert tuple(out.shape) == (st.n, 5)
+        assert rel(out.cpu(), ref) < TOL
+    v1 = kv_impl.kv_impl_snp_weighted_streamed(V[:, 2], *args, pop_block=st._pop_cached, **kw)
+    assert v1.shape == (st.n,)
+    assert rel(v1.cpu()[:, None], ref[:, 2:3]) < TOL
+    # Unit weights and denom = m_eff give the plain normalised operator.
+    ones = st.snp_weighted_kv(V, np.ones(st.m, np.float32), float(st._eff_m_const))
+    assert rel(ones.cpu(), og.kv_f64(codes, st._means_host, st._inv_sds_host, V.cpu().numpy(),
+                                     comp_scale=[1 / float(st._eff_m_const)])) < TOL

@@ -91,7 +91,7 @@ def test_array_source_round_trip_and_partition(cuda):
         st.kv(np.zeros((n, 1), np.float32))
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3", "fp16x2"])
 @pytest.mark.parametrize("n,m,k,miss", [
     (1000, 3000, 7, 0.0),
     (1000, 3000, 7, 0.03),
@@ -114,7 +114,7 @@ def test_kv_matches_fp64_oracle(cuda, precision, n, m, k, miss):
     st.close()
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3", "fp16x2"])
 def test_vector_rhs_and_unnormalized(cuda, precision):
     n, m = 300, 500
     st = _streamer(n, m, seed=5, precision=precision)
@@ -126,7 +126,7 @@ def test_vector_rhs_and_unnormalized(cuda, precision):
     assert col_rel(out, ref) < TOL
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3", "fp16x2"])
 def test_components_stacked_weighted(cuda, precision):
     n, m = 500, 2100
     comps = [700, 1300, 100]
@@ -158,7 +158,7 @@ def test_components_stacked_weighted(cuda, precision):
                                    atol=1e-5)
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3", "fp16x2"])
 def test_xtv_zxb_exact_diag(cuda, precision):
     n, m = 400, 900
     st = _streamer(n, m, seed=17, miss=0.02, precision=precision)
@@ -175,7 +175,8 @@ def test_xtv_zxb_exact_diag(cuda, precision):
                                rtol=1e-6)
 
 
-def test_batched_subsets_equal_single_requests(cuda):
+@pytest.mark.parametrize("prec", [_lib.PREC_BF16X3, _lib.PREC_FP16X2])
+def test_batched_subsets_equal_single_requests(cuda, prec):
     n, m = 700, 1600
     st = _streamer(n, m, seed=19, miss=0.01, precision="bf16x3")
     lib = _lib.load()
@@ -204,7 +205,7 @@ def test_batched_subsets_equal_single_requests(cuda):
     out = torch.empty_like(Vd)
     _lib.check(lib.coherit_geno_kv_batched(
         st.handle, 3, col_start.ctypes.data, np.asarray([1, 2, 3], np.int32).ctypes.data,
-        _lib.PREC_BF16X3, Vd.data_ptr(), k, k, scale.ctypes.data, theta.ctypes.data,
+        prec, Vd.data_ptr(), k, k, scale.ctypes.data, theta.ctypes.data,
         out.data_ptr(), k, stream))
     out = out.cpu().numpy()
     for r, mk in enumerate(masks):
@@ -216,9 +217,10 @@ def test_batched_subsets_equal_single_requests(cuda):
     st.check()
 
 
-def test_wide_rhs_column_blocks(cuda):
+@pytest.mark.parametrize("precision", ["bf16x3", "fp16x2"])
+def test_wide_rhs_column_blocks(cuda, precision):
     n, m, k = 260, 800, 300
-    st = _streamer(n, m, seed=23, precision="bf16x3")
+    st = _streamer(n, m, seed=23, precision=precision)
     codes = oracle_codes(23, n, m, 0.0)
     V = np.random.default_rng(5).normal(size=(n, k)).astype(np.float32)
     out = st.kv(V).cpu().numpy()
@@ -278,6 +280,8 @@ def test_accuracy_at_scale_vs_dense_fp64(cuda):
     truth = (acc / float(st._eff_m_host)).cpu().numpy()
     out = st.kv(V).cpu().numpy()
     assert col_rel(out, truth) < TOL
+    # Two FP16 terms with per-column power-of-two scales hold the same bound.
+    assert col_rel(st.kv(V, precision="fp16x2").cpu().numpy(), truth) < TOL
     # The same columns inside a full-width launch give the same numbers (up
     # to the order of FP64 atomic additions in the rank-one term).
     wide = torch.cat([V, torch.randn((n, 74), generator=gen, device=dev)], dim=1)
@@ -313,5 +317,73 @@ def test_reduced_precisions_with_and_without_split_k(cuda, m):
             kv = st.kv(Vd, precision=prec).cpu().numpy()
             assert col_rel(kv, og.kv_f64(codes, mean, inv, V, comp_scale=[1 / eff])) < tol, \
                 (prec, k, "kv")
+    st.check()
+    st.close()
+
+
+def _dense_truth(st, V, miss_ok=True, W=8192):
+    """FP64 K V from the resident genotype bytes read back through the C ABI
+    (their bit-exactness against the oracle is checked above)."""
+    lib = _lib.load()
+    dev = st.dev
+    n, m = st.n, st.m
+    mean = torch.as_tensor(st._means_host, device=dev, dtype=torch.float64)
+    inv = torch.as_tensor(st._inv_sds_host, device=dev, dtype=torch.float64)
+    acc = torch.zeros((n, V.shape[1]), dtype=torch.float64, device=dev)
+    for s0 in range(0, m, W):
+        w = min(W, m - s0)
+        pw = (w + 3) // 4
+        host = np.empty((n, pw), dtype=np.uint8)
+        _lib.check(lib.coherit_geno_read_packed(st.handle, s0, w, host.ctypes.data,
+                                                _lib.stream_ptr()))
+        pk = torch.as_tensor(host, device=dev)
+        codes = torch.stack([(pk >> (2 * s)) & 3 for s in range(4)], dim=2).reshape(n, 4 * pw)[:, :w]
+        z = (codes.double() - mean[s0:s0 + w]) * inv[s0:s0 + w]
+        z[codes == 3] = 0.0
+        acc += z @ (z.T @ V.double())
+    return (acc / float(st._eff_m_host)).cpu().numpy()
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "fp16x2"])
+def test_mean_heavy_columns_at_n120000(cuda, precision):
+    """n=120,000 x m=40,000 with 1% missing genotypes: columns with a large
+    mean (a ramp i/n, a constant 3, an intercept of ones, N(5, 1)) next to
+    N(0, 1) columns, each within 1e-5 relative of FP64.  Without the column
+    shift in the first contraction the FP32 accumulator holds sums of order
+    n * mean * column mean and the centring subtracts two such numbers; the
+    ramp column then misses 1e-5 at this n.  The ones column is the extreme
+    case: its exact result comes only from sum_i diff_ij (the rounding of
+    the FP32 means)."""
+    n, m = 120000, 40000
+    st = _streamer(n, m, seed=43, miss=0.01, precision=precision)
+    dev = st.dev
+    gen = torch.Generator(device=dev).manual_seed(9)
+    V = torch.randn((n, 8), generator=gen, device=dev)
+    V[:, 0] = torch.arange(n, device=dev, dtype=torch.float32) / n
+    V[:, 1] = 3.0
+    V[:, 2] = 1.0
+    V[:, 3] += 5.0
+    truth = _dense_truth(st, V)
+    out = st.kv(V).cpu().numpy()
+    errs = np.linalg.norm(out - truth, axis=0) / np.linalg.norm(truth, axis=0)
+    assert np.all(errs < TOL), errs
+    # X^T V shares the first contraction: same identity, same bound.
+    xt = st.xtv(V).cpu().numpy()
+    lib = _lib.load()
+    mean = torch.as_tensor(st._means_host, device=dev, dtype=torch.float64)
+    inv = torch.as_tensor(st._inv_sds_host, device=dev, dtype=torch.float64)
+    ref = np.zeros((m, 8))
+    for s0 in range(0, m, 8192):
+        w = min(8192, m - s0)
+        pw = (w + 3) // 4
+        host = np.empty((n, pw), dtype=np.uint8)
+        _lib.check(lib.coherit_geno_read_packed(st.handle, s0, w, host.ctypes.data,
+                                                _lib.stream_ptr()))
+        pk = torch.as_tensor(host, device=dev)
+        codes = torch.stack([(pk >> (2 * s)) & 3 for s in range(4)], dim=2).reshape(n, 4 * pw)[:, :w]
+        z = (codes.double() - mean[s0:s0 + w]) * inv[s0:s0 + w]
+        z[codes == 3] = 0.0
+        ref[s0:s0 + w] = (z.T @ V.double()).cpu().numpy()
+    assert col_rel(xt, ref) < TOL
     st.check()
     st.close()

@@ -70,3 +70,20 @@ def test_zxb_streamed_shape_checks():
         with pytest.raises(ValueError, match=match):
             f(b, args["true_widths"], args["means_by_call"], args["inv_by_call"], n=3, n_calls=2,
               pop_block=None)
+
+
+@pytest.mark.parametrize("shape", [(5,), (5, 3)])
+def test_no_call_blocks_give_zero(shape):
+    """n_calls == 0: the accumulator is returned untouched (kv_impl.py:308-309,
+    :358-359 of the reference), without any device work."""
+    V = torch.ones(shape)
+    z = np.zeros((0, 4), np.float32)
+    out = kv_impl.kv_impl_streamed(V, np.zeros(0, np.int32), z, z, 1.0, n=5, n_calls=0,
+                                   pop_block=None)
+    assert tuple(out.shape) == shape and float(out.abs().sum()) == 0.0
+    out = kv_impl.kv_impl_snp_weighted_streamed(V, np.zeros(0, np.int32), z, z, z, 2.0, n=5,
+                                                n_calls=0, pop_block=None)
+    assert tuple(out.shape) == shape and float(out.abs().sum()) == 0.0
+    with pytest.raises(ValueError, match="code 3"):
+        kv_impl.kv_impl_snp_weighted_streamed(V, np.zeros(0, np.int32), z, z, z, 2.0, n=5,
+                                              n_calls=0, pop_block=None, missing_val=-127)

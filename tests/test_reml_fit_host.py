@@ -129,3 +129,41 @@ def test_eight_grm_maf_ld_partition_fit_matches_oracle():
     param, diag, h2, po, cur, h2_ref, hist, ho = _fit_both(Ks, X, y, slq_m=12)
     _check(diag, h2, cur, h2_ref, param, po)
     assert param.size == 9 and len(hist) >= 2
+
+
+def test_scoring_optimizer_fit_matches_oracle_scoring_fit():
+    """optimizer="smile_scoring" with the phenotype and 64 Rademacher trace
+    probes as one 67-column right-hand-side block ([X | y | probes]): the
+    package's one-trial scoring driver (Taylor log-determinants, Hutchinson
+    traces from the probe columns of the solves) against the oracle's
+    restatement of the same driver, on the same probes."""
+    Ks, X, y = _problem(200, 800, seed=13, comps=[800])
+    n = y.size
+    slq = np.random.default_rng(7).choice([-1.0, 1.0], size=(n, 16))
+    tp = np.random.default_rng(8).choice([-1.0, 1.0], size=(n, 64))
+    Kt = torch.as_tensor(Ks[0], dtype=torch.float32)
+    diags = [torch.diagonal(Kt)]
+    param, hist, diag = reml.fit_reml(
+        y, (lambda V: Kt @ V,), diags, X, n_rand_vec=64, maxiter=500, minq_iter=30,
+        slq_samples=16, slq_m=16, pcg_tol=1e-5, verbose=False, return_diagnostics=True,
+        device="cpu", optimizer="smile_scoring",
+        slq_probes=torch.as_tensor(slq, dtype=torch.float32),
+        trace_probes=torch.as_tensor(tp, dtype=torch.float32))
+    yo, _, _ = oreml.standardize(y)
+    atoms = reml._mean_diag_atoms(diags, n_samples=n)
+    ctx = oreml.Context(yo, [lambda v: Ks[0] @ v], X, diag_atoms=atoms, pcg_tol=1e-6,
+                        maxiter=1000, trace_probes=tp,
+                        affine_cache=oslq.affine_cache(lambda v: Ks[0] @ v, n, slq, 16))
+    po, ho, cur = oreml.fit_scoring(ctx, minq_iter=30)
+    h2 = oreml.heritability(param, 1, atoms)
+    h2_ref = oreml.heritability(po, 1, atoms)
+    assert abs(h2 - h2_ref) < 1e-3, (h2, h2_ref)
+    assert abs(diag["loglik"] - cur["ll"]) <= 1e-4 * abs(cur["ll"])
+    # Same trajectory step by step, Taylor steps included.  On this problem
+    # both settle into the same period-3 cycle (full, full, Taylor) and stop
+    # at the iteration limit: the reference's scoring loop has no other exit
+    # while the step stays above scoring_step_tol.
+    assert len(hist) == len(ho) == 30
+    assert [h["slq_taylor"] for h in hist] == [h["taylor"] for h in ho]
+    for h, o in zip(hist, ho):
+        np.testing.assert_allclose(h["params"], o["params"], rtol=1e-4)

@@ -71,6 +71,7 @@ def _check_pair(h, G, k, mode, precision, scale=None, theta_e=None, seed=0):
     assert _col_rel(a1, r1) < TOL
     assert _col_rel(a2, r2) < TOL
     assert np.all(np.isfinite(a1)) and np.all(np.isfinite(a2))
+    return (V1, a1), (V2, a2)
 
 
 def _n_of(h):
@@ -80,10 +81,24 @@ def _n_of(h):
 
 
 def test_noalloc_sum_with_missing_matches_kv(cuda):
-    h = _create(3000, 7000, comps=[3000, 4000], missing_q24=int(0.01 * (1 << 24)))
+    """Both fixed-scratch calls are also checked against the FP64 oracle
+    (sum over two components with missing genotypes and theta_e), so a fault
+    shared by both entry points (launch sequence, workspace offsets) shows."""
+    from oracle import geno as og
+
+    n, m, miss_q24 = 3000, 7000, int(0.01 * (1 << 24))
+    h = _create(n, m, comps=[3000, 4000], missing_q24=miss_q24)
     try:
         assert _device_bytes(h) > 0
-        _check_pair(h, 2, 20, 0, 1, scale=[1 / 3000.0, 1 / 4000.0], theta_e=0.7, seed=1)
+        scale = [1 / 3000.0, 1 / 4000.0]
+        calls = _check_pair(h, 2, 20, 0, 1, scale=scale, theta_e=0.7, seed=1)
+        codes = og.synth_codes(5, n, np.arange(m), missing_q24=miss_q24)
+        mean, inv, _ = og.stats(codes)
+        comp = np.repeat([0, 1], [3000, 4000])
+        for V, got in calls:
+            ref = og.kv_f64(codes, mean, inv, V.cpu().numpy(), comp_of_snp=comp,
+                            comp_scale=scale, n_components=2, theta_e=0.7)
+            assert _col_rel(got, ref) < TOL
     finally:
         _lib.load().coherit_geno_destroy(h)
 
@@ -94,6 +109,7 @@ def test_noalloc_stacked_wide_and_bf16x1_match_kv(cuda):
         # 200 columns: two column blocks per call at bf16x3.
         _check_pair(h, 2, 200, 1, 1, scale=[0.5, 2.0], seed=2)
         _check_pair(h, 2, 33, 0, 3, seed=3)
+        _check_pair(h, 2, 40, 0, 4, seed=4)
     finally:
         _lib.load().coherit_geno_destroy(h)
 
