@@ -31,6 +31,7 @@ PREC_BF16X3 = 1
 PREC_BF16X2 = 2
 PREC_BF16X1 = 3
 PREC_FP16X2 = 4
+PREC_FP8X5 = 5
 
 MODE_SUM = 0
 MODE_STACKED = 1
@@ -41,6 +42,7 @@ PRECISIONS = {
     "bf16x2": PREC_BF16X2,
     "bf16x1": PREC_BF16X1,
     "fp16x2": PREC_FP16X2,
+    "fp8x5": PREC_FP8X5,
 }
 
 _lock = threading.Lock()

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -246,17 +247,26 @@ int run_operator_fp32(coherit_geno* h, const OpDesc& d, cudaStream_t st);
 // (`bytes` long); never allocates; rejects shapes whose workspace is larger.
 int run_operator_in_scratch(coherit_geno* h, const OpDesc& d, void* scratch, size_t bytes,
                             cudaStream_t st);
-int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t nsplit, bool f16);
+int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t precision);
 int ensure_ws_bytes(coherit_geno* h, size_t bytes);
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 inline int nsplit_of(int precision) {
+  if (precision == COHERIT_PREC_FP8X5) return 5;
   return precision == COHERIT_PREC_BF16X3 ? 3
          : (precision == COHERIT_PREC_BF16X2 || precision == COHERIT_PREC_FP16X2) ? 2 : 1;
 }
-inline bool is_f16(int precision) { return precision == COHERIT_PREC_FP16X2; }
+// Operand type of the tensor-core forms: 0 BF16, 1 FP16, 2 E4M3.
+constexpr int kTyBf16 = 0, kTyF16 = 1, kTyE4M3 = 2;
+inline int op_type(int precision) {
+  return precision == COHERIT_PREC_FP16X2 ? kTyF16
+         : precision == COHERIT_PREC_FP8X5 ? kTyE4M3 : kTyBf16;
+}
+// Per-column power-of-two scales (FP16 and E4M3 forms).
+inline bool is_scaled(int precision) { return op_type(precision) != kTyBf16; }
+inline int elem_bytes(int precision) { return op_type(precision) == kTyE4M3 ? 1 : 2; }
 inline bool is_tc_precision(int precision) {
-  return precision >= COHERIT_PREC_BF16X3 && precision <= COHERIT_PREC_FP16X2;
+  return precision >= COHERIT_PREC_BF16X3 && precision <= COHERIT_PREC_FP8X5;
 }
 
 }  // namespace coherit

@@ -81,7 +81,7 @@ constexpr int kBarrierBytes = 1024;
 
 struct EpiParams {
   int n_groups, G, k, kp, nsplit, stacked, xtv, use_theta_e;
-  int f16;  // FP16X2: V' and S carry per-column power-of-two scales
+  int ty;   // operand type: kTyBf16, kTyF16 or kTyE4M3 (the last two scaled per column)
   int64_t n, m_pad, ldv, ldo;
   int32_t col_start[kMaxGroups + 1];
   const float* gmean[kMaxGroups];
@@ -100,12 +100,12 @@ struct EpiParams {
   // group's samples, row n_seg the column mean abar, rows n_seg + 1 + z the
   // deviations d_z = a_z - abar.
   const float* shift;
-  const float* vscale; // kp: power-of-two scale of V' in K1's B tiles (1 unless f16)
-  unsigned* smax;      // kp: max |S| per column (float bits), f16 only
+  const float* vscale; // kp: power-of-two scale of V' in K1's B tiles (1 for BF16)
+  unsigned* smax;      // kp: max |S| per column (float bits), scaled forms only
   const float* cs;     // kp column sums of the shifted V
   const float* vmiss;  // m_pad x kp (shifted V over missing genotypes) or nullptr
-  __nv_bfloat16* sbuf; // K1 output: S split tiles (16-bit terms, BF16 or FP16 bits)
-  float* sf32;         // m_pad x kp FP32 S (missing genotypes or f16), else nullptr
+  __nv_bfloat16* sbuf; // K1 output: S split tiles (BF16 / FP16 terms, or E4M3 bytes)
+  float* sf32;         // m_pad x kp FP32 S (missing genotypes or scaled forms), else nullptr
   double* rbuf;        // (stacked ? G : 1) x kp
   float* xout;         // X^T V output (m x ldo) when xtv
   const float* V;      // K2: residual term
@@ -182,14 +182,53 @@ __device__ __forceinline__ void split2h(float v, __half& hi, __half& lo) {
 }
 
 // Power-of-two scale that maps a column whose largest magnitude is `mx` into
-// [2^13, 2^14): the FP16 terms then stay normal and far below 65504.  Zero or
-// non-finite maxima give 1.
-__device__ __forceinline__ float pow2_scale(float mx) {
+// [2^(top-1), 2^top): top = 14 for FP16 terms (normal, far below 65504),
+// 8 for E4M3 terms (below 448, and every residual term stays below 256).
+// Zero or non-finite maxima give 1.
+__device__ __forceinline__ float pow2_scale(float mx, int top) {
   if (!(mx > 0.f) || !isfinite(mx)) return 1.f;
   int ex;
   frexpf(mx, &ex);  // mx = f 2^ex, f in [0.5, 1)
-  const int e = max(-100, min(100, 14 - ex));
+  const int e = max(-100, min(100, top - ex));
   return ldexpf(1.f, e);
+}
+__host__ __device__ __forceinline__ int scale_top(int ty) { return ty == kTyE4M3 ? 8 : 14; }
+
+// Five E4M3 terms of x (already scaled below 256): q_0 = e4m3(x), then each
+// term rounds 16 times the previous residual (exact in FP32), so
+// x = sum_t q_t 16^-t + O(2^-20 |x|).
+__device__ __forceinline__ void split5_e4m3(float x, uint8_t (&q)[5]) {
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {
+    const __nv_fp8_storage_t b = __nv_cvt_float_to_fp8(x, __NV_SATFINITE, __NV_E4M3);
+    q[t] = static_cast<uint8_t>(b);
+    const float back = __half2float(__half(__nv_cvt_fp8_to_halfraw(b, __NV_E4M3)));
+    x = (x - back) * 16.f;
+  }
+}
+
+// Byte offset of (column c, K index kk) inside one E4M3 term of a 64-K block
+// of a B tile: core matrices of 8 columns x 16 bytes, 4 along K per 8-column
+// group.
+__host__ __device__ __forceinline__ int64_t btile_off8(int c, int kk) {
+  return ((c >> 3) * 4 + (kk >> 4)) * 128 + (c & 7) * 16 + (kk & 15);
+}
+
+// Decoding to E4M3: codes 0, 1, 2, 3 (missing) -> bytes 0x00, 0x38 (1.0),
+// 0x40 (2.0), 0x00.  16 bytes = 64 codes -> 16 words of 4 E4M3 bytes in K
+// order (word 4w + s holds elements 16w + 4s .. 16w + 4s + 3).
+__device__ __forceinline__ void decode_row_e4m3(const uint4 raw, uint32_t (&a)[16]) {
+  const uint32_t ws[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+  for (int w = 0; w < 4; ++w) {
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const uint32_t t = (ws[w] >> (2 * s)) & 0x03030303u;  // one code per byte
+      const uint32_t sel = (t & 0xFu) | ((t >> 4) & 0xF0u) | ((t >> 8) & 0xF00u) |
+                           ((t >> 12) & 0xF000u);          // one code per nibble
+      a[4 * w + s] = __byte_perm(0x00403800u, 0u, sel);
+    }
+  }
 }
 
 // Offset (elements) of (column c, K index kk) inside one split term of a B
@@ -245,8 +284,8 @@ __device__ __forceinline__ void epilogue_k1(const EpiParams& e, int64_t j, int c
       if (snp >= 0 && c < e.k) e.xout[static_cast<int64_t>(snp) * e.ldo + c] = sval;
       continue;
     }
-    if (e.f16) {
-      // FP16 terms need the column's largest |S| first: keep S in FP32 and
+    if (e.ty != kTyBf16) {
+      // Scaled terms need the column's largest |S| first: keep S in FP32 and
       // its maximum (float bits order like unsigned for |S|; NaN wins);
       // k_split_s writes the B tiles and r afterwards.
       if (c < e.k) e.sf32[j * e.kp + c] = sval;
@@ -287,7 +326,7 @@ __device__ __forceinline__ void epilogue_k2(const EpiParams& e, int64_t i, int c
     if (c >= e.k) break;
     const int grp = group_of(e, c);
     float acc = T[t];
-    if (e.f16) acc *= 1.f / pow2_scale(__uint_as_float(e.smax[c]));
+    if (e.ty != kTyBf16) acc *= 1.f / pow2_scale(__uint_as_float(e.smax[c]), scale_top(e.ty));
     float v = acc - static_cast<float>(e.rbuf[gi * e.kp + c]);
     if (e.use_theta_e) v += e.theta_e[grp] * e.V[i * e.ldv + c];
     if (e.gmask[grp] != nullptr && e.gmask[grp][i] == 0) v = 0.f;
@@ -347,8 +386,8 @@ __global__ void __launch_bounds__(128) k_k2_finish(const float* __restrict__ par
 // the shifted V' = V - a (SPLIT = true) together with V' split into BF16 B
 // tiles for K1.  Rows outside a request's sample subset are read as zero
 // (and are not shifted).
-// Pass 1 also writes the per-chunk column maxima of |V| to mx_part (f16).
-// Pass 2 splits V' * vscale into three BF16 or two FP16 terms.
+// Pass 1 also writes the per-chunk column maxima of |V| to mx_part (scaled
+// forms).  Pass 2 splits V' * vscale into BF16, FP16 or E4M3 terms.
 template <bool SPLIT>
 __global__ void k_prep_v(const float* __restrict__ V, int64_t ldv, int64_t n, int k, int kp,
                          int nsplit, __nv_bfloat16* __restrict__ vt, double* __restrict__ cs_part,
@@ -381,12 +420,26 @@ __global__ void k_prep_v(const float* __restrict__ V, int64_t ldv, int64_t n, in
   if (!SPLIT) return;
   const int cg_n = kp / 8;
   const int64_t chunk_elems = static_cast<int64_t>(nsplit) * kp * kPanel;
+  if (e.ty == kTyE4M3) {
+    // One byte per element: (term, 8-column group, K core, column, byte).
+    uint8_t* vb = reinterpret_cast<uint8_t*>(vt);
+    for (int idx = threadIdx.x; idx < chunk_elems; idx += blockDim.x) {
+      const int kb = idx & 15, cr = (idx >> 4) & 7, kc = (idx >> 7) & 3;
+      const int rest = idx >> 9;
+      const int cg = rest % cg_n, t = rest / cg_n;
+      const int c = cg * 8 + cr, kk = kc * 16 + kb;
+      uint8_t qt[5];
+      split5_e4m3(tile[kk * ld + c] * e.vscale[c], qt);
+      vb[q * chunk_elems + idx] = qt[t];
+    }
+    return;
+  }
   for (int idx = threadIdx.x; idx < chunk_elems; idx += blockDim.x) {
     const int kr = idx & 7, cr = (idx >> 3) & 7, kg = (idx >> 6) & 7;
     const int rest = idx >> 9;
     const int cg = rest % cg_n, t = rest / cg_n;
     const int c = cg * 8 + cr, kk = kg * 8 + kr;
-    if (e.f16) {
+    if (e.ty == kTyF16) {
       __half hi, lo;
       split2h(tile[kk * ld + c] * e.vscale[c], hi, lo);
       reinterpret_cast<__half*>(vt)[q * chunk_elems + idx] = t == 0 ? hi : lo;
@@ -420,8 +473,8 @@ __global__ void __launch_bounds__(256) k_colsum_finish(const double* __restrict_
 // the identity the K1 epilogue uses; the local mean keeps the shifted column
 // and its running sums small).  One CTA per column; each segment's chunk
 // partials are added in chunk order.
-// With f16 it also sets vscale_c = pow2_scale(max |V_c| + max_z |a_zc|), a
-// bound on max |V'_c|, so that V' * vscale fits FP16's range.
+// For the scaled forms it also sets vscale_c = pow2_scale(max |V_c| +
+// max_z |a_zc|), a bound on max |V'_c|, so that V' * vscale fits the terms.
 __global__ void __launch_bounds__(256) k_shift_finish(const double* __restrict__ cs_part,
                                                       const float* __restrict__ mx_part,
                                                       int64_t n_parts, int kp,
@@ -464,7 +517,7 @@ __global__ void __launch_bounds__(256) k_shift_finish(const double* __restrict__
     shift[(static_cast<int64_t>(e.n_seg) + 1 + z) * kp + c] = a - abar;
     mx = fmaxf(mx, fabsf(a));
   }
-  if (e.f16) {
+  if (e.ty != kTyBf16) {
     float vm = 0.f;
     for (int64_t q = threadIdx.x; q < n_parts; q += 256) vm = fmaxf(vm, mx_part[q * kp + c]);
     redm[threadIdx.x] = vm;
@@ -481,7 +534,7 @@ __global__ void __launch_bounds__(256) k_shift_finish(const double* __restrict__
       if (threadIdx.x < w) redm[threadIdx.x] = fmaxf(redm[threadIdx.x], redm[threadIdx.x + w]);
       __syncthreads();
     }
-    if (threadIdx.x == 0) vscale[c] = pow2_scale(vmax + redm[0]);
+    if (threadIdx.x == 0) vscale[c] = pow2_scale(vmax + redm[0], scale_top(e.ty));
   } else if (threadIdx.x == 0) {
     vscale[c] = 1.f;
   }
@@ -545,8 +598,8 @@ __global__ void k_prep_s_from_b(const float* __restrict__ b, int64_t ldb,
   for (int c = 0; c < e.kp; ++c) {
     float sval = 0.f;
     if (c < e.k && snp >= 0) sval = iv * b[static_cast<int64_t>(snp) * ldb + c];
-    if (e.f16) {
-      // FP32 S and its column maximum; k_split_s forms the FP16 tiles and r.
+    if (e.ty != kTyBf16) {
+      // FP32 S and its column maximum; k_split_s forms the scaled tiles and r.
       if (active && c < e.k) e.sf32[j * e.kp + c] = sval;
       unsigned u = __float_as_uint(fabsf(sval));
 #pragma unroll
@@ -573,8 +626,9 @@ __global__ void k_prep_s_from_b(const float* __restrict__ b, int64_t ldb,
   }
 }
 
-// FP16X2: S (FP32, m_pad x kp) -> K2's B tiles of S * tau_c in two FP16
-// terms, tau_c = pow2_scale(max_j |S_jc|), and r = sum_j mu_j S_j in FP64
+// Scaled forms: S (FP32, m_pad x kp) -> K2's B tiles of S * tau_c in two
+// FP16 or five E4M3 terms, tau_c = pow2_scale(max_j |S_jc|), and
+// r = sum_j mu_j S_j in FP64
 // (per component when stacked).  One thread per slot; a warp's 32 slots lie
 // in one component (components start on multiples of 256 slots), checked
 // before the warp reduction.
@@ -588,8 +642,8 @@ __global__ void k_split_s(const __grid_constant__ EpiParams e) {
   const bool uniform = __all_sync(0xffffffffu, gi == g0);
   const int64_t pnl = j / kPanel;
   const int kk = static_cast<int>(j % kPanel);
-  const int64_t term = static_cast<int64_t>(e.kp) * kPanel;
-  __half* sb = reinterpret_cast<__half*>(e.sbuf);
+  const int64_t term = static_cast<int64_t>(e.kp) * kPanel;  // elements of one term
+  const int top = scale_top(e.ty);
   for (int c = 0; c < e.kp; ++c) {
     float sval = 0.f, mu = 0.f;
     if (active && c < e.k) {
@@ -597,12 +651,21 @@ __global__ void k_split_s(const __grid_constant__ EpiParams e) {
       mu = e.gmean[group_of(e, c)][j];
     }
     if (active) {
-      const float tau = c < e.k ? pow2_scale(__uint_as_float(e.smax[c])) : 1.f;
-      __half hi, lo;
-      split2h(sval * tau, hi, lo);
-      const int64_t base = pnl * (2 * term) + btile_off(c, kk);
-      sb[base] = hi;
-      sb[base + term] = lo;
+      const float tau = c < e.k ? pow2_scale(__uint_as_float(e.smax[c]), top) : 1.f;
+      if (e.ty == kTyE4M3) {
+        uint8_t q[5];
+        split5_e4m3(sval * tau, q);
+        uint8_t* sb = reinterpret_cast<uint8_t*>(e.sbuf) + pnl * (5 * term) + btile_off8(c, kk);
+#pragma unroll
+        for (int t = 0; t < 5; ++t) sb[t * term] = q[t];
+      } else {
+        __half hi, lo;
+        split2h(sval * tau, hi, lo);
+        __half* sb = reinterpret_cast<__half*>(e.sbuf);
+        const int64_t base = pnl * (2 * term) + btile_off(c, kk);
+        sb[base] = hi;
+        sb[base + term] = lo;
+      }
     }
     if (c >= e.k) continue;
     double v = static_cast<double>(mu) * static_cast<double>(sval);
@@ -624,10 +687,10 @@ __global__ void k_split_s(const __grid_constant__ EpiParams e) {
 // The split terms always sit side by side in N (nsplit * kp <= 256):
 // accumulating them one after another into one accumulator loses accuracy
 // on long chains (measured 6.5e-4 relative at n = 50,000, m = 500,000).
-static inline int max_kp_for(const coherit_geno* h, int nsplit) {
+static inline int max_kp_for(const coherit_geno* h, int nsplit, int eb) {
   const int budget =
       h->smem_optin - 4096 - kBarrierBytes - CfgNarrow::RG * CfgNarrow::SB * kBlockBytes;
-  const int per_col = 2 * CfgNarrow::SB * nsplit * kPanel * 2;
+  const int per_col = 2 * CfgNarrow::SB * nsplit * kPanel * eb;
   return std::min((256 / nsplit) / 16 * 16, (budget / per_col) / 16 * 16);
 }
 
@@ -696,13 +759,16 @@ static int64_t part_rows_needed(const coherit_geno* h) {
   return rows;
 }
 
-static WsLayout ws_layout(const coherit_geno* h, int kp, int nsplit, bool f16) {
+static WsLayout ws_layout(const coherit_geno* h, int kp, int precision) {
+  const int nsplit = nsplit_of(precision);
+  const int eb = elem_bytes(precision);
+  const bool f16 = is_scaled(precision);
   WsLayout L;
   size_t off = 0;
   L.vt = off;
-  off = align256(off + static_cast<size_t>(h->n_chunks) * nsplit * kp * kPanel * 2);
+  off = align256(off + static_cast<size_t>(h->n_chunks) * nsplit * kp * kPanel * eb);
   L.sbuf = off;
-  off = align256(off + static_cast<size_t>(h->n_panels) * nsplit * kp * kPanel * 2);
+  off = align256(off + static_cast<size_t>(h->n_panels) * nsplit * kp * kPanel * eb);
   L.cs_part = off;
   off = align256(off + static_cast<size_t>(h->n_chunks) * kp * 8);
   L.mx_part = off;
@@ -741,9 +807,9 @@ int ensure_ws_bytes(coherit_geno* h, size_t bytes) {
   return COHERIT_OK;
 }
 
-int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t nsplit, bool f16) {
+int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t precision) {
   const int kp = static_cast<int>(round_up(std::max(k_max, 1), 16));
-  const WsLayout L = ws_layout(h, kp, nsplit, f16);
+  const WsLayout L = ws_layout(h, kp, precision);
   return ensure_ws_bytes(h, L.total);
 }
 
@@ -760,7 +826,7 @@ static int fill_epi(coherit_geno* h, const OpDesc& d, int kp, int nsplit, EpiPar
   e.nsplit = nsplit;
   e.stacked = d.mode == COHERIT_MODE_STACKED ? 1 : 0;
   e.xtv = d.xtv ? 1 : 0;
-  e.f16 = is_f16(d.precision) ? 1 : 0;
+  e.ty = op_type(d.precision);
   e.n = h->n;
   e.m_pad = h->m_pad;
   e.n_seg = static_cast<int>(n_segments(h->n_chunks));
@@ -806,15 +872,23 @@ struct TcLaunchCfg {
 // wide form where its B ring (>= 2 stages) fits shared memory, else the
 // narrow form; always one CTA per SM, which allocates all 512 tensor-memory
 // columns so no second CTA can share the SM.
-static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
+static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int precision) {
+  const int nsplit = nsplit_of(precision);
+  const int eb = elem_bytes(precision);
+  // Tensor-memory columns of one 64-K block of A (E4M3: one byte per code).
+  const uint32_t acols = op_type(precision) == kTyE4M3 ? 16u : 32u;
   TcLaunchCfg c;
   c.side = nsplit > 1 && nsplit * kp <= 256;
   const int acc = c.side ? nsplit * kp : kp;
   c.acc_cols = static_cast<uint32_t>(round_up(acc, 32));
   const size_t cap = static_cast<size_t>(h->smem_optin);
-  if (kp > 16) {
-    const uint32_t slot = 32u * CfgWide::SB;
-    const uint32_t bslot = static_cast<uint32_t>(CfgWide::SB) * nsplit * kp * kPanel * 2;
+  {
+    // Four-block stages (half the barrier round trips per K of two-block
+    // stages) wherever their rings fit: at one CTA per SM they apply 16
+    // columns faster than two-block stages (n = 50,000, m = 500,000: k = 32
+    // in 10.5 ms against k = 16 in 12.7 ms with two-block stages).
+    const uint32_t slot = acols * CfgWide::SB;
+    const uint32_t bslot = static_cast<uint32_t>(CfgWide::SB) * nsplit * kp * kPanel * eb;
     const size_t fixed = kBarrierBytes + static_cast<size_t>(CfgWide::RG) * CfgWide::SB * kBlockBytes;
     const int ra = std::min<int>(kMaxRA, static_cast<int>((512u - c.acc_cols) / slot));
     if (c.acc_cols + CfgWide::MIN_RA * slot <= 512u && ra >= CfgWide::MIN_RA &&
@@ -832,7 +906,7 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
   }
   c.wide = false;
   c.sb = CfgNarrow::SB;
-  const uint32_t slot_cols = 32u * CfgNarrow::SB;
+  const uint32_t slot_cols = acols * CfgNarrow::SB;
   // One CTA per SM for every width: all 512 tensor-memory columns.  Layouts
   // with two CTAs per SM returned a few wrong rows under split K (a whole
   // lane quarter of a tile) even with CTAs of whole warpgroups, and they buy
@@ -840,7 +914,7 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
   const uint32_t cols = 512;
   c.tmem_cols = cols;
   c.RA = std::min<int>(kMaxRA, static_cast<int>((cols - c.acc_cols) / slot_cols));
-  c.bslot = static_cast<uint32_t>(CfgNarrow::SB) * nsplit * kp * kPanel * 2;
+  c.bslot = static_cast<uint32_t>(CfgNarrow::SB) * nsplit * kp * kPanel * eb;
   const size_t fixed =
       kBarrierBytes + static_cast<size_t>(CfgNarrow::RG) * CfgNarrow::SB * kBlockBytes;
   const int ctas_tmem = 512 / static_cast<int>(cols);
@@ -859,7 +933,7 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int nsplit) {
 }
 
 template <bool IS_K1, class Cfg>
-static int launch_tc_cfg(int nsplit, bool f16, bool side, dim3 grid, size_t smem,
+static int launch_tc_cfg(int nsplit, int ty, bool side, dim3 grid, size_t smem,
                          cudaStream_t st, const TcParams& p) {
   auto go = [&](auto kern) -> int {
     CO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -868,22 +942,26 @@ static int launch_tc_cfg(int nsplit, bool f16, bool side, dim3 grid, size_t smem
     CO_CUDA(cudaGetLastError());
     return COHERIT_OK;
   };
-  if (f16) {
+  if (ty == kTyF16) {
     CO_CHECK(nsplit == 2 && side, COHERIT_E_SHAPE, "FP16 terms must fit side by side (2 kp <= 256)");
-    return go(k_tc_op<IS_K1, 2, true, Cfg, true>);
+    return go(k_tc_op<IS_K1, 2, true, Cfg, kTyF16>);
   }
-  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false, Cfg, false>);
+  if (ty == kTyE4M3) {
+    CO_CHECK(nsplit == 5 && side, COHERIT_E_SHAPE, "E4M3 terms must fit side by side (5 kp <= 256)");
+    return go(k_tc_op<IS_K1, 5, true, Cfg, kTyE4M3>);
+  }
+  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false, Cfg, kTyBf16>);
   CO_CHECK(side, COHERIT_E_SHAPE, "split terms must fit side by side (nsplit * kp <= 256)");
-  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true, Cfg, false>);
-  return go(k_tc_op<IS_K1, 3, true, Cfg, false>);
+  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true, Cfg, kTyBf16>);
+  return go(k_tc_op<IS_K1, 3, true, Cfg, kTyBf16>);
 }
 
 template <bool IS_K1>
-static int launch_tc(const TcLaunchCfg& cfg, int nsplit, bool f16, dim3 grid, cudaStream_t st,
+static int launch_tc(const TcLaunchCfg& cfg, int nsplit, int ty, dim3 grid, cudaStream_t st,
                      const TcParams& p) {
   if (cfg.wide)
-    return launch_tc_cfg<IS_K1, CfgWide>(nsplit, f16, cfg.side, grid, cfg.smem, st, p);
-  return launch_tc_cfg<IS_K1, CfgNarrow>(nsplit, f16, cfg.side, grid, cfg.smem, st, p);
+    return launch_tc_cfg<IS_K1, CfgWide>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
+  return launch_tc_cfg<IS_K1, CfgNarrow>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
 }
 
 // Column-block width when k exceeds what one launch holds (each block
@@ -901,7 +979,7 @@ int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
   if (d.precision == COHERIT_PREC_FP32) return run_operator_fp32(h, d, st);
   CO_CHECK(is_tc_precision(d.precision), COHERIT_E_SHAPE, "unknown precision %d", d.precision);
   const int nsplit = nsplit_of(d.precision);
-  const int kmax = max_kp_for(h, nsplit);
+  const int kmax = max_kp_for(h, nsplit, elem_bytes(d.precision));
   if (d.k > kmax) {
     // Column blocks: each re-reads the genotypes.
     CO_CHECK(d.n_groups == 1, COHERIT_E_SHAPE,
@@ -919,7 +997,7 @@ int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
     return COHERIT_OK;
   }
   const int kp = static_cast<int>(round_up(std::max(d.k, 1), 16));
-  int rc = ensure_workspace(h, kp, nsplit, is_f16(d.precision));
+  int rc = ensure_workspace(h, kp, d.precision);
   if (rc != COHERIT_OK) return rc;
   return launch_operator(h, d, kp, nsplit, static_cast<uint8_t*>(h->ws.base), st);
 }
@@ -931,9 +1009,9 @@ int run_operator_in_scratch(coherit_geno* h, const OpDesc& d, void* scratch, siz
   CO_CHECK(is_tc_precision(d.precision), COHERIT_E_SHAPE, "unknown precision %d", d.precision);
   CO_CHECK(d.n_groups == 1, COHERIT_E_SHAPE, "the fixed-scratch operator takes one request");
   const int nsplit = nsplit_of(d.precision);
-  const int step = column_step(d.k, max_kp_for(h, nsplit));
+  const int step = column_step(d.k, max_kp_for(h, nsplit, elem_bytes(d.precision)));
   const int kp = static_cast<int>(round_up(std::max(step, 1), 16));
-  const size_t need = ws_layout(h, kp, nsplit, is_f16(d.precision)).total;
+  const size_t need = ws_layout(h, kp, d.precision).total;
   CO_CHECK(need <= bytes, COHERIT_E_SHAPE,
            "operator needs %zu bytes of scratch for n=%lld, m_pad=%lld, %d columns per launch; "
            "the fixed scratch holds %zu bytes (use coherit_geno_kv)",
@@ -955,8 +1033,9 @@ int run_operator_in_scratch(coherit_geno* h, const OpDesc& d, void* scratch, siz
 // with the workspace at `ws` (laid out by ws_layout(h, kp, nsplit)).
 static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit, uint8_t* ws,
                            cudaStream_t st) {
-  const bool f16 = is_f16(d.precision);
-  const WsLayout L = ws_layout(h, kp, nsplit, f16);
+  const bool f16 = is_scaled(d.precision);  // per-column scales (FP16 or E4M3 terms)
+  const int ty = op_type(d.precision);
+  const WsLayout L = ws_layout(h, kp, d.precision);
   EpiParams e;
   int rc = fill_epi(h, d, kp, nsplit, e);
   if (rc != COHERIT_OK) return rc;
@@ -982,7 +1061,7 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   const int nr = e.stacked ? h->G : 1;
   CO_CUDA(cudaMemsetAsync(rbuf, 0, sizeof(double) * nr * kp, st));
   if (f16) CO_CUDA(cudaMemsetAsync(smax, 0, sizeof(unsigned) * kp, st));
-  const TcLaunchCfg cfg = tc_config(h, kp, nsplit);
+  const TcLaunchCfg cfg = tc_config(h, kp, d.precision);
   const SplitPlan sp = split_plan(h, e.stacked != 0, target_ctas(h), cfg.sb);
   float* part = reinterpret_cast<float*>(ws + L.part);
   const unsigned col_blocks = static_cast<unsigned>((kp / 16 + 3) / 4);
@@ -997,7 +1076,7 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   p.err = h->d_err;
   p.n_chunks = h->n_chunks;
   p.n_panels = h->n_panels;
-  p.b_chunk_bytes = static_cast<int64_t>(nsplit) * kp * kPanel * 2;
+  p.b_chunk_bytes = static_cast<int64_t>(nsplit) * kp * kPanel * elem_bytes(d.precision);
 
   if (!d.zxb) {
     // Column means a of V, then V' = V - a split into K1's B tiles and the
@@ -1027,7 +1106,7 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
     p.part = sp.k1 > 1 ? part : nullptr;
     p.part_stride = h->m_pad * kp;
     p.part_rows = h->m_pad;
-    rc = launch_tc<true>(cfg, nsplit, f16,
+    rc = launch_tc<true>(cfg, nsplit, ty,
                          dim3(static_cast<unsigned>(h->n_ttiles), 1, static_cast<unsigned>(sp.k1)),
                          st, p);
     if (rc != COHERIT_OK) return rc;
@@ -1056,7 +1135,7 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   p.part = sp.k2 > 1 ? part : nullptr;
   p.part_stride = static_cast<int64_t>(nr) * h->n_pad * kp;
   p.part_rows = h->n_pad;
-  rc = launch_tc<false>(cfg, nsplit, f16,
+  rc = launch_tc<false>(cfg, nsplit, ty,
                         dim3(static_cast<unsigned>(h->n_stiles), static_cast<unsigned>(nr),
                              static_cast<unsigned>(sp.k2)),
                         st, p);
@@ -1107,7 +1186,7 @@ int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision) {
     return ensure_ws_bytes(h, static_cast<size_t>(h->m_pad) * kp * sizeof(float));
   CO_CHECK(is_tc_precision(precision), COHERIT_E_SHAPE, "unknown precision %d", precision);
   const int ns = nsplit_of(precision);
-  return ensure_workspace(h, std::min(kp, max_kp_for(h, ns)), ns, is_f16(precision));
+  return ensure_workspace(h, std::min(kp, max_kp_for(h, ns, elem_bytes(precision))), precision);
 }
 
 int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t precision,

@@ -25,9 +25,12 @@
 // with the number of MMAs into one accumulator), so the host bounds every
 // chain this way.
 
-template <bool IS_K1, int NSPLIT, bool SIDE, class Cfg, bool F16>
-__global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant__ TcParams p) {
+template <bool IS_K1, int NSPLIT, bool SIDE, class Cfg, int TY>
+__global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant__ TcParams p) {
   constexpr int kStageBlocks = Cfg::SB;
+  // Tensor-memory columns of one 64-K block of A: 32 for 16-bit operands,
+  // 16 for E4M3 bytes.
+  constexpr uint32_t kACols = TY == kTyE4M3 ? 16u : 32u;
   constexpr int kSets = Cfg::SETS;
   constexpr int kRG = Cfg::RG;
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -113,7 +116,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant
                         p.ksplit >= 1 && static_cast<int>(gridDim.z) == p.ksplit &&
                         (p.ksplit == 1 || p.part != nullptr) &&
                         acc_need <= p.acc_cols && (p.acc_cols & 31u) == 0 &&
-                        p.acc_cols + static_cast<uint32_t>(p.RA) * 32u * kStageBlocks <= p.tmem_cols &&
+                        p.acc_cols + static_cast<uint32_t>(p.RA) * kACols * kStageBlocks <= p.tmem_cols &&
                         p.tmem_cols >= 32 && p.tmem_cols <= 512 &&
                         (p.tmem_cols & (p.tmem_cols - 1)) == 0 && acc_need <= 256 && (e.kp & 15) == 0;
     if (!cfg_ok) {
@@ -176,9 +179,14 @@ __global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant
   } else if (warp == kWarpMMA) {
     // ------------------------------------------------------------ MMA issue
     if (lane == 0) {
-      const uint32_t idesc = F16 ? ptx::idesc_f16_f32(128, SIDE ? NSPLIT * kp : kp)
-                                 : ptx::idesc_bf16_f32(128, SIDE ? NSPLIT * kp : kp);
-      const uint64_t bdesc0 = ptx::smem_desc(ptx::smem_addr(bring), 128u, 1024u);
+      const int nn = SIDE ? NSPLIT * kp : kp;
+      const uint32_t idesc = TY == kTyE4M3 ? ptx::idesc_e4m3_f32(128, nn)
+                             : TY == kTyF16 ? ptx::idesc_f16_f32(128, nn)
+                                            : ptx::idesc_bf16_f32(128, nn);
+      // B tiles: core matrices of 8 columns x 16 bytes; a 64-K block holds
+      // 8 (16-bit) or 4 (8-bit) of them per 8-column group.
+      const uint64_t bdesc0 =
+          ptx::smem_desc(ptx::smem_addr(bring), 128u, TY == kTyE4M3 ? 512u : 1024u);
       const uint32_t term_off = static_cast<uint32_t>(kp * 128) >> 4;
       int as = 0, bs = 0;
       uint32_t pa = 0, pb = 0;
@@ -187,16 +195,21 @@ __global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant
         if (!ptx::mbar_wait(&fullB[bs], pb, p.err, 14, abort_flag)) break;
         ptx::tc_fence_after();
         const uint64_t bslot = bdesc0 + ((static_cast<uint64_t>(bs) * p.bslot_bytes) >> 4);
-        const uint32_t a_slot = tmem + p.acc_cols + static_cast<uint32_t>(as) * (32u * kStageBlocks);
+        const uint32_t a_slot =
+            tmem + p.acc_cols + static_cast<uint32_t>(as) * (kACols * kStageBlocks);
         const uint32_t first = c == 0 ? 0u : 1u;
 #pragma unroll
         for (int b = 0; b < kStageBlocks; ++b) {
           const uint64_t bblk = bslot + ((static_cast<uint64_t>(b) * p.b_chunk_bytes) >> 4);
-          const uint32_t a_col = a_slot + 32u * b;
+          const uint32_t a_col = a_slot + kACols * b;
+          // K steps of one 64-K block: 4 of 16 (16-bit) or 2 of 32 (E4M3);
+          // each advances A by 8 columns and B by two 16-byte core matrices.
 #pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
+          for (int ks = 0; ks < (TY == kTyE4M3 ? 2 : 4); ++ks) {
             const uint32_t acc0 = (b == 0 && ks == 0) ? first : 1u;
-            if (SIDE) {
+            if (TY == kTyE4M3) {
+              ptx::mma_ts_f8(tmem, a_col + ks * 8, bblk + ks * 16, idesc, acc0);
+            } else if (SIDE) {
               ptx::mma_ts(tmem, a_col + ks * 8, bblk + ks * 16, idesc, acc0);
             } else {
 #pragma unroll
@@ -255,10 +268,17 @@ __global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant
       ptx::tc_fence_after();
 #pragma unroll
       for (int b = 0; b < kStageBlocks; ++b) {
-        uint32_t a[32];
-        decode_row<F16>(raw[b], a);
-        ptx::tmem_st32(tmem + lane_base + p.acc_cols +
-                           static_cast<uint32_t>(as * kStageBlocks + b) * 32u, a);
+        const uint32_t col = tmem + lane_base + p.acc_cols +
+                             static_cast<uint32_t>(as * kStageBlocks + b) * kACols;
+        if constexpr (TY == kTyE4M3) {
+          uint32_t a[16];
+          decode_row_e4m3(raw[b], a);
+          ptx::tmem_st16(col, a);
+        } else {
+          uint32_t a[32];
+          decode_row<TY == kTyF16>(raw[b], a);
+          ptx::tmem_st32(col, a);
+        }
       }
       ptx::tmem_wait_st();
       ptx::tc_fence_before();
@@ -286,12 +306,15 @@ __global__ void __launch_bounds__(Cfg::THREADS, 2) k_tc_op(const __grid_constant
 #pragma unroll
           for (int i = 0; i < 16; ++i) T[i] = __uint_as_float(r[i]);
           if (SIDE) {
+            // Terms side by side: 16-bit terms share one scale; E4M3 term t
+            // carries 16^t (each holds the previous residual times 16).
 #pragma unroll
             for (int t = 1; t < NSPLIT; ++t) {
               ptx::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(t * kp + c0), r);
               ptx::tmem_wait_ld();
+              const float wt = TY == kTyE4M3 ? ldexpf(1.f, -4 * t) : 1.f;
 #pragma unroll
-              for (int i = 0; i < 16; ++i) T[i] += __uint_as_float(r[i]);
+              for (int i = 0; i < 16; ++i) T[i] = fmaf(wt, __uint_as_float(r[i]), T[i]);
             }
           }
         } else {

@@ -60,6 +60,13 @@ extern "C" {
 #define COHERIT_PREC_BF16X2 2
 #define COHERIT_PREC_BF16X1 3
 #define COHERIT_PREC_FP16X2 4
+/*  FP8X5   : tcgen05 kind::f8f6f4 tensor cores, genotypes exact in E4M3,
+ *            right-hand sides (and S) scaled per column by a power of two and
+ *            split into five E4M3 terms (term t holds the previous residual
+ *            times 16; ~20 significant bits), FP32 accumulation; K = 32 per
+ *            instruction, half the instructions of the 16-bit forms, for
+ *            blocks of <= 48 columns. */
+#define COHERIT_PREC_FP8X5 5
 
 /* Operator output forms. */
 #define COHERIT_MODE_SUM 0      /* out = sum_g scale_g K_g V (+ theta_e V)         */

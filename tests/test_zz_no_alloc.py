@@ -110,6 +110,7 @@ def test_noalloc_stacked_wide_and_bf16x1_match_kv(cuda):
         _check_pair(h, 2, 200, 1, 1, scale=[0.5, 2.0], seed=2)
         _check_pair(h, 2, 33, 0, 3, seed=3)
         _check_pair(h, 2, 40, 0, 4, seed=4)
+        _check_pair(h, 2, 24, 1, 5, seed=5)
     finally:
         _lib.load().coherit_geno_destroy(h)
 
