@@ -524,6 +524,14 @@ def run_ours(args, wl):
     # Host copies for the end-to-end leg (pinned, as a serving front end holds them).
     ys_host = [y.cpu().pin_memory() for y in ys]
     Xs_host = [X.cpu().pin_memory() for X in Xs]
+    tuner = None
+    if not args.no_autotune:
+        # Launch configurations of the widths the batcher issues (16-column
+        # steps up to its cap), tuned on these genotypes before warm-up.
+        from coherit_gb300.serving import _MAX_BATCH_COLS
+
+        widths = list(range(16, _MAX_BATCH_COLS.get(args.precision, 80) + 1, 16))
+        tuner = st.autotune(widths, precision=args.precision, reps=1)
     srv = REMLServer(st, max_active=R, precision=args.precision, fit_kwargs=fit_kwargs(wl),
                      batch_window_s=args.batch_window)
 
@@ -681,6 +689,7 @@ def run_ours(args, wl):
                     "d2h_bytes_per_step": int(sum(r.var_components.size * 8 for r in e2e_res))},
             "gpu_launches": int(launches),
             "roofline": roof,
+            "autotune": tuner,
             "serving_stream": stream,
             "single_fit_mixed": single,
             "plain_fp32_single_fit": plain,
@@ -1022,7 +1031,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="c3s")
-    ap.add_argument("--precision", default="bf16x3")
+    ap.add_argument("--precision", default="auto",
+                    help="operator precision: auto (fp8x5 up to 48 columns, bf16x3 above), "
+                         "bf16x3, fp8x5, fp16x2")
     ap.add_argument("--requests", type=int, default=8,
                     help="concurrent fit requests per step (the serving batch)")
     ap.add_argument("--stream", type=int, default=24,
@@ -1036,6 +1047,8 @@ def main():
     ap.add_argument("--no-single", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the fixed launch policy (no tuning of the launch widths)")
     ap.add_argument("--sparse12", action="store_true",
                     help="also time the rare-variant (sparse12) operator at the workload's size")
     ap.add_argument("--write-counts", default="",

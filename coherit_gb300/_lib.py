@@ -32,6 +32,7 @@ PREC_BF16X2 = 2
 PREC_BF16X1 = 3
 PREC_FP16X2 = 4
 PREC_FP8X5 = 5
+PREC_AUTO = 6
 
 MODE_SUM = 0
 MODE_STACKED = 1
@@ -43,6 +44,7 @@ PRECISIONS = {
     "bf16x1": PREC_BF16X1,
     "fp16x2": PREC_FP16X2,
     "fp8x5": PREC_FP8X5,
+    "auto": PREC_AUTO,
 }
 
 _lock = threading.Lock()
@@ -86,6 +88,7 @@ _SIGNATURES = {
     "coherit_geno_stats_summary": (C.c_int, [_p, _i32, _p, _p, _p, _p]),
     "coherit_geno_exact_diag": (C.c_int, [_p, _i32, _p, _p]),
     "coherit_geno_reserve": (C.c_int, [_p, _i32, _i32]),
+    "coherit_geno_autotune": (C.c_int, [_p, _i32, _i32, _i32, _p, _p, _p, _p]),
     "coherit_geno_kv": (
         C.c_int,
         [_p, _i32, _i32, _i32, _p, _i64, _i32, _p, _i32, _f32, _p, _p, _i64, _p],

@@ -22,7 +22,9 @@
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
 #include <cstdint>
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/coherit_gpu.h"
@@ -167,6 +169,14 @@ struct StatsSlot {
   double atom_total = 0.0;
 };
 
+// A launch configuration chosen by the autotuner for one (columns per
+// launch, precision): stage size, ring depths and the grid the split-K plan
+// aims for (target_mult x SMs).
+struct TuneChoice {
+  int wide = 0, RA = 0, RB = 0, target_mult = 4;
+  float ms = 0.f;
+};
+
 struct Workspace {
   void* base = nullptr;
   size_t bytes = 0;
@@ -198,6 +208,7 @@ struct coherit_geno {
   int32_t* d_csr_idx = nullptr;
   std::vector<coherit::StatsSlot> slots;
   coherit::Workspace ws;
+  std::map<std::pair<int, int>, coherit::TuneChoice> tuned;  // (kp, precision)
   int* d_err = nullptr;
   int sm_count = 0;
   int smem_optin = 232448;   // max dynamic shared memory per CTA
@@ -251,6 +262,12 @@ int ensure_workspace(coherit_geno* h, int32_t k_max, int32_t precision);
 int ensure_ws_bytes(coherit_geno* h, size_t bytes);
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+// AUTO resolves per launch width: E4M3 terms up to 48 columns, BF16x3 above.
+constexpr int kAutoFp8MaxCols = 48;
+inline int resolve_precision(int precision, int32_t k) {
+  if (precision != COHERIT_PREC_AUTO) return precision;
+  return round_up(k > 0 ? k : 1, 16) <= kAutoFp8MaxCols ? COHERIT_PREC_FP8X5 : COHERIT_PREC_BF16X3;
+}
 inline int nsplit_of(int precision) {
   if (precision == COHERIT_PREC_FP8X5) return 5;
   return precision == COHERIT_PREC_BF16X3 ? 3

@@ -737,7 +737,18 @@ static SplitPlan split_plan(const coherit_geno* h, bool stacked, int64_t target_
 }
 
 // Grid size that fills about two waves of the operator kernel.
-static int64_t target_ctas(const coherit_geno* h) { return 4LL * std::max(h->sm_count, 1); }
+// Grid size the split-K plan fills: about two waves (4 x SMs), or the
+// autotuner's choice for this width and precision.  Partial buffers are sized
+// for the largest multiple the tuner tries.
+constexpr int kDefaultTargetMult = 4;
+constexpr int kMaxTargetMult = 8;
+static int64_t target_ctas(const coherit_geno* h, int mult = kDefaultTargetMult) {
+  return static_cast<int64_t>(mult) * std::max(h->sm_count, 1);
+}
+static int64_t target_ctas_for(const coherit_geno* h, int kp, int precision) {
+  const auto it = h->tuned.find({kp, precision});
+  return target_ctas(h, it == h->tuned.end() ? kDefaultTargetMult : it->second.target_mult);
+}
 
 struct WsLayout {
   size_t vt, sbuf, cs_part, mx_part, cs, shift, vscale, smax, rbuf, vmiss, sf32, part, total;
@@ -752,7 +763,7 @@ static int64_t part_rows_needed(const coherit_geno* h) {
   for (int q = 0; q < 4; ++q) {
     const bool stacked = (q & 1) != 0;
     const int sb = (q & 2) ? CfgWide::SB : CfgNarrow::SB;
-    const SplitPlan s = split_plan(h, stacked, target_ctas(h), sb);
+    const SplitPlan s = split_plan(h, stacked, target_ctas(h, kMaxTargetMult), sb);
     if (s.k1 > 1) rows = std::max<int64_t>(rows, s.k1 * h->m_pad);
     if (s.k2 > 1) rows = std::max<int64_t>(rows, s.k2 * s.nr * h->n_pad);
   }
@@ -872,7 +883,23 @@ struct TcLaunchCfg {
 // wide form where its B ring (>= 2 stages) fits shared memory, else the
 // narrow form; always one CTA per SM, which allocates all 512 tensor-memory
 // columns so no second CTA can share the SM.
+static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision, int want_wide,
+                                    int ra_req, int rb_req);
+
+// Launch configuration: the autotuner's choice for (kp, precision) when there
+// is one, else the fixed policy below.
 static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int precision) {
+  const auto it = h->tuned.find({kp, precision});
+  if (it != h->tuned.end())
+    return tc_config_policy(h, kp, precision, it->second.wide, it->second.RA, it->second.RB);
+  return tc_config_policy(h, kp, precision, -1, 0, 0);
+}
+
+// want_wide: -1 policy, 0 two-block stages, 1 four-block stages (if their
+// rings fit); ra_req / rb_req: ring depths (0 = largest that fits), clamped
+// to what fits tensor memory, shared memory and the barrier arrays.
+static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision, int want_wide,
+                                    int ra_req, int rb_req) {
   const int nsplit = nsplit_of(precision);
   const int eb = elem_bytes(precision);
   // Tensor-memory columns of one 64-K block of A (E4M3: one byte per code).
@@ -882,7 +909,7 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int precision) {
   const int acc = c.side ? nsplit * kp : kp;
   c.acc_cols = static_cast<uint32_t>(round_up(acc, 32));
   const size_t cap = static_cast<size_t>(h->smem_optin);
-  {
+  if (want_wide != 0) {
     // Four-block stages (half the barrier round trips per K of two-block
     // stages) wherever their rings fit: at one CTA per SM they apply 16
     // columns faster than two-block stages (n = 50,000, m = 500,000: k = 32
@@ -890,7 +917,8 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int precision) {
     const uint32_t slot = acols * CfgWide::SB;
     const uint32_t bslot = static_cast<uint32_t>(CfgWide::SB) * nsplit * kp * kPanel * eb;
     const size_t fixed = kBarrierBytes + static_cast<size_t>(CfgWide::RG) * CfgWide::SB * kBlockBytes;
-    const int ra = std::min<int>(kMaxRA, static_cast<int>((512u - c.acc_cols) / slot));
+    int ra = std::min<int>(kMaxRA, static_cast<int>((512u - c.acc_cols) / slot));
+    if (ra_req > 0) ra = std::min(ra, std::max(ra_req, CfgWide::MIN_RA));
     if (c.acc_cols + CfgWide::MIN_RA * slot <= 512u && ra >= CfgWide::MIN_RA &&
         fixed + 2 * static_cast<size_t>(bslot) <= cap - 4096) {
       c.wide = true;
@@ -899,6 +927,7 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int precision) {
       c.RA = ra;
       c.bslot = bslot;
       int rb = static_cast<int>((cap - 4096 - fixed) / bslot);
+      if (rb_req > 0) rb = std::min(rb, rb_req);
       c.RB = std::max(2, std::min(kMaxRB, rb));
       c.smem = fixed + static_cast<size_t>(c.RB) * bslot;
       return c;
@@ -914,12 +943,14 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int precision) {
   const uint32_t cols = 512;
   c.tmem_cols = cols;
   c.RA = std::min<int>(kMaxRA, static_cast<int>((cols - c.acc_cols) / slot_cols));
+  if (ra_req > 0) c.RA = std::min(c.RA, std::max(ra_req, CfgNarrow::MIN_RA));
   c.bslot = static_cast<uint32_t>(CfgNarrow::SB) * nsplit * kp * kPanel * eb;
   const size_t fixed =
       kBarrierBytes + static_cast<size_t>(CfgNarrow::RG) * CfgNarrow::SB * kBlockBytes;
   const int ctas_tmem = 512 / static_cast<int>(cols);
   const size_t target = ctas_tmem >= 2 ? std::min<size_t>(112 * 1024, cap) : cap - 4096;
   int rb = static_cast<int>((target - fixed) / c.bslot);
+  if (rb_req > 0) rb = std::min(rb, rb_req);
   rb = std::max(2, std::min(kMaxRB, rb));
   while (rb > 2 && fixed + static_cast<size_t>(rb) * c.bslot > cap) --rb;
   c.RB = rb;
@@ -976,6 +1007,24 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
                            cudaStream_t st);
 
 int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
+  if (d.precision == COHERIT_PREC_AUTO) {
+    OpDesc r = d;
+    r.precision = resolve_precision(d.precision, d.k);
+    if (r.precision == COHERIT_PREC_FP8X5 || d.k <= max_kp_for(h, 3, 2) || d.n_groups > 1)
+      return run_operator(h, r, st);
+    // Wider than one BF16x3 launch: column blocks, each resolved by width.
+    const int step = column_step(d.k, max_kp_for(h, 3, 2));
+    for (int c0 = 0; c0 < d.k; c0 += step) {
+      OpDesc s = d;
+      s.k = std::min(step, d.k - c0);
+      s.V = d.V + c0;
+      s.out = d.out + c0;
+      s.col_start = {0, s.k};
+      int rc = run_operator(h, s, st);
+      if (rc != COHERIT_OK) return rc;
+    }
+    return COHERIT_OK;
+  }
   if (d.precision == COHERIT_PREC_FP32) return run_operator_fp32(h, d, st);
   CO_CHECK(is_tc_precision(d.precision), COHERIT_E_SHAPE, "unknown precision %d", d.precision);
   const int nsplit = nsplit_of(d.precision);
@@ -1002,8 +1051,11 @@ int run_operator(coherit_geno* h, const OpDesc& d, cudaStream_t st) {
   return launch_operator(h, d, kp, nsplit, static_cast<uint8_t*>(h->ws.base), st);
 }
 
-int run_operator_in_scratch(coherit_geno* h, const OpDesc& d, void* scratch, size_t bytes,
+int run_operator_in_scratch(coherit_geno* h, const OpDesc& d0, void* scratch, size_t bytes,
                             cudaStream_t st) {
+  OpDesc d = d0;
+  if (d.precision == COHERIT_PREC_AUTO)
+    d.precision = resolve_precision(d.precision, std::min<int32_t>(d.k, kAutoFp8MaxCols + 1));
   CO_CHECK(d.precision != COHERIT_PREC_FP32, COHERIT_E_UNSUPPORTED,
            "the fixed-scratch operator runs the tensor-core precisions only");
   CO_CHECK(is_tc_precision(d.precision), COHERIT_E_SHAPE, "unknown precision %d", d.precision);
@@ -1062,7 +1114,7 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   CO_CUDA(cudaMemsetAsync(rbuf, 0, sizeof(double) * nr * kp, st));
   if (f16) CO_CUDA(cudaMemsetAsync(smax, 0, sizeof(unsigned) * kp, st));
   const TcLaunchCfg cfg = tc_config(h, kp, d.precision);
-  const SplitPlan sp = split_plan(h, e.stacked != 0, target_ctas(h), cfg.sb);
+  const SplitPlan sp = split_plan(h, e.stacked != 0, target_ctas_for(h, kp, d.precision), cfg.sb);
   float* part = reinterpret_cast<float*>(ws + L.part);
   const unsigned col_blocks = static_cast<unsigned>((kp / 16 + 3) / 4);
 
@@ -1184,9 +1236,130 @@ int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision) {
   const int kp = static_cast<int>(round_up(std::max(k_max, 1), 16));
   if (precision == COHERIT_PREC_FP32)
     return ensure_ws_bytes(h, static_cast<size_t>(h->m_pad) * kp * sizeof(float));
+  if (precision == COHERIT_PREC_AUTO) {
+    // Both forms AUTO may pick: E4M3 up to 48 columns, BF16x3 above.
+    int rc = coherit_geno_reserve(h, std::min(k_max, kAutoFp8MaxCols), COHERIT_PREC_FP8X5);
+    if (rc != COHERIT_OK || k_max <= kAutoFp8MaxCols) return rc;
+    return coherit_geno_reserve(h, k_max, COHERIT_PREC_BF16X3);
+  }
   CO_CHECK(is_tc_precision(precision), COHERIT_E_SHAPE, "unknown precision %d", precision);
   const int ns = nsplit_of(precision);
   return ensure_workspace(h, std::min(kp, max_kp_for(h, ns, elem_bytes(precision))), precision);
+}
+
+int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32_t reps,
+                          int32_t* choice, float* best_ms, float* default_ms, void* stream) {
+  CO_CHECK(h != nullptr, COHERIT_E_CLOSED, "genotype handle is closed");
+  CO_CHECK(k >= 1 && reps >= 1, COHERIT_E_SHAPE, "autotune needs k >= 1 and reps >= 1");
+  const int prec = resolve_precision(precision, k);
+  CO_CHECK(is_tc_precision(prec), COHERIT_E_UNSUPPORTED,
+           "the autotuner tunes the tensor-core precisions only");
+  const int ns = nsplit_of(prec);
+  const int kp = static_cast<int>(round_up(k, 16));
+  CO_CHECK(kp <= max_kp_for(h, ns, elem_bytes(prec)), COHERIT_E_SHAPE,
+           "autotune width %d exceeds one launch (%d columns)", k,
+           max_kp_for(h, ns, elem_bytes(prec)));
+  CO_CHECK(!h->slots.empty() && h->slots[0].used, COHERIT_E_INDEX, "stats slot 0 is not initialised");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const std::pair<int, int> key{kp, prec};
+  h->tuned.erase(key);
+  int rc = ensure_workspace(h, kp, prec);
+  if (rc != COHERIT_OK) return rc;
+  float* buf = nullptr;
+  CO_CUDA(cudaMalloc(&buf, sizeof(float) * 2 * h->n * kp));
+  CO_CUDA(cudaMemsetAsync(buf, 0, sizeof(float) * h->n * kp, st));
+  OpDesc d;
+  rc = make_single(h, 0, kp, nullptr, d);
+  d.mode = COHERIT_MODE_SUM;
+  d.precision = prec;
+  d.V = buf;
+  d.ldv = kp;
+  d.out = buf + h->n * kp;
+  d.ldo = kp;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  auto time_once = [&](float& ms) -> int {
+    int r = run_operator(h, d, st);  // warm
+    if (r != COHERIT_OK) return r;
+    CO_CUDA(cudaEventRecord(e0, st));
+    for (int i = 0; i < reps && r == COHERIT_OK; ++i) r = run_operator(h, d, st);
+    if (r != COHERIT_OK) return r;
+    CO_CUDA(cudaEventRecord(e1, st));
+    CO_CUDA(cudaEventSynchronize(e1));
+    CO_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    ms /= static_cast<float>(reps);
+    return COHERIT_OK;
+  };
+  float t_def = 0.f;
+  if (rc == COHERIT_OK && ce == cudaSuccess) rc = time_once(t_def);
+  // Candidates: stage size x A-ring depth x B-ring depth x split-K grid.
+  TuneChoice best;
+  best.ms = t_def;
+  {
+    const TcLaunchCfg c0 = tc_config_policy(h, kp, prec, -1, 0, 0);
+    best.wide = c0.wide ? 1 : 0;
+    best.RA = c0.RA;
+    best.RB = c0.RB;
+    best.target_mult = kDefaultTargetMult;
+  }
+  int tried = 0;
+  for (int wide = 1; wide >= 0 && rc == COHERIT_OK && ce == cudaSuccess; --wide) {
+    const TcLaunchCfg full = tc_config_policy(h, kp, prec, wide, 0, 0);
+    if ((full.wide ? 1 : 0) != wide) continue;  // four-block rings do not fit
+    const int ra_min = wide ? CfgWide::MIN_RA : CfgNarrow::MIN_RA;
+    const int ras[2] = {full.RA, std::max(ra_min, full.RA / 2)};
+    const int rbs[3] = {full.RB, std::max(2, full.RB / 2), 2};
+    for (int ia = 0; ia < 2 && rc == COHERIT_OK; ++ia) {
+      if (ia == 1 && ras[1] == ras[0]) continue;
+      for (int ib = 0; ib < 3 && rc == COHERIT_OK; ++ib) {
+        if ((ib == 1 && rbs[1] == rbs[0]) || (ib == 2 && (rbs[2] == rbs[1] || rbs[2] == rbs[0])))
+          continue;
+        for (int mult = 2; mult <= kMaxTargetMult && rc == COHERIT_OK; mult *= 2) {
+          TuneChoice c;
+          c.wide = wide;
+          c.RA = ras[ia];
+          c.RB = rbs[ib];
+          c.target_mult = mult;
+          h->tuned[key] = c;
+          float ms = 0.f;
+          rc = time_once(ms);
+          ++tried;
+          if (rc == COHERIT_OK && ms < best.ms) {
+            best = c;
+            best.ms = ms;
+          }
+        }
+      }
+    }
+  }
+  h->tuned[key] = best;
+  if (rc == COHERIT_OK && ce == cudaSuccess) {
+    int herr = 0;
+    ce = cudaMemcpy(&herr, h->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess && herr != 0) {
+      set_error("operator kernel reported error %d while tuning", herr);
+      rc = COHERIT_E_CUDA;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (rc != COHERIT_OK) {
+    h->tuned.erase(key);
+    return rc;
+  }
+  if (ce != cudaSuccess) return cuda_status(ce, "autotune");
+  if (choice) {
+    choice[0] = best.wide;
+    choice[1] = best.RA;
+    choice[2] = best.RB;
+    choice[3] = best.target_mult;
+    choice[4] = tried;
+  }
+  if (best_ms) *best_ms = best.ms;
+  if (default_ms) *default_ms = t_def;
+  return COHERIT_OK;
 }
 
 int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t precision,

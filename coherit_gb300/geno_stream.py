@@ -557,6 +557,25 @@ class GenoBlockStreamer:
         prec = _lib.PRECISIONS[precision or self.precision]
         _lib.check(self._lib.coherit_geno_reserve(self._h(), int(k_max), prec), "reserve")
 
+    def autotune(self, widths, precision: str | None = None, reps: int = 2) -> list:
+        """Time candidate launch configurations of the operator for each
+        width (stage size, ring depths, split-K grid) on these genotypes and
+        keep the fastest for later launches of that width and precision
+        (coherit_geno_autotune).  Returns one record per width."""
+        out = []
+        prec = self._prec_code(precision)
+        for k in widths:
+            ch = (C.c_int32 * 5)()
+            best, dflt = C.c_float(), C.c_float()
+            _lib.check(self._lib.coherit_geno_autotune(
+                self._h(), int(k), prec, int(reps), ch, C.byref(best), C.byref(dflt),
+                _lib.stream_ptr()), "autotune")
+            out.append({"k": int(k), "precision": precision or self.precision,
+                        "four_block_stages": bool(ch[0]), "a_ring": int(ch[1]),
+                        "b_ring": int(ch[2]), "grid_x_sms": int(ch[3]), "candidates": int(ch[4]),
+                        "best_ms": round(best.value, 4), "default_ms": round(dflt.value, 4)})
+        return out
+
     def _prec_code(self, precision) -> int:
         return self._prec if precision is None else _lib.PRECISIONS[precision]
 

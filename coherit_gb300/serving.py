@@ -41,7 +41,8 @@ from .reml import REMLProbeCache, fit_reml, prime_probe_cache
 
 # Widest right-hand-side block one batched launch takes per precision: the
 # split terms of all columns sit side by side in one MMA (N <= 256).
-_MAX_BATCH_COLS = {"bf16x3": 80, "bf16x2": 128, "bf16x1": 256}
+_MAX_BATCH_COLS = {"bf16x3": 80, "bf16x2": 128, "bf16x1": 256, "fp16x2": 128, "fp8x5": 48,
+                   "auto": 80}
 
 
 @dataclasses.dataclass

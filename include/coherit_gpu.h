@@ -67,6 +67,10 @@ extern "C" {
  *            instruction, half the instructions of the 16-bit forms, for
  *            blocks of <= 48 columns. */
 #define COHERIT_PREC_FP8X5 5
+/*  AUTO    : per launch, FP8X5 for blocks of <= 48 columns (half the MMA
+ *            instructions where their count bounds the time) and BF16X3 for
+ *            wider blocks; both hold the 1e-5 operator bound. */
+#define COHERIT_PREC_AUTO 6
 
 /* Operator output forms. */
 #define COHERIT_MODE_SUM 0      /* out = sum_g scale_g K_g V (+ theta_e V)         */
@@ -224,6 +228,22 @@ int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision);
  * Replaces kv_impl_streamed (kv_impl.py:268-326), kv_impl_partitioned_weighted
  * (:1089-1135), kv_impl_partitioned_stacked (:1138-1187),
  * kv_impl_snp_weighted_streamed (:329-379).                                 */
+/* Launch-configuration autotuner (no counterpart in the reference, whose
+ * jitted kernels have no tunable launch shape).  Times the operator at width
+ * k (one launch, <= 80 columns at BF16X3, 48 at FP8X5, 128 at FP16X2) and
+ * `precision` (AUTO resolves by width) on this handle's genotypes and stats
+ * slot 0 under each candidate configuration -- two- or four-block pipeline
+ * stages, tensor-memory A-ring depth, shared-memory B-ring depth, and the
+ * grid size (2, 4 or 8 x SMs) the split-K plan fills -- `reps` timed
+ * applications each (CUDA events on `stream`), and keeps the fastest for
+ * every later launch of that width and precision on the handle.  Allocates
+ * and frees two n x k buffers; synchronises `stream`.  choice (5 ints, may
+ * be NULL): four-block stages (0/1), A-ring slots, B-ring slots, grid
+ * multiple, candidates tried; best_ms / default_ms: per-application times of
+ * the kept and of the fixed-policy configuration.                          */
+int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32_t reps,
+                          int32_t* choice, float* best_ms, float* default_ms, void* stream);
+
 int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t precision,
                     const float* V, int64_t ldv, int32_t k, const float* comp_scale,
                     int32_t use_theta_e, float theta_e, const float* snp_weight,

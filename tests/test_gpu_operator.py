@@ -91,7 +91,7 @@ def test_array_source_round_trip_and_partition(cuda):
         st.kv(np.zeros((n, 1), np.float32))
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16x3", "fp16x2", "fp8x5"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3", "fp16x2", "fp8x5", "auto"])
 @pytest.mark.parametrize("n,m,k,miss", [
     (1000, 3000, 7, 0.0),
     (1000, 3000, 7, 0.03),
@@ -175,7 +175,8 @@ def test_xtv_zxb_exact_diag(cuda, precision):
                                rtol=1e-6)
 
 
-@pytest.mark.parametrize("prec", [_lib.PREC_BF16X3, _lib.PREC_FP16X2, _lib.PREC_FP8X5])
+@pytest.mark.parametrize("prec", [_lib.PREC_BF16X3, _lib.PREC_FP16X2, _lib.PREC_FP8X5,
+                                  _lib.PREC_AUTO])
 def test_batched_subsets_equal_single_requests(cuda, prec):
     n, m = 700, 1600
     st = _streamer(n, m, seed=19, miss=0.01, precision="bf16x3")
@@ -390,5 +391,28 @@ def test_mean_heavy_columns_at_n120000(cuda, precision):
         z[codes == 3] = 0.0
         ref[s0:s0 + w] = (z.T @ V.double()).cpu().numpy()
     assert col_rel(xt, ref) < tol
+    st.check()
+    st.close()
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "fp8x5"])
+def test_autotuned_configuration_keeps_parity(cuda, precision):
+    """The autotuner's kept configuration (stage size, ring depths, split-K
+    grid) gives the same operator within 1e-5 of FP64, and reports a valid
+    choice no slower than the fixed policy."""
+    n, m, k = 3000, 9000, 20
+    st = _streamer(n, m, seed=37, miss=0.01, precision=precision)
+    codes = oracle_codes(37, n, m, 0.01)
+    rec = st.autotune([k, 7], reps=1)
+    assert len(rec) == 2
+    for r in rec:
+        assert r["candidates"] >= 2 and r["a_ring"] >= 2 and 2 <= r["b_ring"] <= 16
+        assert r["grid_x_sms"] in (2, 4, 8)
+        assert r["best_ms"] <= r["default_ms"] * 1.0001
+    V = np.random.default_rng(8).normal(size=(n, k)).astype(np.float32)
+    out = st.kv(torch.as_tensor(V, device=cuda)).cpu().numpy()
+    ref = og.kv_f64(codes, st._means_host, st._inv_sds_host, V,
+                    comp_scale=[1 / float(st._eff_m_const)])
+    assert col_rel(out, ref) < TOL
     st.check()
     st.close()
