@@ -213,6 +213,25 @@ class _OperatorBundle:
     projected_core_atoms: object | None = None
 
 
+def _theta_ref_from_var_components(G: int, var_components_init=None) -> np.ndarray:
+    """Weights of the preconditioner's reference kernel sum_g theta_ref,g K_g
+    (reml_model.py:808-832): the first G variance components clamped at zero
+    and normalised to sum 1; uniform 1/G without them or when they sum to
+    zero or a non-finite value."""
+    if var_components_init is None:
+        th = np.ones(G, dtype=np.float32)
+    else:
+        th0 = np.asarray(var_components_init, dtype=np.float32).reshape(-1)
+        if th0.size < G:
+            raise ValueError(f"var_components_init length mismatch: expected at least {G}, "
+                             f"got {th0.size}.")
+        th = np.maximum(th0[:G], 0.0)
+    total = float(np.sum(th))
+    if total <= 0.0 or not np.isfinite(total):
+        return np.full(G, 1.0 / max(1, G), dtype=np.float64)
+    return (th / np.float32(total)).astype(np.float64)
+
+
 class InfinitesimalREMLFitter:
     """Fit the infinitesimal (multi-)GRM REML model on resident genotypes."""
 
@@ -419,11 +438,7 @@ class InfinitesimalREMLFitter:
         G = len(ops.K_mvs)
         atoms = np.asarray([float(torch.as_tensor(d).double().mean()) for d in ops.diag_list])
         if theta_ref is None:
-            if var_components_init is not None:
-                theta_ref = np.asarray(var_components_init, float)[:G]
-            else:
-                theta_ref = np.where(atoms > 0, 1.0 / max(float(np.sum(atoms)), 1e-12), 0.0)
-        theta_ref = np.asarray(theta_ref, float)
+            theta_ref = _theta_ref_from_var_components(G, var_components_init)
         sk = cfg.sketch_precision
         if self._smile_operators:
             def K_ref(V):
@@ -531,7 +546,7 @@ class InfinitesimalREMLFitter:
         conf = self.precond_conf if precond and cfg.precond_rank > 0 else None
         refresh = None
         if conf is not None and G > 1:
-            refresh = lambda p: self._build_projected_core_precond(ops, theta_ref=np.asarray(p)[:G])
+            refresh = lambda p: self._build_projected_core_precond(ops, var_components_init=p)
         reps = []
         n_reps = max(1, int(cfg.n_reml_reps))
         for r in range(n_reps):
