@@ -437,7 +437,8 @@ def serve_step(srv, ys, Xs, host: bool):
 
 
 def serving_stream(st, wl, n_requests: int, rate_per_s: float, seed: int, max_active: int,
-                   min_subset: int | None = None):
+                   min_subset: int | None = None, precision: str = "bf16x3",
+                   precond_rank: int = 0):
     """A bounded stream of heterogeneous requests with Poisson arrivals over
     the resident genotypes (the serving workload's request mix on this
     matrix): each request a random sample subset (size log-uniform in
@@ -470,8 +471,9 @@ def serving_stream(st, wl, n_requests: int, rate_per_s: float, seed: int, max_ac
         X = np.column_stack([np.ones(size), rng.normal(size=(size, p))]).astype(np.float32)
         reqs.append((y, X, mask))
     gaps = rng.exponential(1.0 / rate_per_s, size=n_requests)
-    srv = REMLServer(st, max_active=max_active, fit_kwargs=fit_kwargs(wl))
-    b0 = srv.batcher.launches
+    srv = REMLServer(st, max_active=max_active, precision=precision, fit_kwargs=fit_kwargs(wl),
+                     precond_rank=precond_rank)
+    b0, c0 = srv.batcher.launches, srv.batcher.columns
     t0 = time.perf_counter()
     futs = []
     for (y, X, mask), gap in zip(reqs, gaps):
@@ -487,6 +489,7 @@ def serving_stream(st, wl, n_requests: int, rate_per_s: float, seed: int, max_ac
         wall = time.perf_counter() - t0
         per_launch = list(srv.batcher.requests_per_launch)
         launches = srv.batcher.launches - b0
+        columns = srv.batcher.columns - c0
     finally:
         srv.close()
     lat = [r.latency for r in res] or [float("nan")]
@@ -497,8 +500,11 @@ def serving_stream(st, wl, n_requests: int, rate_per_s: float, seed: int, max_ac
                           "p99": round(_percentile(lat, 0.99), 3)},
             "subset_sizes": [int(m.sum()) for _, _, m in reqs][:8],
             "operator_launches": launches,
+            "operator_launches_per_fit": round(launches / max(len(res), 1), 1),
+            "rhs_columns_per_launch": round(columns / max(launches, 1), 1),
             "mean_requests_per_launch": round(float(np.mean(per_launch)), 2) if per_launch else 0.0,
-            "max_active": max_active, "seed": seed}
+            "max_active": max_active, "precision": precision, "precond_rank": precond_rank,
+            "seed": seed}
 
 
 def run_ours(args, wl):
@@ -635,7 +641,8 @@ def run_ours(args, wl):
         stream = None
         if args.stream > 0:
             stream = serving_stream(st, wl, args.stream, args.stream_rate, seed=wl.seed + 99,
-                                    max_active=R)
+                                    max_active=R, precision=args.precision,
+                                    precond_rank=args.stream_precond)
         sparse = None
         if args.sparse12:
             sparse = sparse12_operator(wl.n, wl.m, k_typ, hbm_peak, roof["ms_per_application"],
@@ -703,9 +710,41 @@ def run_ours(args, wl):
                            "rhs_columns_per_fit": fit_cols,
                            "source": "bench.py serving run (timed fits)"}, f, indent=1)
     st.close()
+    if result is not None and args.c4_stream > 0:
+        result["serving_stream_c4"] = c4_stream(args, dev)
     if dist is not None:
         dist.destroy_process_group()
     return result
+
+
+def c4_stream(args, dev):
+    """The c4 serving workload, bounded: ``--c4-stream`` requests (of c4's
+    512) over one resident n=200,000 x m=600,000 matrix, sample subsets
+    log-uniform in [1e4, 2e5], 1-20 covariates, h2 ~ U(0.05, 0.8), Poisson
+    arrivals at ``--c4-rate`` per second, 8 fits in flight.  Runs after the
+    headline workload's matrix is released."""
+    import torch
+
+    from coherit_gb300.configs import C4, C4_SUBSET_MIN
+    from coherit_gb300.serving import _MAX_BATCH_COLS
+
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    st = build_problem(C4, dev)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    try:
+        if not args.no_autotune:
+            st.autotune(list(range(16, _MAX_BATCH_COLS.get(args.precision, 80) + 1, 16)),
+                        precision=args.precision, reps=1)
+        out = serving_stream(st, C4, args.c4_stream, args.c4_rate, seed=C4.seed + 99,
+                             max_active=8, min_subset=C4_SUBSET_MIN, precision=args.precision,
+                             precond_rank=args.stream_precond)
+    finally:
+        st.close()
+    out.update({"workload": C4.name, "n": C4.n, "m": C4.m, "build_s": round(build_s, 2),
+                "note": f"first {args.c4_stream} requests of the 512-request c4 stream"})
+    return out
 
 
 METRIC = ("REML fits/hr, p50/p99 latency: mixed-precision batched serving form "
@@ -1000,12 +1039,47 @@ def run_stream_only(args, wl):
     sampler.start()
     out = serving_stream(st, wl, args.stream, args.stream_rate, seed=wl.seed + 99,
                          max_active=args.requests,
-                         min_subset=C4_SUBSET_MIN if wl.name.startswith("c4") else None)
+                         min_subset=C4_SUBSET_MIN if wl.name.startswith("c4") else None,
+                         precision=args.precision, precond_rank=args.stream_precond)
     clocks = sampler.stop()
     st.close()
     out.update({"metric": "REML fits/hr over a Poisson request stream", "config": wl.name,
                 "n": wl.n, "m": wl.m, "build_s": round(build_s, 2), "clocks": clocks})
     return out
+
+
+def run_mma_rate(args, wl):
+    """Tensor-core issue-rate table (``--mma-rate``): cycles per tcgen05.mma
+    (M = 128, A in tensor memory) by operand kind, width N and issuing threads
+    per SM, with the aggregate rate of all SMs (CUDA events) as TFLOP/s.  The
+    operator's narrow launches are bound by this rate, not by HBM."""
+    import ctypes as C
+
+    import torch
+
+    from coherit_gb300 import _lib
+
+    torch.cuda.set_device(0)
+    lib = _lib.load()
+    iters = 1 << 14
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    _, tensor_peak, peak_src = _peaks()
+    rows = []
+    for kind, kname, kk in ((0, "bf16", 16), (1, "e4m3", 32)):
+        for issuers in (1, 2):
+            for n in (16, 32, 48, 64, 80, 96, 128, 160, 192, 224, 256):
+                if issuers == 2 and n > 224:
+                    continue
+                cyc, ms = C.c_double(), C.c_double()
+                _lib.check(lib.coherit_mma_rate(kind, n, issuers, iters, C.byref(cyc),
+                                                C.byref(ms), _lib.stream_ptr()), "mma rate")
+                flops = 2.0 * 128 * n * kk * iters * issuers * sms
+                rows.append({"kind": kname, "N": n, "issuers": issuers,
+                             "cycles_per_mma": round(cyc.value, 1),
+                             "tflops": round(flops / (ms.value * 1e-3) / 1e12, 1)})
+    return {"metric": "tcgen05.mma issue rate", "unit": "cycles per instruction",
+            "iters": iters, "sms": sms, "peak_tflops": tensor_peak, "peak_source": peak_src,
+            "rows": rows}
 
 
 def run_sparse_only(args, wl):
@@ -1040,6 +1114,13 @@ def main():
                     help="requests in the Poisson-arrival subset stream (0 = skip)")
     ap.add_argument("--stream-rate", type=float, default=2.0,
                     help="stream arrivals per second (Poisson)")
+    ap.add_argument("--stream-precond", type=int, default=0,
+                    help="projected-core preconditioner rank of the streamed fits (0 = none)")
+    ap.add_argument("--c4-stream", type=int, default=16,
+                    help="requests of the c4 serving stream (200k x 600k) run after the "
+                         "headline workload (0 = skip)")
+    ap.add_argument("--c4-rate", type=float, default=0.5,
+                    help="c4 stream arrivals per second (Poisson)")
     ap.add_argument("--batch-window", type=float, default=0.01,
                     help="seconds the batcher waits for the other active fits")
     ap.add_argument("--single-fits", type=int, default=3,
@@ -1061,13 +1142,17 @@ def main():
                     help="run only the Poisson request stream on the workload's matrix")
     ap.add_argument("--sparse", type=int, default=0, metavar="K",
                     help="time the rare-variant operator at width K instead of fits")
+    ap.add_argument("--mma-rate", action="store_true",
+                    help="print the tensor-core instruction issue-rate table")
     ap.add_argument("--n", type=int, default=0, help="with --operator/--sparse: samples")
     ap.add_argument("--m", type=int, default=0, help="with --operator/--sparse: SNPs")
     args = ap.parse_args()
     from coherit_gb300.configs import WORKLOADS
 
     wl = WORKLOADS[args.config]
-    if args.operator > 0:
+    if args.mma_rate:
+        out = run_mma_rate(args, wl)
+    elif args.operator > 0:
         out = run_operator_only(args, wl)
     elif args.sparse > 0:
         out = run_sparse_only(args, wl)

@@ -37,6 +37,7 @@ import torch
 
 from . import _lib
 from .geno_stream import GenoBlockStreamer
+from .precond import ProjectedCorePrecondConf, build_lowrank_basis
 from .reml import REMLProbeCache, fit_reml, prime_probe_cache
 
 # Widest right-hand-side block one batched launch takes per precision: the
@@ -285,12 +286,21 @@ class REMLServer:
     sample count and right-hand-side width; default half the free memory).
     ``fit_kwargs`` go to ``fit_reml`` (defaults: 30 trace probes, 30 SLQ
     probes x 30 Lanczos steps, PCG tol 1e-5, 20 AI iterations).
+
+    ``precond_rank`` > 0 gives every fit's PCG solves a projected-core
+    preconditioner of that rank (reml_model.py:863-960, single GRM): a
+    Nystrom basis U of the request's own kernel (K over its sample subset)
+    from two operator applications of width rank + 8, which join the other
+    fits' launches, and the core diag(eigenvalues) - atom I.  Full-cohort
+    requests share one.  It changes how fast PCG converges, not the
+    solutions it converges to; the SLQ log-determinant is not preconditioned
+    (the affine SLQ form takes none).
     """
 
     def __init__(self, streamer: GenoBlockStreamer, *, max_active: int = 8,
                  hbm_budget_bytes: float | None = None, precision: str = "bf16x3",
                  batch_window_s: float = 0.01, max_batch_cols: int | None = None,
-                 fit_kwargs: dict | None = None):
+                 fit_kwargs: dict | None = None, precond_rank: int = 0):
         if streamer.n_components != 1:
             raise ValueError("REMLServer serves single-GRM fits (one genotype component).")
         if precision not in _MAX_BATCH_COLS:
@@ -329,6 +339,9 @@ class REMLServer:
         self._full_cache = REMLProbeCache()
         self._full_cache_key = None
         self._full_cache_lock = threading.Lock()
+        self.precond_rank = max(0, int(precond_rank))
+        self._full_precond = None
+        self._full_precond_lock = threading.Lock()
         self._cv = threading.Condition()
         self._waiting: deque[_Request] = deque()
         self._active = 0
@@ -478,6 +491,33 @@ class REMLServer:
         req.eff, req.atom = float(et.value), float(at.value)
         req.idx = torch.as_tensor(np.flatnonzero(req.mask), dtype=torch.long, device=st.dev)
 
+    def _projected_core(self, K, req: _Request):
+        """Projected-core preconditioner of one request's kernel K (single
+        GRM, reml_model.py:863-960 with uniform reference weight 1): Nystrom
+        basis U, eigenvalues e of U^T K U, core diag(e) - atom I, identity
+        diagonal atom."""
+        dev = self.st.dev
+        rank = int(min(self.precond_rank, req.n_sub))
+        seed = int(req.fit_kwargs.get("seed", 0))
+        U, evals = build_lowrank_basis(K, req.n_sub, rank, key=seed + 4321, device=dev)
+        r = int(U.shape[1])
+        eye = torch.eye(r, dtype=U.dtype, device=dev)
+        core = torch.diag(evals.to(U.dtype))[None] - float(req.atom) * eye[None]
+        return ProjectedCorePrecondConf(
+            U=U, core_atoms=core, total_rank=r, n_grm=1, diag_mode="scalar_identity",
+            diag_atoms=torch.tensor([req.atom], dtype=torch.float32, device=dev),
+            residual_diag_atoms=torch.ones(1, dtype=torch.float32, device=dev), identity=eye)
+
+    def _precond_for(self, req: _Request, K):
+        if self.precond_rank <= 0:
+            return None
+        if req.mask is not None:
+            return self._projected_core(K, req)
+        with self._full_precond_lock:
+            if self._full_precond is None:
+                self._full_precond = self._projected_core(self._full_K, req)
+            return self._full_precond
+
     def _shared_cache_key(self, req: _Request):
         """(seed, slq_samples, slq_m) when the request may use the shared
         full-cohort probe cache, else None (subset requests, caller-supplied
@@ -521,6 +561,8 @@ class REMLServer:
             else:
                 K_mvs = [lambda V: b.apply(req, V, inv_eff, None)]
             diag = torch.tensor(req.atom, dtype=torch.float32, device=self.st.dev)
+            if "precond_conf" not in kw:
+                kw["precond_conf"] = self._precond_for(req, K_mvs[0])
             param, hist, d = fit_reml(req.y, K_mvs, [diag], req.covar, weighted_hv=whv,
                                       device=self.st.dev, return_diagnostics=True, **kw)
             gen = float(np.dot(param[:1], np.asarray(d.get("genetic_trace_atoms", [1.0]))))

@@ -244,6 +244,18 @@ int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision);
 int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32_t reps,
                           int32_t* choice, float* best_ms, float* default_ms, void* stream);
 
+/* Tensor-core instruction-rate probe (no counterpart in the reference: it
+ * measures the ceiling of this library's operator, not a reference step).
+ * One CTA per SM; `issuers` (1 or 2) threads per CTA, on different SM
+ * sub-partitions, each issue `iters` back-to-back tcgen05.mma of M = 128,
+ * N = n_cols (multiple of 16; <= 256 with one issuer, <= 224 with two),
+ * A in tensor memory, B in shared memory, kind 0 = BF16 (K = 16) or
+ * 1 = E4M3 (K = 32), on zero operands.  cycles: SM cycles per instruction
+ * of one issuer of CTA 0; ms: device time of the whole launch (CUDA events
+ * on `stream`).  Allocates and frees 12 bytes; synchronises `stream`.       */
+int coherit_mma_rate(int32_t kind, int32_t n_cols, int32_t issuers, int32_t iters,
+                     double* cycles, double* ms, void* stream);
+
 int coherit_geno_kv(coherit_geno_t* h, int32_t slot, int32_t mode, int32_t precision,
                     const float* V, int64_t ldv, int32_t k, const float* comp_scale,
                     int32_t use_theta_e, float theta_e, const float* snp_weight,
