@@ -90,6 +90,7 @@ _SIGNATURES = {
     "coherit_geno_reserve": (C.c_int, [_p, _i32, _i32]),
     "coherit_geno_autotune": (C.c_int, [_p, _i32, _i32, _i32, _p, _p, _p, _p]),
     "coherit_mma_rate": (C.c_int, [_i32, _i32, _i32, _i32, _p, _p, _p]),
+    "coherit_geno_set_launch": (C.c_int, [_p, _i32, _i32, _p]),
     "coherit_geno_kv": (
         C.c_int,
         [_p, _i32, _i32, _i32, _p, _i64, _i32, _p, _i32, _f32, _p, _p, _i64, _p],

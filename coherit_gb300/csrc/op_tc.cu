@@ -125,6 +125,7 @@ struct TcParams {
   uint32_t tmem_cols;
   uint32_t acc_cols;
   int* err;
+  int64_t n_tiles;      // tiles along gridDim.x (the grid may add padding CTAs)
   int ksplit;           // CTAs along K (gridDim.z); > 1 writes partials
   float* part;          // ksplit x part_stride FP32 partials (ksplit > 1)
   int64_t part_stride;  // floats per K share: rows x kp
@@ -870,6 +871,7 @@ static int fill_epi(coherit_geno* h, const OpDesc& d, int kp, int nsplit, EpiPar
 struct TcLaunchCfg {
   bool wide;   // StageCfg<4, 2> instead of StageCfg<2, 3>
   int sb;      // blocks per stage of that configuration
+  int cluster; // CTAs per cluster sharing each B tile (1, 2 or 4)
   int RB, RA;
   bool side;
   uint32_t bslot;
@@ -884,27 +886,32 @@ struct TcLaunchCfg {
 // narrow form; always one CTA per SM, which allocates all 512 tensor-memory
 // columns so no second CTA can share the SM.
 static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision, int want_wide,
-                                    int ra_req, int rb_req);
+                                    int ra_req, int rb_req, int cluster = 0);
 
 // Launch configuration: the autotuner's choice for (kp, precision) when there
 // is one, else the fixed policy below.
 static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int precision) {
   const auto it = h->tuned.find({kp, precision});
   if (it != h->tuned.end())
-    return tc_config_policy(h, kp, precision, it->second.wide, it->second.RA, it->second.RB);
+    return tc_config_policy(h, kp, precision, it->second.wide, it->second.RA, it->second.RB,
+                            it->second.cluster);
   return tc_config_policy(h, kp, precision, -1, 0, 0);
 }
+
+// CTAs per cluster of the fixed policy (no tuned choice).
+constexpr int kDefaultCluster = 1;
 
 // want_wide: -1 policy, 0 two-block stages, 1 four-block stages (if their
 // rings fit); ra_req / rb_req: ring depths (0 = largest that fits), clamped
 // to what fits tensor memory, shared memory and the barrier arrays.
 static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision, int want_wide,
-                                    int ra_req, int rb_req) {
+                                    int ra_req, int rb_req, int cluster) {
   const int nsplit = nsplit_of(precision);
   const int eb = elem_bytes(precision);
   // Tensor-memory columns of one 64-K block of A (E4M3: one byte per code).
   const uint32_t acols = op_type(precision) == kTyE4M3 ? 16u : 32u;
   TcLaunchCfg c;
+  c.cluster = cluster == 2 || cluster == 4 ? cluster : (cluster == 1 ? 1 : kDefaultCluster);
   c.side = nsplit > 1 && nsplit * kp <= 256;
   const int acc = c.side ? nsplit * kp : kp;
   c.acc_cols = static_cast<uint32_t>(round_up(acc, 32));
@@ -963,36 +970,67 @@ static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision
   return c;
 }
 
-template <bool IS_K1, class Cfg>
+template <bool IS_K1, class Cfg, int CL>
 static int launch_tc_cfg(int nsplit, int ty, bool side, dim3 grid, size_t smem,
                          cudaStream_t st, const TcParams& p) {
   auto go = [&](auto kern) -> int {
     CO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));
-    kern<<<grid, Cfg::THREADS, smem, st>>>(p); note_launch();
+    if constexpr (CL == 1) {
+      kern<<<grid, Cfg::THREADS, smem, st>>>(p);
+    } else {
+      cudaLaunchConfig_t lc = {};
+      lc.gridDim = grid;
+      lc.blockDim = dim3(Cfg::THREADS);
+      lc.dynamicSmemBytes = smem;
+      lc.stream = st;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = CL;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      lc.attrs = at;
+      lc.numAttrs = 1;
+      CO_CUDA(cudaLaunchKernelEx(&lc, kern, p));
+    }
+    note_launch();
     CO_CUDA(cudaGetLastError());
     return COHERIT_OK;
   };
   if (ty == kTyF16) {
     CO_CHECK(nsplit == 2 && side, COHERIT_E_SHAPE, "FP16 terms must fit side by side (2 kp <= 256)");
-    return go(k_tc_op<IS_K1, 2, true, Cfg, kTyF16>);
+    return go(k_tc_op<IS_K1, 2, true, Cfg, kTyF16, CL>);
   }
   if (ty == kTyE4M3) {
     CO_CHECK(nsplit == 5 && side, COHERIT_E_SHAPE, "E4M3 terms must fit side by side (5 kp <= 256)");
-    return go(k_tc_op<IS_K1, 5, true, Cfg, kTyE4M3>);
+    return go(k_tc_op<IS_K1, 5, true, Cfg, kTyE4M3, CL>);
   }
-  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false, Cfg, kTyBf16>);
+  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false, Cfg, kTyBf16, CL>);
   CO_CHECK(side, COHERIT_E_SHAPE, "split terms must fit side by side (nsplit * kp <= 256)");
-  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true, Cfg, kTyBf16>);
-  return go(k_tc_op<IS_K1, 3, true, Cfg, kTyBf16>);
+  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true, Cfg, kTyBf16, CL>);
+  return go(k_tc_op<IS_K1, 3, true, Cfg, kTyBf16, CL>);
 }
 
+template <bool IS_K1, class Cfg>
+static int launch_tc_cl(const TcLaunchCfg& cfg, int nsplit, int ty, dim3 grid, cudaStream_t st,
+                        const TcParams& p) {
+  if (cfg.cluster == 4)
+    return launch_tc_cfg<IS_K1, Cfg, 4>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
+  if (cfg.cluster == 2)
+    return launch_tc_cfg<IS_K1, Cfg, 2>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
+  return launch_tc_cfg<IS_K1, Cfg, 1>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
+}
+
+// grid.x = tiles; the launch rounds it up to whole clusters.
 template <bool IS_K1>
 static int launch_tc(const TcLaunchCfg& cfg, int nsplit, int ty, dim3 grid, cudaStream_t st,
-                     const TcParams& p) {
-  if (cfg.wide)
-    return launch_tc_cfg<IS_K1, CfgWide>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
-  return launch_tc_cfg<IS_K1, CfgNarrow>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
+                     const TcParams& p0) {
+  TcParams p = p0;
+  p.n_tiles = grid.x;
+  const unsigned cl = static_cast<unsigned>(cfg.cluster);
+  grid.x = (grid.x + cl - 1) / cl * cl;
+  if (cfg.wide) return launch_tc_cl<IS_K1, CfgWide>(cfg, nsplit, ty, grid, st, p);
+  return launch_tc_cl<IS_K1, CfgNarrow>(cfg, nsplit, ty, grid, st, p);
 }
 
 // Column-block width when k exceeds what one launch holds (each block
@@ -1302,6 +1340,7 @@ int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32
     best.RA = c0.RA;
     best.RB = c0.RB;
     best.target_mult = kDefaultTargetMult;
+    best.cluster = c0.cluster;
   }
   int tried = 0;
   for (int wide = 1; wide >= 0 && rc == COHERIT_OK && ce == cudaSuccess; --wide) {
@@ -1317,6 +1356,7 @@ int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32
           continue;
         for (int mult = 2; mult <= kMaxTargetMult && rc == COHERIT_OK; mult *= 2) {
           TuneChoice c;
+          c.cluster = 1;
           c.wide = wide;
           c.RA = ras[ia];
           c.RB = rbs[ib];
@@ -1330,6 +1370,24 @@ int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32
             best.ms = ms;
           }
         }
+      }
+    }
+  }
+  // Clusters of 2 or 4 CTAs sharing every B tile, on the best rings found
+  // without them.
+  const TuneChoice single = best;
+  for (int cl = 2; cl <= 4 && rc == COHERIT_OK && ce == cudaSuccess; cl *= 2) {
+    for (int mult = 2; mult <= kMaxTargetMult && rc == COHERIT_OK; mult *= 2) {
+      TuneChoice c = single;
+      c.cluster = cl;
+      c.target_mult = mult;
+      h->tuned[key] = c;
+      float ms = 0.f;
+      rc = time_once(ms);
+      ++tried;
+      if (rc == COHERIT_OK && ms < best.ms) {
+        best = c;
+        best.ms = ms;
       }
     }
   }
@@ -1356,9 +1414,40 @@ int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32
     choice[2] = best.RB;
     choice[3] = best.target_mult;
     choice[4] = tried;
+    choice[5] = best.cluster;
   }
   if (best_ms) *best_ms = best.ms;
   if (default_ms) *default_ms = t_def;
+  return COHERIT_OK;
+}
+
+int coherit_geno_set_launch(coherit_geno_t* h, int32_t k, int32_t precision,
+                            const int32_t* cfg) {
+  CO_CHECK(h != nullptr, COHERIT_E_CLOSED, "genotype handle is closed");
+  CO_CHECK(k >= 1, COHERIT_E_SHAPE, "width must be >= 1");
+  const int prec = resolve_precision(precision, k);
+  CO_CHECK(is_tc_precision(prec), COHERIT_E_UNSUPPORTED,
+           "launch configurations exist for the tensor-core precisions only");
+  const std::pair<int, int> key{static_cast<int>(round_up(k, 16)), prec};
+  if (cfg == nullptr) {
+    h->tuned.erase(key);
+    return COHERIT_OK;
+  }
+  CO_CHECK(cfg[0] == 0 || cfg[0] == 1, COHERIT_E_SHAPE, "stage form must be 0 or 1");
+  CO_CHECK(cfg[1] >= 0 && cfg[1] <= kMaxRA && cfg[2] >= 0 && cfg[2] <= kMaxRB, COHERIT_E_SHAPE,
+           "ring depths must lie in [0, %d] and [0, %d] (0 = largest that fits)", kMaxRA,
+           kMaxRB);
+  CO_CHECK(cfg[3] == 2 || cfg[3] == 4 || cfg[3] == 8, COHERIT_E_SHAPE,
+           "grid multiple must be 2, 4 or 8");
+  CO_CHECK(cfg[5] == 1 || cfg[5] == 2 || cfg[5] == 4, COHERIT_E_SHAPE,
+           "CTAs per cluster must be 1, 2 or 4");
+  TuneChoice c;
+  c.wide = cfg[0];
+  c.RA = cfg[1];
+  c.RB = cfg[2];
+  c.target_mult = cfg[3];
+  c.cluster = cfg[5];
+  h->tuned[key] = c;
   return COHERIT_OK;
 }
 

@@ -24,8 +24,19 @@
 // accumulation loses precision over very long chains (relative error grows
 // with the number of MMAs into one accumulator), so the host bounds every
 // chain this way.
+//
+// Clusters (CL > 1): the CL CTAs of a cluster own consecutive tiles of the
+// same K share and so read the same B tile at every stage.  Each copies 1/CL
+// of the stage into the B ring of every CTA of the cluster (bulk copy with
+// cluster multicast, within this GPU's memory), which divides the B traffic
+// from L2 by CL; a B slot is refilled once every CTA's MMAs are done with it
+// (each MMA thread's commit arrives on that slot's empty barrier in every
+// CTA, so the barrier counts CL arrivals).  A CTA leaves only after the last
+// arrivals of the other CTAs on its own barriers have landed.  The grid is a
+// whole number of clusters; a padding CTA repeats the last tile without
+// writing results.
 
-template <bool IS_K1, int NSPLIT, bool SIDE, class Cfg, int TY>
+template <bool IS_K1, int NSPLIT, bool SIDE, class Cfg, int TY, int CL>
 __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant__ TcParams p) {
   constexpr int kStageBlocks = Cfg::SB;
   // Tensor-memory columns of one 64-K block of A: 32 for 16-bit operands,
@@ -54,8 +65,10 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
   const int RA = p.RA;
   const int RB = p.RB;
 
-  const int64_t tile = blockIdx.x;
+  const bool active = blockIdx.x < p.n_tiles;
+  const int64_t tile = active ? static_cast<int64_t>(blockIdx.x) : p.n_tiles - 1;
   const int comp = blockIdx.y;
+  constexpr uint16_t kClusterMask = static_cast<uint16_t>((1u << CL) - 1u);
   const int zsplit = blockIdx.z;
   int64_t ntot;
   const uint8_t* gbase;
@@ -92,7 +105,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
     }
     for (int i = 0; i < kMaxRB; ++i) {
       ptx::mbar_init(&fullB[i], 1);
-      ptx::mbar_init(&emptyB[i], 1);
+      ptx::mbar_init(&emptyB[i], CL);
     }
     for (int i = 0; i < kMaxRA; ++i) {
       ptx::mbar_init(&decoded[i], 4);
@@ -118,7 +131,9 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
                         acc_need <= p.acc_cols && (p.acc_cols & 31u) == 0 &&
                         p.acc_cols + static_cast<uint32_t>(p.RA) * kACols * kStageBlocks <= p.tmem_cols &&
                         p.tmem_cols >= 32 && p.tmem_cols <= 512 &&
-                        (p.tmem_cols & (p.tmem_cols - 1)) == 0 && acc_need <= 256 && (e.kp & 15) == 0;
+                        (p.tmem_cols & (p.tmem_cols - 1)) == 0 && acc_need <= 256 && (e.kp & 15) == 0 &&
+                        p.n_tiles >= 1 && p.n_tiles <= static_cast<int64_t>(gridDim.x) &&
+                        gridDim.x % CL == 0 && p.bslot_bytes % (16u * CL) == 0;
     if (!cfg_ok) {
       if (threadIdx.x == 0) atomicCAS(p.err, 0, 30);
       return;
@@ -128,6 +143,9 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
   ptx::tc_fence_before();
   __syncthreads();
   ptx::tc_fence_after();
+  // Every CTA of the cluster has initialised its barriers before any copy or
+  // commit reaches them.
+  if constexpr (CL > 1) ptx::cluster_sync();
   const uint32_t tmem = *tmem_slot;
 
   if (warp == kWarpG) {
@@ -161,13 +179,31 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
       int issued = 0;
       int s = 0;
       uint32_t ph = 0;
+      const uint32_t share = p.bslot_bytes / CL;
+      const uint32_t own = CL > 1 ? ptx::cluster_ctarank() * share : 0u;
       for (int c = 0; c < nch; ++c) {
         if (c >= RB && !ptx::mbar_wait(&emptyB[s], ph ^ 1u, p.err, 12, abort_flag)) break;
+        // The full slot arrives on this CTA's barrier: its own share and the
+        // shares the other CTAs of the cluster multicast.
         ptx::mbar_arrive_expect_tx(&fullB[s], p.bslot_bytes);
-        ptx::bulk_g2s(bring + static_cast<size_t>(s) * p.bslot_bytes,
-                      bbase + static_cast<int64_t>(c) * stage_b_bytes, p.bslot_bytes, &fullB[s]);
+        if constexpr (CL > 1)
+          ptx::bulk_g2s_multicast(bring + static_cast<size_t>(s) * p.bslot_bytes + own,
+                                  bbase + static_cast<int64_t>(c) * stage_b_bytes + own, share,
+                                  &fullB[s], kClusterMask);
+        else
+          ptx::bulk_g2s(bring + static_cast<size_t>(s) * p.bslot_bytes,
+                        bbase + static_cast<int64_t>(c) * stage_b_bytes, p.bslot_bytes, &fullB[s]);
         issued = c + 1;
         if (++s == RB) { s = 0; ph ^= 1u; }
+      }
+      if constexpr (CL > 1) {
+        // The other CTAs' commits for the last use of every slot arrive on
+        // this CTA's barriers: wait for them before the CTA may exit.
+        if (!*abort_flag)
+          for (int c = (nch > RB ? nch - RB : 0); c < nch; ++c)
+            if (!ptx::mbar_wait(&emptyB[c % RB], static_cast<uint32_t>(c / RB) & 1u, p.err, 21,
+                                abort_flag))
+              break;
       }
       if (*abort_flag) {
         for (int c = (issued > RB ? issued - RB : 0); c < issued; ++c) {
@@ -220,7 +256,10 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
           }
         }
         ptx::mma_commit(&emptyA[as]);
-        ptx::mma_commit(&emptyB[bs]);
+        if constexpr (CL > 1)
+          ptx::mma_commit_multicast(&emptyB[bs], kClusterMask);
+        else
+          ptx::mma_commit(&emptyB[bs]);
         if (++as == RA) { as = 0; pa ^= 1u; }
         if (++bs == RB) { bs = 0; pb ^= 1u; }
       }
@@ -293,7 +332,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
       const bool w_ok = ptx::mbar_wait(done, 0, p.err, 17, abort_flag);
       ok = __all_sync(0xffffffffu, w_ok);
     }
-    if (ok) {
+    if (ok && active) {
       ptx::tc_fence_after();
       const int64_t rowid = tile * kTile + row;
       // Column chunks of 16 rotate over the kSets warps of a quarter.

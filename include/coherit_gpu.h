@@ -234,15 +234,26 @@ int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision);
  * `precision` (AUTO resolves by width) on this handle's genotypes and stats
  * slot 0 under each candidate configuration -- two- or four-block pipeline
  * stages, tensor-memory A-ring depth, shared-memory B-ring depth, and the
- * grid size (2, 4 or 8 x SMs) the split-K plan fills -- `reps` timed
- * applications each (CUDA events on `stream`), and keeps the fastest for
- * every later launch of that width and precision on the handle.  Allocates
- * and frees two n x k buffers; synchronises `stream`.  choice (5 ints, may
- * be NULL): four-block stages (0/1), A-ring slots, B-ring slots, grid
- * multiple, candidates tried; best_ms / default_ms: per-application times of
- * the kept and of the fixed-policy configuration.                          */
+ * grid size (2, 4 or 8 x SMs) the split-K plan fills, and clusters of 2 or
+ * 4 CTAs that share each B tile (one multicast copy from L2 instead of one
+ * per CTA) -- `reps` timed applications each (CUDA events on `stream`), and
+ * keeps the fastest for every later launch of that width and precision on
+ * the handle.  Allocates and frees two n x k buffers; synchronises `stream`.
+ * choice (6 ints, may be NULL): four-block stages (0/1), A-ring slots,
+ * B-ring slots, grid multiple, candidates tried, CTAs per cluster;
+ * best_ms / default_ms: per-application times of the kept and of the
+ * fixed-policy configuration.                                             */
 int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32_t reps,
                           int32_t* choice, float* best_ms, float* default_ms, void* stream);
+
+/* Pin the launch configuration of width k (rounded up to 16) and
+ * `precision` (AUTO resolves by width) on this handle, in place of the fixed
+ * policy or a tuned choice (no counterpart in the reference): cfg (6 ints,
+ * the layout of coherit_geno_autotune's choice) = four-block stages (0/1),
+ * A-ring slots, B-ring slots (0 = largest that fits; depths are clamped to
+ * what fits), grid multiple (2, 4 or 8), unused, CTAs per cluster (1, 2 or
+ * 4).  cfg NULL returns the width to the fixed policy.                      */
+int coherit_geno_set_launch(coherit_geno_t* h, int32_t k, int32_t precision, const int32_t* cfg);
 
 /* Tensor-core instruction-rate probe (no counterpart in the reference: it
  * measures the ceiling of this library's operator, not a reference step).

@@ -408,7 +408,7 @@ def test_autotuned_configuration_keeps_parity(cuda, precision):
     assert len(rec) == 2
     for r in rec:
         assert r["candidates"] >= 2 and r["a_ring"] >= 2 and 2 <= r["b_ring"] <= 16
-        assert r["grid_x_sms"] in (2, 4, 8)
+        assert r["grid_x_sms"] in (2, 4, 8) and r["cluster"] in (1, 2, 4)
         assert r["best_ms"] <= r["default_ms"] * 1.0001
     V = np.random.default_rng(8).normal(size=(n, k)).astype(np.float32)
     out = st.kv(torch.as_tensor(V, device=cuda)).cpu().numpy()
@@ -434,3 +434,40 @@ def test_mma_rate_probe(cuda, kind):
         assert ms.value > 0.0
     with pytest.raises(ValueError):
         _lib.check(lib.coherit_mma_rate(kind, 240, 2, 16, None, None, _lib.stream_ptr()))
+
+
+@pytest.mark.parametrize("m", [30000, 80000])
+def test_cluster_shared_b_tiles_match_single_ctas(cuda, m):
+    """Clusters of 2 and 4 CTAs that share each B tile through multicast
+    copies compute the same tiles as single CTAs: every precision, narrow and
+    four-block stages, with split K (m = 30,000) and without (m = 80,000),
+    and with an odd tile count (235 SNP tiles, 157 sample tiles: the last
+    cluster carries a padding CTA).  Same split plan, so the only difference
+    is the order of the FP64 rank-one additions (1e-6); against FP64 at the
+    precision's bound."""
+    n = 20000
+    st = _streamer(n, m, seed=9, miss=0.01)
+    codes = oracle_codes(9, n, m, 0.01)
+    mean, inv = st._means_host, st._inv_sds_host
+    eff = float(st._eff_m_host)
+    for prec, k, tol in (("bf16x3", 16, TOL), ("bf16x3", 64, TOL), ("fp8x5", 16, TOL),
+                         ("fp8x5", 48, TOL), ("fp16x2", 32, 2 * TOL), ("bf16x1", 32, 6e-3)):
+        V = np.random.default_rng(k + m).normal(size=(n, k)).astype(np.float32)
+        Vd = torch.as_tensor(V, device=cuda)
+        ref = og.kv_f64(codes, mean, inv, V, comp_scale=[1 / eff])
+        for wide in (False, True):
+            outs = {}
+            for cl in (1, 2, 4):
+                st.set_launch(k, prec, four_block_stages=wide, cluster=cl, grid_x_sms=4)
+                outs[cl] = st.kv(Vd, precision=prec).cpu().numpy()
+                xt = st.xtv(Vd, precision=prec).cpu().numpy()
+                if cl == 1:
+                    xt1 = xt
+                else:
+                    assert col_rel(xt, xt1) < 1e-6, (prec, k, wide, cl, "xtv")
+            assert col_rel(outs[1], ref) < tol, (prec, k, wide)
+            for cl in (2, 4):
+                assert col_rel(outs[cl], outs[1]) < 1e-6, (prec, k, wide, cl)
+        st.set_launch(k, prec, policy=True)
+    st.check()
+    st.close()
