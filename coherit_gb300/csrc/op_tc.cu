@@ -121,6 +121,7 @@ struct TcParams {
   int64_t b_chunk_bytes;
   int RB;
   int RA;
+  int RG;               // genotype ring stages (<= the configuration's barrier slots)
   uint32_t bslot_bytes;
   uint32_t tmem_cols;
   uint32_t acc_cols;
@@ -872,6 +873,7 @@ struct TcLaunchCfg {
   bool wide;   // StageCfg<4, 2> instead of StageCfg<2, 3>
   int sb;      // blocks per stage of that configuration
   int cluster; // CTAs per cluster sharing each B tile (1, 2 or 4)
+  int RG;      // genotype ring stages
   int RB, RA;
   bool side;
   uint32_t bslot;
@@ -879,62 +881,69 @@ struct TcLaunchCfg {
   size_t smem;
 };
 
+// Requested launch shape: wide -1 policy, 0 two-block stages, 1 four-block
+// stages (if their rings fit); ring depths 0 = largest that fits (genotype
+// ring: the configuration's full depth), clamped to what fits tensor
+// memory, shared memory and the barrier arrays; cluster 0 = policy.
+struct LaunchReq {
+  int wide = -1, RA = 0, RB = 0, RG = 0, cluster = 0;
+};
+
+static LaunchReq req_of(const TuneChoice& t) {
+  LaunchReq r;
+  r.wide = t.wide;
+  r.RA = t.RA;
+  r.RB = t.RB;
+  r.RG = t.RG;
+  r.cluster = t.cluster;
+  return r;
+}
+
+// CTAs per cluster of the fixed policy (no tuned choice).
+constexpr int kDefaultCluster = 1;
+
 // Accumulator: NSPLIT*kp columns, the split terms side by side in N (one MMA
 // per K step, N <= 256).  The A ring takes the remaining tensor-memory
 // columns.  Blocks of <= 16 columns use the narrow form; wider blocks use the
 // wide form where its B ring (>= 2 stages) fits shared memory, else the
 // narrow form; always one CTA per SM, which allocates all 512 tensor-memory
 // columns so no second CTA can share the SM.
-static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision, int want_wide,
-                                    int ra_req, int rb_req, int cluster = 0);
-
-// Launch configuration: the autotuner's choice for (kp, precision) when there
-// is one, else the fixed policy below.
-static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int precision) {
-  const auto it = h->tuned.find({kp, precision});
-  if (it != h->tuned.end())
-    return tc_config_policy(h, kp, precision, it->second.wide, it->second.RA, it->second.RB,
-                            it->second.cluster);
-  return tc_config_policy(h, kp, precision, -1, 0, 0);
-}
-
-// CTAs per cluster of the fixed policy (no tuned choice).
-constexpr int kDefaultCluster = 1;
-
-// want_wide: -1 policy, 0 two-block stages, 1 four-block stages (if their
-// rings fit); ra_req / rb_req: ring depths (0 = largest that fits), clamped
-// to what fits tensor memory, shared memory and the barrier arrays.
-static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision, int want_wide,
-                                    int ra_req, int rb_req, int cluster) {
+static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision,
+                                    const LaunchReq& rq) {
   const int nsplit = nsplit_of(precision);
   const int eb = elem_bytes(precision);
   // Tensor-memory columns of one 64-K block of A (E4M3: one byte per code).
   const uint32_t acols = op_type(precision) == kTyE4M3 ? 16u : 32u;
   TcLaunchCfg c;
-  c.cluster = cluster == 2 || cluster == 4 ? cluster : (cluster == 1 ? 1 : kDefaultCluster);
+  c.cluster = rq.cluster == 1 || rq.cluster == 2 || rq.cluster == 4 ? rq.cluster : kDefaultCluster;
   c.side = nsplit > 1 && nsplit * kp <= 256;
   const int acc = c.side ? nsplit * kp : kp;
   c.acc_cols = static_cast<uint32_t>(round_up(acc, 32));
   const size_t cap = static_cast<size_t>(h->smem_optin);
-  if (want_wide != 0) {
+  auto ring_g = [&](int sets, int full) {
+    return rq.RG >= sets && rq.RG <= full && rq.RG % sets == 0 ? rq.RG : full;
+  };
+  if (rq.wide != 0) {
     // Four-block stages (half the barrier round trips per K of two-block
     // stages) wherever their rings fit: at one CTA per SM they apply 16
     // columns faster than two-block stages (n = 50,000, m = 500,000: k = 32
     // in 10.5 ms against k = 16 in 12.7 ms with two-block stages).
+    const int rg = ring_g(CfgWide::SETS, CfgWide::RG);
     const uint32_t slot = acols * CfgWide::SB;
     const uint32_t bslot = static_cast<uint32_t>(CfgWide::SB) * nsplit * kp * kPanel * eb;
-    const size_t fixed = kBarrierBytes + static_cast<size_t>(CfgWide::RG) * CfgWide::SB * kBlockBytes;
+    const size_t fixed = kBarrierBytes + static_cast<size_t>(rg) * CfgWide::SB * kBlockBytes;
     int ra = std::min<int>(kMaxRA, static_cast<int>((512u - c.acc_cols) / slot));
-    if (ra_req > 0) ra = std::min(ra, std::max(ra_req, CfgWide::MIN_RA));
+    if (rq.RA > 0) ra = std::min(ra, std::max(rq.RA, CfgWide::MIN_RA));
     if (c.acc_cols + CfgWide::MIN_RA * slot <= 512u && ra >= CfgWide::MIN_RA &&
         fixed + 2 * static_cast<size_t>(bslot) <= cap - 4096) {
       c.wide = true;
       c.sb = CfgWide::SB;
+      c.RG = rg;
       c.tmem_cols = 512;
       c.RA = ra;
       c.bslot = bslot;
       int rb = static_cast<int>((cap - 4096 - fixed) / bslot);
-      if (rb_req > 0) rb = std::min(rb, rb_req);
+      if (rq.RB > 0) rb = std::min(rb, rq.RB);
       c.RB = std::max(2, std::min(kMaxRB, rb));
       c.smem = fixed + static_cast<size_t>(c.RB) * bslot;
       return c;
@@ -942,32 +951,37 @@ static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision
   }
   c.wide = false;
   c.sb = CfgNarrow::SB;
+  c.RG = ring_g(CfgNarrow::SETS, CfgNarrow::RG);
   const uint32_t slot_cols = acols * CfgNarrow::SB;
   // One CTA per SM for every width: all 512 tensor-memory columns.  Layouts
   // with two CTAs per SM returned a few wrong rows under split K (a whole
-  // lane quarter of a tile) even with CTAs of whole warpgroups, and they buy
-  // little: the SM's tensor pipe runs the two CTAs' MMAs one after the other.
+  // lane quarter of a tile) even with CTAs of whole warpgroups.
   const uint32_t cols = 512;
   c.tmem_cols = cols;
   c.RA = std::min<int>(kMaxRA, static_cast<int>((cols - c.acc_cols) / slot_cols));
-  if (ra_req > 0) c.RA = std::min(c.RA, std::max(ra_req, CfgNarrow::MIN_RA));
+  if (rq.RA > 0) c.RA = std::min(c.RA, std::max(rq.RA, CfgNarrow::MIN_RA));
   c.bslot = static_cast<uint32_t>(CfgNarrow::SB) * nsplit * kp * kPanel * eb;
-  const size_t fixed =
-      kBarrierBytes + static_cast<size_t>(CfgNarrow::RG) * CfgNarrow::SB * kBlockBytes;
-  const int ctas_tmem = 512 / static_cast<int>(cols);
-  const size_t target = ctas_tmem >= 2 ? std::min<size_t>(112 * 1024, cap) : cap - 4096;
-  int rb = static_cast<int>((target - fixed) / c.bslot);
-  if (rb_req > 0) rb = std::min(rb, rb_req);
+  const size_t fixed = kBarrierBytes + static_cast<size_t>(c.RG) * CfgNarrow::SB * kBlockBytes;
+  int rb = static_cast<int>((cap - 4096 - fixed) / c.bslot);
+  if (rq.RB > 0) rb = std::min(rb, rq.RB);
   rb = std::max(2, std::min(kMaxRB, rb));
   while (rb > 2 && fixed + static_cast<size_t>(rb) * c.bslot > cap) --rb;
   c.RB = rb;
   c.smem = fixed + static_cast<size_t>(rb) * c.bslot;
-  // Never let more CTAs share an SM than its tensor memory can hold: a
-  // further CTA would block in tcgen05.alloc.
+  // One CTA per SM: pad the shared-memory request until a second CTA cannot
+  // fit (it would block in tcgen05.alloc).
   const size_t sm_bytes = static_cast<size_t>(h->smem_per_sm);
-  while (static_cast<int>(sm_bytes / (c.smem + 1024)) > ctas_tmem && c.smem + 4096 <= cap)
+  while (static_cast<int>(sm_bytes / (c.smem + 1024)) > 1 && c.smem + 4096 <= cap)
     c.smem += 4096;
   return c;
+}
+
+// Launch configuration: the autotuner's choice for (kp, precision) when there
+// is one, else the fixed policy.
+static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int precision) {
+  const auto it = h->tuned.find({kp, precision});
+  if (it != h->tuned.end()) return tc_config_policy(h, kp, precision, req_of(it->second));
+  return tc_config_policy(h, kp, precision, LaunchReq());
 }
 
 template <bool IS_K1, class Cfg, int CL>
@@ -1160,6 +1174,7 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   memset(&p, 0, sizeof(p));
   p.RB = cfg.RB;
   p.RA = cfg.RA;
+  p.RG = cfg.RG;
   p.bslot_bytes = cfg.bslot;
   p.tmem_cols = cfg.tmem_cols;
   p.acc_cols = cfg.acc_cols;
@@ -1331,43 +1346,57 @@ int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32
   };
   float t_def = 0.f;
   if (rc == COHERIT_OK && ce == cudaSuccess) rc = time_once(t_def);
-  // Candidates: stage size x A-ring depth x B-ring depth x split-K grid.
+  // Candidates: stage size x genotype-ring depth (full, or half where that
+  // frees shared memory for another B slot) x A-ring depth x B-ring depth x
+  // split-K grid.
   TuneChoice best;
   best.ms = t_def;
   {
-    const TcLaunchCfg c0 = tc_config_policy(h, kp, prec, -1, 0, 0);
+    const TcLaunchCfg c0 = tc_config_policy(h, kp, prec, LaunchReq());
     best.wide = c0.wide ? 1 : 0;
     best.RA = c0.RA;
     best.RB = c0.RB;
+    best.RG = c0.RG;
     best.target_mult = kDefaultTargetMult;
     best.cluster = c0.cluster;
   }
   int tried = 0;
   for (int wide = 1; wide >= 0 && rc == COHERIT_OK && ce == cudaSuccess; --wide) {
-    const TcLaunchCfg full = tc_config_policy(h, kp, prec, wide, 0, 0);
+    LaunchReq rq;
+    rq.wide = wide;
+    const TcLaunchCfg full = tc_config_policy(h, kp, prec, rq);
     if ((full.wide ? 1 : 0) != wide) continue;  // four-block rings do not fit
-    const int ra_min = wide ? CfgWide::MIN_RA : CfgNarrow::MIN_RA;
-    const int ras[2] = {full.RA, std::max(ra_min, full.RA / 2)};
-    const int rbs[3] = {full.RB, std::max(2, full.RB / 2), 2};
-    for (int ia = 0; ia < 2 && rc == COHERIT_OK; ++ia) {
-      if (ia == 1 && ras[1] == ras[0]) continue;
-      for (int ib = 0; ib < 3 && rc == COHERIT_OK; ++ib) {
-        if ((ib == 1 && rbs[1] == rbs[0]) || (ib == 2 && (rbs[2] == rbs[1] || rbs[2] == rbs[0])))
-          continue;
-        for (int mult = 2; mult <= kMaxTargetMult && rc == COHERIT_OK; mult *= 2) {
-          TuneChoice c;
-          c.cluster = 1;
-          c.wide = wide;
-          c.RA = ras[ia];
-          c.RB = rbs[ib];
-          c.target_mult = mult;
-          h->tuned[key] = c;
-          float ms = 0.f;
-          rc = time_once(ms);
-          ++tried;
-          if (rc == COHERIT_OK && ms < best.ms) {
-            best = c;
-            best.ms = ms;
+    const int sets = wide ? CfgWide::SETS : CfgNarrow::SETS;
+    const int rgs[2] = {full.RG, 2 * sets};
+    for (int ig = 0; ig < 2 && rc == COHERIT_OK; ++ig) {
+      rq.RG = rgs[ig];
+      const TcLaunchCfg fg = tc_config_policy(h, kp, prec, rq);
+      if (ig == 1 && (rgs[1] == rgs[0] || fg.RB <= full.RB)) continue;
+      const int ra_min = wide ? CfgWide::MIN_RA : CfgNarrow::MIN_RA;
+      const int ras[2] = {fg.RA, std::max(ra_min, fg.RA / 2)};
+      const int rbs[3] = {fg.RB, std::max(2, fg.RB / 2), 2};
+      for (int ia = 0; ia < 2 && rc == COHERIT_OK; ++ia) {
+        if (ia == 1 && ras[1] == ras[0]) continue;
+        for (int ib = 0; ib < 3 && rc == COHERIT_OK; ++ib) {
+          if ((ib == 1 && rbs[1] == rbs[0]) ||
+              (ib == 2 && (rbs[2] == rbs[1] || rbs[2] == rbs[0])))
+            continue;
+          for (int mult = 2; mult <= kMaxTargetMult && rc == COHERIT_OK; mult *= 2) {
+            TuneChoice c;
+            c.cluster = 1;
+            c.wide = wide;
+            c.RG = rgs[ig];
+            c.RA = ras[ia];
+            c.RB = rbs[ib];
+            c.target_mult = mult;
+            h->tuned[key] = c;
+            float ms = 0.f;
+            rc = time_once(ms);
+            ++tried;
+            if (rc == COHERIT_OK && ms < best.ms) {
+              best = c;
+              best.ms = ms;
+            }
           }
         }
       }
@@ -1415,6 +1444,7 @@ int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32
     choice[3] = best.target_mult;
     choice[4] = tried;
     choice[5] = best.cluster;
+    choice[6] = best.RG;
   }
   if (best_ms) *best_ms = best.ms;
   if (default_ms) *default_ms = t_def;
@@ -1441,7 +1471,10 @@ int coherit_geno_set_launch(coherit_geno_t* h, int32_t k, int32_t precision,
            "grid multiple must be 2, 4 or 8");
   CO_CHECK(cfg[5] == 1 || cfg[5] == 2 || cfg[5] == 4, COHERIT_E_SHAPE,
            "CTAs per cluster must be 1, 2 or 4");
+  CO_CHECK(cfg[6] >= 0 && cfg[6] <= CfgNarrow::RG, COHERIT_E_SHAPE,
+           "genotype ring depth must lie in [0, %d] (0 = full)", CfgNarrow::RG);
   TuneChoice c;
+  c.RG = cfg[6];
   c.wide = cfg[0];
   c.RA = cfg[1];
   c.RB = cfg[2];

@@ -43,11 +43,11 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
   // 16 for E4M3 bytes.
   constexpr uint32_t kACols = TY == kTyE4M3 ? 16u : 32u;
   constexpr int kSets = Cfg::SETS;
-  constexpr int kRG = Cfg::RG;
+  constexpr int kMaxRG = Cfg::RG;  // barrier slots; the ring itself holds p.RG stages
   extern __shared__ __align__(1024) uint8_t smem[];
   uint64_t* fullG = reinterpret_cast<uint64_t*>(smem);
-  uint64_t* emptyG = fullG + kRG;
-  uint64_t* fullB = emptyG + kRG;
+  uint64_t* emptyG = fullG + kMaxRG;
+  uint64_t* fullB = emptyG + kMaxRG;
   uint64_t* emptyB = fullB + kMaxRB;
   uint64_t* decoded = emptyB + kMaxRB;
   uint64_t* emptyA = decoded + kMaxRA;
@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   constexpr int kStageBytes = kStageBlocks * kBlockBytes;
   uint8_t* gring = smem + kBarrierBytes;
+  const int kRG = p.RG;
   uint8_t* bring = gring + kRG * kStageBytes;
 
   const int warp = threadIdx.x >> 5;
@@ -99,7 +100,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
 
   if (threadIdx.x == 0) {
     // Each chunk is consumed and decoded by one set of 4 warps.
-    for (int i = 0; i < kRG; ++i) {
+    for (int i = 0; i < kMaxRG; ++i) {
       ptx::mbar_init(&fullG[i], 1);
       ptx::mbar_init(&emptyG[i], 4);
     }
@@ -125,6 +126,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
     // is more than one barrier phase behind (parity waits are ambiguous
     // beyond one phase).
     const bool cfg_ok = p.RA >= kSets && p.RA >= Cfg::MIN_RA && p.RA <= kMaxRA && p.RB >= 1 &&
+                        kRG >= kSets && kRG <= kMaxRG && kRG % kSets == 0 &&
                         p.RB <= kMaxRB &&
                         p.ksplit >= 1 && static_cast<int>(gridDim.z) == p.ksplit &&
                         (p.ksplit == 1 || p.part != nullptr) &&

@@ -239,8 +239,11 @@ int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision);
  * per CTA) -- `reps` timed applications each (CUDA events on `stream`), and
  * keeps the fastest for every later launch of that width and precision on
  * the handle.  Allocates and frees two n x k buffers; synchronises `stream`.
- * choice (6 ints, may be NULL): four-block stages (0/1), A-ring slots,
- * B-ring slots, grid multiple, candidates tried, CTAs per cluster;
+ * Genotype-ring depth is a candidate too (full, or two stages per decoder
+ * set where that frees shared memory for another B slot).
+ * choice (7 ints, may be NULL): four-block stages (0/1), A-ring slots,
+ * B-ring slots, grid multiple, candidates tried, CTAs per cluster,
+ * genotype-ring stages;
  * best_ms / default_ms: per-application times of the kept and of the
  * fixed-policy configuration.                                             */
 int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32_t reps,
@@ -248,11 +251,13 @@ int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32
 
 /* Pin the launch configuration of width k (rounded up to 16) and
  * `precision` (AUTO resolves by width) on this handle, in place of the fixed
- * policy or a tuned choice (no counterpart in the reference): cfg (6 ints,
+ * policy or a tuned choice (no counterpart in the reference): cfg (7 ints,
  * the layout of coherit_geno_autotune's choice) = four-block stages (0/1),
  * A-ring slots, B-ring slots (0 = largest that fits; depths are clamped to
  * what fits), grid multiple (2, 4 or 8), unused, CTAs per cluster (1, 2 or
- * 4).  cfg NULL returns the width to the fixed policy.                      */
+ * 4), genotype-ring stages (0 = full; else a multiple of the decoder sets,
+ * 2 for four-block and 3 for two-block stages).  cfg NULL returns the width
+ * to the fixed policy.                                                     */
 int coherit_geno_set_launch(coherit_geno_t* h, int32_t k, int32_t precision, const int32_t* cfg);
 
 /* Tensor-core instruction-rate probe (no counterpart in the reference: it

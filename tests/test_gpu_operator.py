@@ -439,7 +439,8 @@ def test_mma_rate_probe(cuda, kind):
 @pytest.mark.parametrize("m", [30000, 80000])
 def test_cluster_shared_b_tiles_match_single_ctas(cuda, m):
     """Clusters of 2 and 4 CTAs that share each B tile through multicast
-    copies compute the same tiles as single CTAs: every precision, narrow and
+    copies, and shallower genotype rings, compute the same tiles as single
+    CTAs with the full ring: every precision, narrow and
     four-block stages, with split K (m = 30,000) and without (m = 80,000),
     and with an odd tile count (235 SNP tiles, 157 sample tiles: the last
     cluster carries a padding CTA).  Same split plan, so the only difference
@@ -465,8 +466,13 @@ def test_cluster_shared_b_tiles_match_single_ctas(cuda, m):
                     xt1 = xt
                 else:
                     assert col_rel(xt, xt1) < 1e-6, (prec, k, wide, cl, "xtv")
+            # A shallower genotype ring (two stages per decoder set) with
+            # clusters of 2: same tiles again.
+            st.set_launch(k, prec, four_block_stages=wide, cluster=2, grid_x_sms=4,
+                          g_ring=4 if wide else 6)
+            outs["g"] = st.kv(Vd, precision=prec).cpu().numpy()
             assert col_rel(outs[1], ref) < tol, (prec, k, wide)
-            for cl in (2, 4):
+            for cl in (2, 4, "g"):
                 assert col_rel(outs[cl], outs[1]) < 1e-6, (prec, k, wide, cl)
         st.set_launch(k, prec, policy=True)
     st.check()
