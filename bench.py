@@ -303,7 +303,14 @@ def _percentile(xs, q):
 
 
 def _nsplit(precision: str) -> int:
-    return {"bf16x3": 3, "bf16x2": 2, "fp16x2": 2, "bf16x1": 1}.get(precision, 0)
+    return {"bf16x3": 3, "bf16x2": 2, "fp16x2": 2, "bf16x1": 1, "fp8x5": 5}.get(precision, 0)
+
+
+def _resolve(precision: str, k: int) -> str:
+    """The form AUTO takes at width k: E4M3 tiles up to 48 columns, bf16x3 above."""
+    if precision == "auto":
+        return "fp8x5" if k <= 48 else "bf16x3"
+    return precision
 
 
 def operator_roofline(st, k, hbm_peak, tensor_peak, reps=10, precision=None):
@@ -311,10 +318,11 @@ def operator_roofline(st, k, hbm_peak, tensor_peak, reps=10, precision=None):
     tensor fractions (algorithmic bytes n*ceil(m/4) + 8nk + 8m and flops
     4nmk), timed with CUDA events on the launching stream.  For the
     tensor-core precisions also the MMA instruction count of the two
-    contractions (M = 128, K = 16: n_pad * m_pad / 1024 per launch) and the
-    SM cycles per instruction this time implies: an instruction of N <= ~190
-    costs a fixed ~90-140 cycles on GB300 whatever N is, so narrow launches
-    are bound by the instruction count, not by HBM."""
+    contractions (M = 128, K = 16 for the 16-bit forms and 32 for E4M3:
+    2 * n_pad * m_pad / (128 K) per launch) and the SM cycles per
+    instruction this time implies: one issuing thread pays a fixed 120
+    cycles per instruction up to N = 224 on GB300 (bench.py --mma-rate), so
+    narrow launches are bound by the instruction count, not by HBM."""
     import torch
 
     precision = precision or st.precision
@@ -354,16 +362,19 @@ def operator_roofline(st, k, hbm_peak, tensor_peak, reps=10, precision=None):
                  "algorithmic_flops": alg_flops, "hbm_gbs": round(gbs, 1),
                  "hbm_frac": round(hbm_frac, 4), "tensor_tflops": round(tfs, 1),
                  "tensor_frac": round(ten_frac, 4)})
-    ns = _nsplit(precision)
+    form = _resolve(precision, k)
+    ns = _nsplit(form)
     if ns:
         info = st.info()
         kp = (k + 15) // 16 * 16
-        max_cols = 128 if precision == "fp16x2" else (256 // ns) // 16 * 16
+        max_cols = 128 if form == "fp16x2" else (256 // ns) // 16 * 16
         launches = -(-kp // max_cols)
-        instr = 2.0 * info["n_pad"] * info["m_pad"] / 2048.0 * launches
+        kk = 32 if form == "fp8x5" else 16
+        instr = 2.0 * info["n_pad"] * info["m_pad"] / (128.0 * kk) * launches
         sm_hz, sms = _sm_clock_hz(), torch.cuda.get_device_properties(st.dev).multi_processor_count
         roof["mma_issue"] = {
             "instructions_per_application": int(instr),
+            "form": form, "k_per_instruction": kk,
             "n_per_instruction": ns * min(kp, max_cols),
             "cycles_per_instruction_per_sm": round(ms * 1e-3 * sm_hz * sms / instr, 1),
             "sm_clock_mhz_assumed": sm_hz / 1e6}
