@@ -980,24 +980,17 @@ def run_operator_only(args, wl):
             "gpu_launches": int(launches), "peak_source": peak_src}
 
 
-def run_smile_only(args, wl):
-    """SMILE block-weighted operator at the c5 shape (``--smile K``): n=100,000
-    x m=300,000 (or --n/--m), blocks of 500 SNPs with W_b ~ Wishart(500, I)/500
-    in FP32 (seeded), kernel-trace normalisation; K V at width K timed with
-    CUDA events on the launching stream.  Algorithmic work: the two genome
-    contractions (4nmk flops, n*ceil(m/4) genotype bytes) plus the W_b
-    products (2*m*500*k flops, 4*500*m bytes of W)."""
+def smile_problem(n, m, block, dev):
+    """The c5 operator: MAF/HWE genotypes (seed 5), m/block blocks with
+    W_b ~ Wishart(block, I)/block in FP32 (seeded), kernel-trace
+    normalisation.  Returns (streamer, operator, build seconds)."""
     import torch
 
     from coherit_gb300.geno_stream import GenoBlockStreamer, SyntheticSource
     from coherit_gb300.smile_block_w import SmileBlockWeightedOperator
 
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
-    n, m, block, k = args.n or 100000, args.m or 300000, 500, args.smile
     if m % block:
         raise ValueError("m must be a multiple of the 500-SNP block size")
-    hbm_peak, tensor_peak, peak_src = _peaks()
     st = GenoBlockStreamer(SyntheticSource(n, m, seed=5), device=dev, precision="bf16x3")
     rng = np.random.default_rng(5)
     Ws = []
@@ -1007,7 +1000,108 @@ def run_smile_only(args, wl):
     t0 = time.perf_counter()
     op = SmileBlockWeightedOperator(st, Ws, normalization="kernel_trace", diag_mode="mean")
     torch.cuda.synchronize()
-    build_s = time.perf_counter() - t0
+    return st, op, time.perf_counter() - t0
+
+
+def run_lambda_path(args, wl):
+    """c5's weighted-LASSO V^-1 work along a 20-point lambda path
+    (``--lambda-path``): the SMILE operator at n=100,000 x m=300,000 (600
+    blocks of 500 SNPs, or --n/--m), H = theta_g K + theta_e I with the
+    kernel trace-normalised (theta_g = theta_e = 0.5), phenotype from 200
+    causal SNPs with Laplace(0, 0.1) effects at h2 0.5 plus an intercept.
+    A screening solve H^-1 [y, 1] gives the projected score |Z^T P y|
+    (lasso_cd.py:791-822); along the path the next 64 markers by score enter
+    the candidate set at each point and their standardised columns are
+    solved as one 64-column batched PCG (run_sparse_reml_pipeline.py:
+    1202-1297, :2300-2380), BF16x3 genotype tiles, tol 1e-5.  Device time
+    of each point's solve with CUDA events on the launching stream; column
+    extraction is reported apart."""
+    import torch
+
+    from coherit_gb300 import _lib
+    from coherit_gb300.hinv import compute_projected_hinv_vector, solve_hinv_columns_batched
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n, m, block = args.n or 100000, args.m or 300000, 500
+    points, width, tol, maxiter = 20, 64, 1e-5, 1000
+    st, op, build_s = smile_problem(n, m, block, dev)
+    rng = np.random.default_rng(55)
+    causal = rng.choice(m, size=200, replace=False)
+    beta = np.zeros((m, 1), dtype=np.float32)
+    beta[causal, 0] = rng.laplace(0.0, 0.1, size=200)
+    g = st.zxb(torch.as_tensor(beta, device=dev))[:, 0].double()
+    g = (g - g.mean()) / g.std() * np.sqrt(0.5)
+    e = torch.as_tensor(rng.standard_normal(n) * np.sqrt(0.5), device=dev)
+    y = (g + e).float()
+    ones = torch.ones(n, device=dev)
+    tg, te = 0.5, 0.5
+
+    def hv(V):
+        return tg * op.kv(V) + te * V
+
+    l0 = _lib.load().coherit_launch_count()
+    t0 = time.perf_counter()
+    sol, sdiag = solve_hinv_columns_batched(hv=hv, precond=None,
+                                            rhs=torch.stack([y, ones], dim=1).contiguous(),
+                                            warm_start=None, tol=tol, maxiter=maxiter,
+                                            batch_size=width, stage="screening")
+    u = compute_projected_hinv_vector(covar=np.ones((n, 1)),
+                                      Hinv_covar=sol[:, 1:].double().cpu().numpy(),
+                                      Hinv_target=sol[:, 0].double().cpu().numpy(), ridge=1e-6)
+    score = st.xtv(torch.as_tensor(u, dtype=torch.float32, device=dev)).abs().cpu().numpy()
+    order = np.argsort(-score, kind="stable")
+    torch.cuda.synchronize()
+    screen_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    per_point, iters, extract_s = [], [], 0.0
+    for i in range(points):
+        markers = np.sort(order[i * width:(i + 1) * width])
+        t1 = time.perf_counter()
+        Z = st.standardized_columns(markers).contiguous()
+        torch.cuda.synchronize()
+        extract_s += time.perf_counter() - t1
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, d = solve_hinv_columns_batched(hv=hv, precond=None, rhs=Z, warm_start=None, tol=tol,
+                                          maxiter=maxiter, batch_size=width,
+                                          stage=f"lambda point {i}")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        per_point.append(round(e0.elapsed_time(e1), 2))
+        iters.append(int(d["total_batch_iterations"]))
+    launches = _lib.load().coherit_launch_count() - l0
+    st.check()
+    st.close()
+    total_ms = float(sum(per_point))
+    return {"metric": "c5 lambda-path V^-1 batched solves (64 RHS per point, 20 points)",
+            "value": round(total_ms / 1e3, 3), "unit": "s", "higher_is_better": False,
+            "config": {"workload": f"c5_n{n}_m{m}_blocks{m // block}x{block}",
+                       "rhs_per_point": width, "points": points, "pcg_tol": tol,
+                       "precision": "bf16x3", "theta": [tg, te]},
+            "ms_per_point": per_point, "pcg_iterations_per_point": iters,
+            "mean_ms_per_point": round(total_ms / points, 1),
+            "screening_s": round(screen_s, 3), "screening_iterations":
+                int(sdiag["total_batch_iterations"]),
+            "column_extraction_s": round(extract_s, 3), "build_s": round(build_s, 2),
+            "gpu_launches": int(launches), "data": "synthetic (seeded)"}
+
+
+def run_smile_only(args, wl):
+    """SMILE block-weighted operator at the c5 shape (``--smile K``): n=100,000
+    x m=300,000 (or --n/--m), blocks of 500 SNPs with W_b ~ Wishart(500, I)/500
+    in FP32 (seeded), kernel-trace normalisation; K V at width K timed with
+    CUDA events on the launching stream.  Algorithmic work: the two genome
+    contractions (4nmk flops, n*ceil(m/4) genotype bytes) plus the W_b
+    products (2*m*500*k flops, 4*500*m bytes of W)."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n, m, block, k = args.n or 100000, args.m or 300000, 500, args.smile
+    hbm_peak, tensor_peak, peak_src = _peaks()
+    st, op, build_s = smile_problem(n, m, block, dev)
     V = torch.randn(n, k, device=dev)
     for _ in range(max(3, args.warmup)):
         op.kv(V)
@@ -1157,6 +1251,8 @@ def main():
                     help="run only the Poisson request stream on the workload's matrix")
     ap.add_argument("--sparse", type=int, default=0, metavar="K",
                     help="time the rare-variant operator at width K instead of fits")
+    ap.add_argument("--lambda-path", action="store_true",
+                    help="time c5's 20-point lambda path of 64-column V^-1 solves")
     ap.add_argument("--mma-rate", action="store_true",
                     help="print the tensor-core instruction issue-rate table")
     ap.add_argument("--n", type=int, default=0, help="with --operator/--sparse: samples")
@@ -1167,6 +1263,8 @@ def main():
     wl = WORKLOADS[args.config]
     if args.mma_rate:
         out = run_mma_rate(args, wl)
+    elif args.lambda_path:
+        out = run_lambda_path(args, wl)
     elif args.operator > 0:
         out = run_operator_only(args, wl)
     elif args.sparse > 0:

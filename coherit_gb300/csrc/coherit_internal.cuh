@@ -173,7 +173,7 @@ struct StatsSlot {
 // launch, precision): stage size, ring depths and the grid the split-K plan
 // aims for (target_mult x SMs).
 struct TuneChoice {
-  int wide = 0, RA = 0, RB = 0, RG = 0, target_mult = 4, cluster = 1;
+  int wide = 0, RA = 0, RB = 0, RG = 0, target_mult = 4, cluster = 1, tiles = 1;
   float ms = 0.f;
 };
 

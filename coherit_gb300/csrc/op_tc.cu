@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "coherit_internal.cuh"
 #include "tc_ptx.cuh"
@@ -722,11 +723,13 @@ struct SplitPlan {
   int64_t nr;     // K2 component blocks (G when stacked, else 1)
 };
 
-// K shares of one launch whose stages hold `sb` blocks.
-static SplitPlan split_plan(const coherit_geno* h, bool stacked, int64_t target_ctas, int sb) {
+// K shares of one launch whose stages hold `sb` blocks and whose CTAs own
+// `tiles` row tiles each.
+static SplitPlan split_plan(const coherit_geno* h, bool stacked, int64_t target_ctas, int sb,
+                            int tiles) {
   SplitPlan s;
   s.nr = stacked ? h->G : 1;
-  s.k1 = split_count(h->n_chunks / sb, h->n_ttiles, target_ctas, sb);
+  s.k1 = split_count(h->n_chunks / sb, (h->n_ttiles + tiles - 1) / tiles, target_ctas, sb);
   int64_t stages2 = h->n_panels / sb;
   if (stacked) {
     stages2 = 0;
@@ -734,7 +737,7 @@ static SplitPlan split_plan(const coherit_geno* h, bool stacked, int64_t target_
       stages2 = std::max<int64_t>(
           stages2, (h->comp_slot_start[g + 1] - h->comp_slot_start[g]) / kPanel / sb);
   }
-  s.k2 = split_count(stages2, h->n_stiles * s.nr, target_ctas, sb);
+  s.k2 = split_count(stages2, (h->n_stiles + tiles - 1) / tiles * s.nr, target_ctas, sb);
   return s;
 }
 
@@ -762,10 +765,11 @@ static size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255);
 // over both output modes.  K1's partials are consumed before K2 runs.
 static int64_t part_rows_needed(const coherit_geno* h) {
   int64_t rows = 0;
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < 8; ++q) {
     const bool stacked = (q & 1) != 0;
     const int sb = (q & 2) ? CfgWide::SB : CfgNarrow::SB;
-    const SplitPlan s = split_plan(h, stacked, target_ctas(h, kMaxTargetMult), sb);
+    const int tiles = (q & 4) ? 2 : 1;
+    const SplitPlan s = split_plan(h, stacked, target_ctas(h, kMaxTargetMult), sb, tiles);
     if (s.k1 > 1) rows = std::max<int64_t>(rows, s.k1 * h->m_pad);
     if (s.k2 > 1) rows = std::max<int64_t>(rows, s.k2 * s.nr * h->n_pad);
   }
@@ -873,6 +877,7 @@ struct TcLaunchCfg {
   bool wide;   // StageCfg<4, 2> instead of StageCfg<2, 3>
   int sb;      // blocks per stage of that configuration
   int cluster; // CTAs per cluster sharing each B tile (1, 2 or 4)
+  int tiles;   // row tiles per CTA (1, or 2 with two MMA-issuing threads)
   int RG;      // genotype ring stages
   int RB, RA;
   bool side;
@@ -886,7 +891,7 @@ struct TcLaunchCfg {
 // ring: the configuration's full depth), clamped to what fits tensor
 // memory, shared memory and the barrier arrays; cluster 0 = policy.
 struct LaunchReq {
-  int wide = -1, RA = 0, RB = 0, RG = 0, cluster = 0;
+  int wide = -1, RA = 0, RB = 0, RG = 0, cluster = 0, tiles = 0;
 };
 
 static LaunchReq req_of(const TuneChoice& t) {
@@ -896,11 +901,14 @@ static LaunchReq req_of(const TuneChoice& t) {
   r.RB = t.RB;
   r.RG = t.RG;
   r.cluster = t.cluster;
+  r.tiles = t.tiles;
   return r;
 }
 
-// CTAs per cluster of the fixed policy (no tuned choice).
+// CTAs per cluster and row tiles per CTA of the fixed policy (no tuned
+// choice); two tiles only where their accumulators and rings fit.
 constexpr int kDefaultCluster = 1;
+constexpr int kDefaultTiles = 1;
 
 // Accumulator: NSPLIT*kp columns, the split terms side by side in N (one MMA
 // per K step, N <= 256).  The A ring takes the remaining tensor-memory
@@ -915,7 +923,7 @@ static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision
   // Tensor-memory columns of one 64-K block of A (E4M3: one byte per code).
   const uint32_t acols = op_type(precision) == kTyE4M3 ? 16u : 32u;
   TcLaunchCfg c;
-  c.cluster = rq.cluster == 1 || rq.cluster == 2 || rq.cluster == 4 ? rq.cluster : kDefaultCluster;
+  c.cluster = rq.cluster == 1 || rq.cluster == 2 ? rq.cluster : kDefaultCluster;
   c.side = nsplit > 1 && nsplit * kp <= 256;
   const int acc = c.side ? nsplit * kp : kp;
   c.acc_cols = static_cast<uint32_t>(round_up(acc, 32));
@@ -923,57 +931,70 @@ static TcLaunchCfg tc_config_policy(const coherit_geno* h, int kp, int precision
   auto ring_g = [&](int sets, int full) {
     return rq.RG >= sets && rq.RG <= full && rq.RG % sets == 0 ? rq.RG : full;
   };
-  if (rq.wide != 0) {
-    // Four-block stages (half the barrier round trips per K of two-block
-    // stages) wherever their rings fit: at one CTA per SM they apply 16
-    // columns faster than two-block stages (n = 50,000, m = 500,000: k = 32
-    // in 10.5 ms against k = 16 in 12.7 ms with two-block stages).
-    const int rg = ring_g(CfgWide::SETS, CfgWide::RG);
-    const uint32_t slot = acols * CfgWide::SB;
-    const uint32_t bslot = static_cast<uint32_t>(CfgWide::SB) * nsplit * kp * kPanel * eb;
-    const size_t fixed = kBarrierBytes + static_cast<size_t>(rg) * CfgWide::SB * kBlockBytes;
-    int ra = std::min<int>(kMaxRA, static_cast<int>((512u - c.acc_cols) / slot));
-    if (rq.RA > 0) ra = std::min(ra, std::max(rq.RA, CfgWide::MIN_RA));
-    if (c.acc_cols + CfgWide::MIN_RA * slot <= 512u && ra >= CfgWide::MIN_RA &&
-        fixed + 2 * static_cast<size_t>(bslot) <= cap - 4096) {
-      c.wide = true;
-      c.sb = CfgWide::SB;
-      c.RG = rg;
-      c.tmem_cols = 512;
-      c.RA = ra;
-      c.bslot = bslot;
-      int rb = static_cast<int>((cap - 4096 - fixed) / bslot);
-      if (rq.RB > 0) rb = std::min(rb, rq.RB);
-      c.RB = std::max(2, std::min(kMaxRB, rb));
-      c.smem = fixed + static_cast<size_t>(c.RB) * bslot;
-      return c;
+  const int want_tiles = rq.tiles == 1 || rq.tiles == 2 ? rq.tiles : kDefaultTiles;
+  // Two tiles per CTA where both accumulators, an A ring of at least the
+  // minimum depth for both tiles and the doubled genotype slots fit; else one.
+  for (int tiles = want_tiles; tiles >= 1; --tiles) {
+    c.tiles = tiles;
+    const uint32_t acc_all = static_cast<uint32_t>(tiles) * c.acc_cols;
+    if (acc_all >= 512u) continue;
+    if (rq.wide != 0) {
+      // Four-block stages (half the barrier round trips per K of two-block
+      // stages) wherever their rings fit: at one CTA per SM they apply 16
+      // columns faster than two-block stages (n = 50,000, m = 500,000: k = 32
+      // in 10.5 ms against k = 16 in 12.7 ms with two-block stages).
+      const int rg = ring_g(CfgWide::SETS, CfgWide::RG);
+      const uint32_t slot = acols * CfgWide::SB * tiles;
+      const uint32_t bslot = static_cast<uint32_t>(CfgWide::SB) * nsplit * kp * kPanel * eb;
+      const size_t fixed =
+          kBarrierBytes + static_cast<size_t>(rg) * CfgWide::SB * kBlockBytes * tiles;
+      int ra = std::min<int>(kMaxRA, static_cast<int>((512u - acc_all) / slot));
+      if (rq.RA > 0) ra = std::min(ra, std::max(rq.RA, CfgWide::MIN_RA));
+      if (acc_all + CfgWide::MIN_RA * slot <= 512u && ra >= CfgWide::MIN_RA &&
+          fixed + 2 * static_cast<size_t>(bslot) <= cap - 4096) {
+        c.wide = true;
+        c.sb = CfgWide::SB;
+        c.RG = rg;
+        c.tmem_cols = 512;
+        c.RA = ra;
+        c.bslot = bslot;
+        int rb = static_cast<int>((cap - 4096 - fixed) / bslot);
+        if (rq.RB > 0) rb = std::min(rb, rq.RB);
+        c.RB = std::max(2, std::min(kMaxRB, rb));
+        c.smem = fixed + static_cast<size_t>(c.RB) * bslot;
+        return c;
+      }
     }
+    c.wide = false;
+    c.sb = CfgNarrow::SB;
+    c.RG = ring_g(CfgNarrow::SETS, CfgNarrow::RG);
+    const uint32_t slot_cols = acols * CfgNarrow::SB * tiles;
+    c.bslot = static_cast<uint32_t>(CfgNarrow::SB) * nsplit * kp * kPanel * eb;
+    const size_t fixed =
+        kBarrierBytes + static_cast<size_t>(c.RG) * CfgNarrow::SB * kBlockBytes * tiles;
+    if (tiles > 1 && (acc_all + CfgNarrow::MIN_RA * slot_cols > 512u ||
+                      fixed + 2 * static_cast<size_t>(c.bslot) > cap - 4096))
+      continue;
+    // One CTA per SM for every width: all 512 tensor-memory columns.  Layouts
+    // with two CTAs per SM returned a few wrong rows under split K (a whole
+    // lane quarter of a tile) even with CTAs of whole warpgroups.
+    c.tmem_cols = 512;
+    c.RA = std::min<int>(kMaxRA, static_cast<int>((512u - acc_all) / slot_cols));
+    if (rq.RA > 0) c.RA = std::min(c.RA, std::max(rq.RA, CfgNarrow::MIN_RA));
+    int rb = static_cast<int>((cap - 4096 - fixed) / c.bslot);
+    if (rq.RB > 0) rb = std::min(rb, rq.RB);
+    rb = std::max(2, std::min(kMaxRB, rb));
+    while (rb > 2 && fixed + static_cast<size_t>(rb) * c.bslot > cap) --rb;
+    c.RB = rb;
+    c.smem = fixed + static_cast<size_t>(rb) * c.bslot;
+    // One CTA per SM: pad the shared-memory request until a second CTA cannot
+    // fit (it would block in tcgen05.alloc).
+    const size_t sm_bytes = static_cast<size_t>(h->smem_per_sm);
+    while (static_cast<int>(sm_bytes / (c.smem + 1024)) > 1 && c.smem + 4096 <= cap)
+      c.smem += 4096;
+    return c;
   }
-  c.wide = false;
-  c.sb = CfgNarrow::SB;
-  c.RG = ring_g(CfgNarrow::SETS, CfgNarrow::RG);
-  const uint32_t slot_cols = acols * CfgNarrow::SB;
-  // One CTA per SM for every width: all 512 tensor-memory columns.  Layouts
-  // with two CTAs per SM returned a few wrong rows under split K (a whole
-  // lane quarter of a tile) even with CTAs of whole warpgroups.
-  const uint32_t cols = 512;
-  c.tmem_cols = cols;
-  c.RA = std::min<int>(kMaxRA, static_cast<int>((cols - c.acc_cols) / slot_cols));
-  if (rq.RA > 0) c.RA = std::min(c.RA, std::max(rq.RA, CfgNarrow::MIN_RA));
-  c.bslot = static_cast<uint32_t>(CfgNarrow::SB) * nsplit * kp * kPanel * eb;
-  const size_t fixed = kBarrierBytes + static_cast<size_t>(c.RG) * CfgNarrow::SB * kBlockBytes;
-  int rb = static_cast<int>((cap - 4096 - fixed) / c.bslot);
-  if (rq.RB > 0) rb = std::min(rb, rq.RB);
-  rb = std::max(2, std::min(kMaxRB, rb));
-  while (rb > 2 && fixed + static_cast<size_t>(rb) * c.bslot > cap) --rb;
-  c.RB = rb;
-  c.smem = fixed + static_cast<size_t>(rb) * c.bslot;
-  // One CTA per SM: pad the shared-memory request until a second CTA cannot
-  // fit (it would block in tcgen05.alloc).
-  const size_t sm_bytes = static_cast<size_t>(h->smem_per_sm);
-  while (static_cast<int>(sm_bytes / (c.smem + 1024)) > 1 && c.smem + 4096 <= cap)
-    c.smem += 4096;
-  return c;
+  return c;  // not reached: one tile always fits (max_kp_for)
 }
 
 // Launch configuration: the autotuner's choice for (kp, precision) when there
@@ -984,7 +1005,7 @@ static TcLaunchCfg tc_config(const coherit_geno* h, int kp, int precision) {
   return tc_config_policy(h, kp, precision, LaunchReq());
 }
 
-template <bool IS_K1, class Cfg, int CL>
+template <bool IS_K1, class Cfg, int CL, int TILES>
 static int launch_tc_cfg(int nsplit, int ty, bool side, dim3 grid, size_t smem,
                          cudaStream_t st, const TcParams& p) {
   auto go = [&](auto kern) -> int {
@@ -1013,35 +1034,44 @@ static int launch_tc_cfg(int nsplit, int ty, bool side, dim3 grid, size_t smem,
   };
   if (ty == kTyF16) {
     CO_CHECK(nsplit == 2 && side, COHERIT_E_SHAPE, "FP16 terms must fit side by side (2 kp <= 256)");
-    return go(k_tc_op<IS_K1, 2, true, Cfg, kTyF16, CL>);
+    return go(k_tc_op<IS_K1, 2, true, Cfg, kTyF16, CL, TILES>);
   }
   if (ty == kTyE4M3) {
     CO_CHECK(nsplit == 5 && side, COHERIT_E_SHAPE, "E4M3 terms must fit side by side (5 kp <= 256)");
-    return go(k_tc_op<IS_K1, 5, true, Cfg, kTyE4M3, CL>);
+    return go(k_tc_op<IS_K1, 5, true, Cfg, kTyE4M3, CL, TILES>);
   }
-  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false, Cfg, kTyBf16, CL>);
+  if (nsplit == 1) return go(k_tc_op<IS_K1, 1, false, Cfg, kTyBf16, CL, TILES>);
   CO_CHECK(side, COHERIT_E_SHAPE, "split terms must fit side by side (nsplit * kp <= 256)");
-  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true, Cfg, kTyBf16, CL>);
-  return go(k_tc_op<IS_K1, 3, true, Cfg, kTyBf16, CL>);
+  if (nsplit == 2) return go(k_tc_op<IS_K1, 2, true, Cfg, kTyBf16, CL, TILES>);
+  return go(k_tc_op<IS_K1, 3, true, Cfg, kTyBf16, CL, TILES>);
 }
 
+// Built forms: single CTAs with one or two tiles, clusters of 2 CTAs with
+// one tile each.
 template <bool IS_K1, class Cfg>
 static int launch_tc_cl(const TcLaunchCfg& cfg, int nsplit, int ty, dim3 grid, cudaStream_t st,
                         const TcParams& p) {
-  if (cfg.cluster == 4)
-    return launch_tc_cfg<IS_K1, Cfg, 4>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
+  CO_CHECK((cfg.cluster == 1 || cfg.cluster == 2) && (cfg.tiles == 1 || cfg.tiles == 2) &&
+               !(cfg.cluster == 2 && cfg.tiles == 2),
+           COHERIT_E_SHAPE, "no operator kernel for %d CTAs per cluster with %d tiles per CTA",
+           cfg.cluster, cfg.tiles);
+  if (cfg.tiles == 2)
+    return launch_tc_cfg<IS_K1, Cfg, 1, 2>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
   if (cfg.cluster == 2)
-    return launch_tc_cfg<IS_K1, Cfg, 2>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
-  return launch_tc_cfg<IS_K1, Cfg, 1>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
+    return launch_tc_cfg<IS_K1, Cfg, 2, 1>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
+  return launch_tc_cfg<IS_K1, Cfg, 1, 1>(nsplit, ty, cfg.side, grid, cfg.smem, st, p);
 }
 
-// grid.x = tiles; the launch rounds it up to whole clusters.
+// grid.x = row tiles; the launch gives each CTA cfg.tiles of them and rounds
+// the CTA count up to whole clusters.
 template <bool IS_K1>
 static int launch_tc(const TcLaunchCfg& cfg, int nsplit, int ty, dim3 grid, cudaStream_t st,
                      const TcParams& p0) {
   TcParams p = p0;
   p.n_tiles = grid.x;
   const unsigned cl = static_cast<unsigned>(cfg.cluster);
+  const unsigned tl = static_cast<unsigned>(cfg.tiles);
+  grid.x = (grid.x + tl - 1) / tl;
   grid.x = (grid.x + cl - 1) / cl * cl;
   if (cfg.wide) return launch_tc_cl<IS_K1, CfgWide>(cfg, nsplit, ty, grid, st, p);
   return launch_tc_cl<IS_K1, CfgNarrow>(cfg, nsplit, ty, grid, st, p);
@@ -1166,7 +1196,8 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   CO_CUDA(cudaMemsetAsync(rbuf, 0, sizeof(double) * nr * kp, st));
   if (f16) CO_CUDA(cudaMemsetAsync(smax, 0, sizeof(unsigned) * kp, st));
   const TcLaunchCfg cfg = tc_config(h, kp, d.precision);
-  const SplitPlan sp = split_plan(h, e.stacked != 0, target_ctas_for(h, kp, d.precision), cfg.sb);
+  const SplitPlan sp =
+      split_plan(h, e.stacked != 0, target_ctas_for(h, kp, d.precision), cfg.sb, cfg.tiles);
   float* part = reinterpret_cast<float*>(ws + L.part);
   const unsigned col_blocks = static_cast<unsigned>((kp / 16 + 3) / 4);
 
@@ -1332,92 +1363,123 @@ int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t ce = cudaEventCreate(&e0);
   if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  int nrep = reps;
   auto time_once = [&](float& ms) -> int {
     int r = run_operator(h, d, st);  // warm
     if (r != COHERIT_OK) return r;
     CO_CUDA(cudaEventRecord(e0, st));
-    for (int i = 0; i < reps && r == COHERIT_OK; ++i) r = run_operator(h, d, st);
+    for (int i = 0; i < nrep && r == COHERIT_OK; ++i) r = run_operator(h, d, st);
     if (r != COHERIT_OK) return r;
     CO_CUDA(cudaEventRecord(e1, st));
     CO_CUDA(cudaEventSynchronize(e1));
     CO_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    ms /= static_cast<float>(reps);
+    ms /= static_cast<float>(nrep);
     return COHERIT_OK;
   };
   float t_def = 0.f;
   if (rc == COHERIT_OK && ce == cudaSuccess) rc = time_once(t_def);
-  // Candidates: stage size x genotype-ring depth (full, or half where that
-  // frees shared memory for another B slot) x A-ring depth x B-ring depth x
-  // split-K grid.
-  TuneChoice best;
-  best.ms = t_def;
+  TuneChoice def;
   {
     const TcLaunchCfg c0 = tc_config_policy(h, kp, prec, LaunchReq());
-    best.wide = c0.wide ? 1 : 0;
-    best.RA = c0.RA;
-    best.RB = c0.RB;
-    best.RG = c0.RG;
-    best.target_mult = kDefaultTargetMult;
-    best.cluster = c0.cluster;
+    def.wide = c0.wide ? 1 : 0;
+    def.RA = c0.RA;
+    def.RB = c0.RB;
+    def.RG = c0.RG;
+    def.target_mult = kDefaultTargetMult;
+    def.cluster = c0.cluster;
+    def.tiles = c0.tiles;
+    def.ms = t_def;
   }
+  std::vector<TuneChoice> timed;
   int tried = 0;
-  for (int wide = 1; wide >= 0 && rc == COHERIT_OK && ce == cudaSuccess; --wide) {
-    LaunchReq rq;
-    rq.wide = wide;
-    const TcLaunchCfg full = tc_config_policy(h, kp, prec, rq);
-    if ((full.wide ? 1 : 0) != wide) continue;  // four-block rings do not fit
-    const int sets = wide ? CfgWide::SETS : CfgNarrow::SETS;
-    const int rgs[2] = {full.RG, 2 * sets};
-    for (int ig = 0; ig < 2 && rc == COHERIT_OK; ++ig) {
-      rq.RG = rgs[ig];
-      const TcLaunchCfg fg = tc_config_policy(h, kp, prec, rq);
-      if (ig == 1 && (rgs[1] == rgs[0] || fg.RB <= full.RB)) continue;
-      const int ra_min = wide ? CfgWide::MIN_RA : CfgNarrow::MIN_RA;
-      const int ras[2] = {fg.RA, std::max(ra_min, fg.RA / 2)};
-      const int rbs[3] = {fg.RB, std::max(2, fg.RB / 2), 2};
-      for (int ia = 0; ia < 2 && rc == COHERIT_OK; ++ia) {
-        if (ia == 1 && ras[1] == ras[0]) continue;
-        for (int ib = 0; ib < 3 && rc == COHERIT_OK; ++ib) {
-          if ((ib == 1 && rbs[1] == rbs[0]) ||
-              (ib == 2 && (rbs[2] == rbs[1] || rbs[2] == rbs[0])))
-            continue;
-          for (int mult = 2; mult <= kMaxTargetMult && rc == COHERIT_OK; mult *= 2) {
-            TuneChoice c;
-            c.cluster = 1;
-            c.wide = wide;
-            c.RG = rgs[ig];
-            c.RA = ras[ia];
-            c.RB = rbs[ib];
-            c.target_mult = mult;
-            h->tuned[key] = c;
-            float ms = 0.f;
-            rc = time_once(ms);
-            ++tried;
-            if (rc == COHERIT_OK && ms < best.ms) {
-              best = c;
-              best.ms = ms;
+  auto try_choice = [&](TuneChoice c) {
+    if (rc != COHERIT_OK || ce != cudaSuccess) return;
+    h->tuned[key] = c;
+    float ms = 0.f;
+    rc = time_once(ms);
+    ++tried;
+    if (rc == COHERIT_OK) {
+      c.ms = ms;
+      timed.push_back(c);
+    }
+  };
+  // Candidates: tiles per CTA x stage size x genotype-ring depth (full, or
+  // two stages per decoder set where that frees shared memory for another B
+  // slot) x A-ring depth x B-ring depth x split-K grid.
+  for (int tiles = 1; tiles <= 2; ++tiles) {
+    for (int wide = 1; wide >= 0; --wide) {
+      LaunchReq rq;
+      rq.wide = wide;
+      rq.tiles = tiles;
+      const TcLaunchCfg full = tc_config_policy(h, kp, prec, rq);
+      if ((full.wide ? 1 : 0) != wide || full.tiles != tiles) continue;  // rings do not fit
+      const int sets = wide ? CfgWide::SETS : CfgNarrow::SETS;
+      const int rgs[2] = {full.RG, 2 * sets};
+      for (int ig = 0; ig < 2; ++ig) {
+        rq.RG = rgs[ig];
+        const TcLaunchCfg fg = tc_config_policy(h, kp, prec, rq);
+        if (ig == 1 && (rgs[1] == rgs[0] || fg.RB <= full.RB)) continue;
+        const int ra_min = wide ? CfgWide::MIN_RA : CfgNarrow::MIN_RA;
+        const int ras[2] = {fg.RA, std::max(ra_min, fg.RA / 2)};
+        const int rbs[3] = {fg.RB, std::max(2, fg.RB / 2), 2};
+        for (int ia = 0; ia < 2; ++ia) {
+          if (ia == 1 && ras[1] == ras[0]) continue;
+          for (int ib = 0; ib < 3; ++ib) {
+            if ((ib == 1 && rbs[1] == rbs[0]) ||
+                (ib == 2 && (rbs[2] == rbs[1] || rbs[2] == rbs[0])))
+              continue;
+            for (int mult = 2; mult <= kMaxTargetMult; mult *= 2) {
+              TuneChoice c;
+              c.cluster = 1;
+              c.tiles = tiles;
+              c.wide = wide;
+              c.RG = rgs[ig];
+              c.RA = ras[ia];
+              c.RB = rbs[ib];
+              c.target_mult = mult;
+              try_choice(c);
             }
           }
         }
       }
     }
   }
-  // Clusters of 2 or 4 CTAs sharing every B tile, on the best rings found
-  // without them.
-  const TuneChoice single = best;
-  for (int cl = 2; cl <= 4 && rc == COHERIT_OK && ce == cudaSuccess; cl *= 2) {
-    for (int mult = 2; mult <= kMaxTargetMult && rc == COHERIT_OK; mult *= 2) {
-      TuneChoice c = single;
-      c.cluster = cl;
+  // Clusters of 2 CTAs sharing every B tile, on the best one-tile rings.
+  {
+    TuneChoice b1 = def;
+    for (const TuneChoice& c : timed)
+      if (c.tiles == 1 && c.ms < b1.ms) b1 = c;
+    for (int mult = 2; mult <= kMaxTargetMult; mult *= 2) {
+      TuneChoice c = b1;
+      c.cluster = 2;
+      c.tiles = 1;
       c.target_mult = mult;
+      try_choice(c);
+    }
+  }
+  // One timed application is noisy (clock and power state): re-time the
+  // fastest three and the fixed policy with three times the repetitions
+  // and keep the fastest.
+  TuneChoice best = def;
+  if (rc == COHERIT_OK && ce == cudaSuccess) {
+    std::sort(timed.begin(), timed.end(),
+              [](const TuneChoice& x, const TuneChoice& y) { return x.ms < y.ms; });
+    if (timed.size() > 3) timed.resize(3);
+    timed.push_back(def);
+    nrep = 3 * reps;
+    best.ms = 3.4e38f;
+    for (TuneChoice c : timed) {
+      if (rc != COHERIT_OK) break;
       h->tuned[key] = c;
       float ms = 0.f;
       rc = time_once(ms);
-      ++tried;
       if (rc == COHERIT_OK && ms < best.ms) {
         best = c;
         best.ms = ms;
       }
+      if (c.wide == def.wide && c.RA == def.RA && c.RB == def.RB && c.RG == def.RG &&
+          c.target_mult == def.target_mult && c.cluster == def.cluster && c.tiles == def.tiles)
+        t_def = ms;
     }
   }
   h->tuned[key] = best;
@@ -1445,6 +1507,7 @@ int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32
     choice[4] = tried;
     choice[5] = best.cluster;
     choice[6] = best.RG;
+    choice[7] = best.tiles;
   }
   if (best_ms) *best_ms = best.ms;
   if (default_ms) *default_ms = t_def;
@@ -1469,12 +1532,15 @@ int coherit_geno_set_launch(coherit_geno_t* h, int32_t k, int32_t precision,
            kMaxRB);
   CO_CHECK(cfg[3] == 2 || cfg[3] == 4 || cfg[3] == 8, COHERIT_E_SHAPE,
            "grid multiple must be 2, 4 or 8");
-  CO_CHECK(cfg[5] == 1 || cfg[5] == 2 || cfg[5] == 4, COHERIT_E_SHAPE,
-           "CTAs per cluster must be 1, 2 or 4");
+  CO_CHECK(cfg[5] == 1 || cfg[5] == 2, COHERIT_E_SHAPE, "CTAs per cluster must be 1 or 2");
   CO_CHECK(cfg[6] >= 0 && cfg[6] <= CfgNarrow::RG, COHERIT_E_SHAPE,
            "genotype ring depth must lie in [0, %d] (0 = full)", CfgNarrow::RG);
+  CO_CHECK(cfg[7] == 1 || cfg[7] == 2, COHERIT_E_SHAPE, "tiles per CTA must be 1 or 2");
+  CO_CHECK(!(cfg[5] == 2 && cfg[7] == 2), COHERIT_E_SHAPE,
+           "clusters of 2 CTAs run one tile per CTA");
   TuneChoice c;
   c.RG = cfg[6];
+  c.tiles = cfg[7];
   c.wide = cfg[0];
   c.RA = cfg[1];
   c.RB = cfg[2];

@@ -25,6 +25,17 @@
 // with the number of MMAs into one accumulator), so the host bounds every
 // chain this way.
 //
+// Two tiles per CTA (TILES = 2): the CTA owns two consecutive row tiles of
+// the same K share, which read the same B tile at every stage.  One genotype
+// ring slot holds both tiles' blocks of a stage, each decoder warp decodes
+// its rows of both tiles into one A-ring slot (tile 0's blocks, then tile
+// 1's), and two threads issue the MMAs -- lane 0 of warp 1 for tile 0 into
+// accumulator 0, lane 0 of warp 3 for tile 1 into accumulator 1 -- so the
+// SM runs two instruction streams (one thread pays a fixed ~120 cycles per
+// tcgen05.mma whatever N is) on one B supply.  A and B slots are released
+// when both issuers' commits have arrived.  A padding tile (odd tile count)
+// repeats the last tile without writing results.
+//
 // Clusters (CL > 1): the CL CTAs of a cluster own consecutive tiles of the
 // same K share and so read the same B tile at every stage.  Each copies 1/CL
 // of the stage into the B ring of every CTA of the cluster (bulk copy with
@@ -36,8 +47,9 @@
 // whole number of clusters; a padding CTA repeats the last tile without
 // writing results.
 
-template <bool IS_K1, int NSPLIT, bool SIDE, class Cfg, int TY, int CL>
+template <bool IS_K1, int NSPLIT, bool SIDE, class Cfg, int TY, int CL, int TILES>
 __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant__ TcParams p) {
+  static_assert(TILES == 1 || TILES == 2, "one or two tiles per CTA");
   constexpr int kStageBlocks = Cfg::SB;
   // Tensor-memory columns of one 64-K block of A: 32 for 16-bit operands,
   // 16 for E4M3 bytes.
@@ -54,10 +66,11 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
   uint64_t* done = emptyA + kMaxRA;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-  constexpr int kStageBytes = kStageBlocks * kBlockBytes;
+  constexpr int kStageBytes = kStageBlocks * kBlockBytes;   // one tile's blocks of a stage
+  constexpr int kGSlotBytes = TILES * kStageBytes;           // a genotype ring slot
   uint8_t* gring = smem + kBarrierBytes;
   const int kRG = p.RG;
-  uint8_t* bring = gring + kRG * kStageBytes;
+  uint8_t* bring = gring + kRG * kGSlotBytes;
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -66,19 +79,28 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
   const int RA = p.RA;
   const int RB = p.RB;
 
-  const bool active = blockIdx.x < p.n_tiles;
-  const int64_t tile = active ? static_cast<int64_t>(blockIdx.x) : p.n_tiles - 1;
+  // Tile t of this CTA: row tile blockIdx.x * TILES + t (padding tiles past
+  // the last one repeat it and write nothing).
+  int64_t tile[TILES];
+  bool active[TILES];
+#pragma unroll
+  for (int t = 0; t < TILES; ++t) {
+    const int64_t tt = static_cast<int64_t>(blockIdx.x) * TILES + t;
+    active[t] = tt < p.n_tiles;
+    tile[t] = active[t] ? tt : p.n_tiles - 1;
+  }
   const int comp = blockIdx.y;
   constexpr uint16_t kClusterMask = static_cast<uint16_t>((1u << CL) - 1u);
   const int zsplit = blockIdx.z;
   int64_t ntot;
-  const uint8_t* gbase;
+  const uint8_t* gbase[TILES];
   const uint8_t* bbase;
   const int64_t stage_b_bytes = kStageBlocks * p.b_chunk_bytes;
   // Stages of kStageBlocks consecutive 2 KB blocks along K.
   if (IS_K1) {
     ntot = p.n_chunks / kStageBlocks;
-    gbase = p.geno + tile * p.n_chunks * kBlockBytes;
+#pragma unroll
+    for (int t = 0; t < TILES; ++t) gbase[t] = p.geno + tile[t] * p.n_chunks * kBlockBytes;
     bbase = p.bsrc;
   } else {
     int64_t p0 = 0, p1 = p.n_panels;
@@ -87,7 +109,8 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
       p1 = p.comp_slot_start[comp + 1] / kPanel;
     }
     ntot = (p1 - p0) / kStageBlocks;
-    gbase = p.geno + (tile * p.n_panels + p0) * kBlockBytes;
+#pragma unroll
+    for (int t = 0; t < TILES; ++t) gbase[t] = p.geno + (tile[t] * p.n_panels + p0) * kBlockBytes;
     bbase = p.bsrc + p0 * p.b_chunk_bytes;
   }
   // This CTA's share of the K stages: [s0, s0 + nch).  The host keeps a
@@ -95,7 +118,8 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
   // hold.
   const int64_t s0 = ntot * zsplit / p.ksplit;
   const int nch = static_cast<int>(ntot * (zsplit + 1) / p.ksplit - s0);
-  gbase += s0 * (kStageBlocks * kBlockBytes);
+#pragma unroll
+  for (int t = 0; t < TILES; ++t) gbase[t] += s0 * kStageBytes;
   bbase += s0 * stage_b_bytes;
 
   if (threadIdx.x == 0) {
@@ -104,15 +128,17 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
       ptx::mbar_init(&fullG[i], 1);
       ptx::mbar_init(&emptyG[i], 4);
     }
+    // Empty barriers of the A and B rings and `done` count one commit per
+    // issuing thread (per CTA of the cluster for B).
     for (int i = 0; i < kMaxRB; ++i) {
       ptx::mbar_init(&fullB[i], 1);
-      ptx::mbar_init(&emptyB[i], CL);
+      ptx::mbar_init(&emptyB[i], CL * TILES);
     }
     for (int i = 0; i < kMaxRA; ++i) {
       ptx::mbar_init(&decoded[i], 4);
-      ptx::mbar_init(&emptyA[i], 1);
+      ptx::mbar_init(&emptyA[i], TILES);
     }
-    ptx::mbar_init(done, 1);
+    ptx::mbar_init(done, TILES);
     *abort_flag = 0;
     ptx::fence_barrier_init();
   }
@@ -131,10 +157,12 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
                         p.ksplit >= 1 && static_cast<int>(gridDim.z) == p.ksplit &&
                         (p.ksplit == 1 || p.part != nullptr) &&
                         acc_need <= p.acc_cols && (p.acc_cols & 31u) == 0 &&
-                        p.acc_cols + static_cast<uint32_t>(p.RA) * kACols * kStageBlocks <= p.tmem_cols &&
+                        TILES * p.acc_cols +
+                                static_cast<uint32_t>(p.RA) * kACols * kStageBlocks * TILES <=
+                            p.tmem_cols &&
                         p.tmem_cols >= 32 && p.tmem_cols <= 512 &&
                         (p.tmem_cols & (p.tmem_cols - 1)) == 0 && acc_need <= 256 && (e.kp & 15) == 0 &&
-                        p.n_tiles >= 1 && p.n_tiles <= static_cast<int64_t>(gridDim.x) &&
+                        p.n_tiles >= 1 && p.n_tiles <= static_cast<int64_t>(gridDim.x) * TILES &&
                         gridDim.x % CL == 0 && p.bslot_bytes % (16u * CL) == 0;
     if (!cfg_ok) {
       if (threadIdx.x == 0) atomicCAS(p.err, 0, 30);
@@ -160,9 +188,11 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
       uint32_t ph = 0;
       for (int c = 0; c < nch; ++c) {
         if (c >= kRG && !ptx::mbar_wait(&emptyG[s], ph ^ 1u, p.err, 11, abort_flag)) break;
-        ptx::mbar_arrive_expect_tx(&fullG[s], kStageBytes);
-        ptx::bulk_g2s(gring + s * kStageBytes, gbase + static_cast<int64_t>(c) * kStageBytes,
-                      kStageBytes, &fullG[s]);
+        ptx::mbar_arrive_expect_tx(&fullG[s], kGSlotBytes);
+#pragma unroll
+        for (int t = 0; t < TILES; ++t)
+          ptx::bulk_g2s(gring + s * kGSlotBytes + t * kStageBytes,
+                        gbase[t] + static_cast<int64_t>(c) * kStageBytes, kStageBytes, &fullG[s]);
         issued = c + 1;
         if (++s == kRG) { s = 0; ph ^= 1u; }
       }
@@ -214,8 +244,10 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
         }
       }
     }
-  } else if (warp == kWarpMMA) {
+  } else if (warp == kWarpMMA || (TILES == 2 && warp == kWarpIdle)) {
     // ------------------------------------------------------------ MMA issue
+    // Warp 1 issues tile 0's MMAs, warp 3 (two tiles per CTA) tile 1's.
+    const int mt = warp == kWarpMMA ? 0 : 1;
     if (lane == 0) {
       const int nn = SIDE ? NSPLIT * kp : kp;
       const uint32_t idesc = TY == kTyE4M3 ? ptx::idesc_e4m3_f32(128, nn)
@@ -233,8 +265,9 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
         if (!ptx::mbar_wait(&fullB[bs], pb, p.err, 14, abort_flag)) break;
         ptx::tc_fence_after();
         const uint64_t bslot = bdesc0 + ((static_cast<uint64_t>(bs) * p.bslot_bytes) >> 4);
-        const uint32_t a_slot =
-            tmem + p.acc_cols + static_cast<uint32_t>(as) * (kACols * kStageBlocks);
+        const uint32_t a_slot = tmem + TILES * p.acc_cols +
+                                static_cast<uint32_t>(as * TILES + mt) * (kACols * kStageBlocks);
+        const uint32_t dacc = tmem + static_cast<uint32_t>(mt) * p.acc_cols;
         const uint32_t first = c == 0 ? 0u : 1u;
 #pragma unroll
         for (int b = 0; b < kStageBlocks; ++b) {
@@ -246,13 +279,13 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
           for (int ks = 0; ks < (TY == kTyE4M3 ? 2 : 4); ++ks) {
             const uint32_t acc0 = (b == 0 && ks == 0) ? first : 1u;
             if (TY == kTyE4M3) {
-              ptx::mma_ts_f8(tmem, a_col + ks * 8, bblk + ks * 16, idesc, acc0);
+              ptx::mma_ts_f8(dacc, a_col + ks * 8, bblk + ks * 16, idesc, acc0);
             } else if (SIDE) {
-              ptx::mma_ts(tmem, a_col + ks * 8, bblk + ks * 16, idesc, acc0);
+              ptx::mma_ts(dacc, a_col + ks * 8, bblk + ks * 16, idesc, acc0);
             } else {
 #pragma unroll
               for (int t = 0; t < NSPLIT; ++t)
-                ptx::mma_ts(tmem, a_col + ks * 8, bblk + ks * 16 + t * term_off, idesc,
+                ptx::mma_ts(dacc, a_col + ks * 8, bblk + ks * 16 + t * term_off, idesc,
                             t == 0 ? acc0 : 1u);
             }
           }
@@ -277,7 +310,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
       }
     }
   } else if (warp == kWarpIdle) {
-    // Pads the CTA to whole warpgroups (see StageCfg::THREADS).
+    // One tile per CTA: pads the CTA to whole warpgroups (see StageCfg::THREADS).
   } else {
     // --------------------------------------------- decoders, then epilogue
     // Decoder warp sets: set s handles chunks s, s + kSets, ...; within a set
@@ -295,11 +328,13 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
     for (int c = set; c < nch; c += kSets) {
       bool w_ok = ptx::mbar_wait(&fullG[gs], gph, p.err, 15, abort_flag);
       if (!__all_sync(0xffffffffu, w_ok)) { ok = false; break; }
-      uint4 raw[kStageBlocks];
+      uint4 raw[TILES][kStageBlocks];
 #pragma unroll
-      for (int b = 0; b < kStageBlocks; ++b)
-        raw[b] = *reinterpret_cast<const uint4*>(gring + gs * kStageBytes + b * kBlockBytes +
-                                                 row * kRowBytes);
+      for (int t = 0; t < TILES; ++t)
+#pragma unroll
+        for (int b = 0; b < kStageBlocks; ++b)
+          raw[t][b] = *reinterpret_cast<const uint4*>(gring + gs * kGSlotBytes + t * kStageBytes +
+                                                      b * kBlockBytes + row * kRowBytes);
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&emptyG[gs]);
       if (c >= RA) {
@@ -308,19 +343,22 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
       }
       ptx::tc_fence_after();
 #pragma unroll
-      for (int b = 0; b < kStageBlocks; ++b) {
-        const uint32_t col = tmem + lane_base + p.acc_cols +
-                             static_cast<uint32_t>(as * kStageBlocks + b) * kACols;
-        if constexpr (TY == kTyE4M3) {
-          uint32_t a[16];
-          decode_row_e4m3(raw[b], a);
-          ptx::tmem_st16(col, a);
-        } else {
-          uint32_t a[32];
-          decode_row<TY == kTyF16>(raw[b], a);
-          ptx::tmem_st32(col, a);
+      for (int t = 0; t < TILES; ++t)
+#pragma unroll
+        for (int b = 0; b < kStageBlocks; ++b) {
+          const uint32_t col =
+              tmem + lane_base + TILES * p.acc_cols +
+              static_cast<uint32_t>((as * TILES + t) * kStageBlocks + b) * kACols;
+          if constexpr (TY == kTyE4M3) {
+            uint32_t a[16];
+            decode_row_e4m3(raw[t][b], a);
+            ptx::tmem_st16(col, a);
+          } else {
+            uint32_t a[32];
+            decode_row<TY == kTyF16>(raw[t][b], a);
+            ptx::tmem_st32(col, a);
+          }
         }
-      }
       ptx::tmem_wait_st();
       ptx::tc_fence_before();
       __syncwarp();
@@ -334,46 +372,52 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_tc_op(const __grid_constant
       const bool w_ok = ptx::mbar_wait(done, 0, p.err, 17, abort_flag);
       ok = __all_sync(0xffffffffu, w_ok);
     }
-    if (ok && active) {
+    if (ok) {
       ptx::tc_fence_after();
-      const int64_t rowid = tile * kTile + row;
-      // Column chunks of 16 rotate over the kSets warps of a quarter.
-      for (int c0 = 16 * set; c0 < kp; c0 += 16 * kSets) {
-        float T[16];
-        if (nch > 0) {
-          uint32_t r[16];
-          ptx::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(c0), r);
-          ptx::tmem_wait_ld();
 #pragma unroll
-          for (int i = 0; i < 16; ++i) T[i] = __uint_as_float(r[i]);
-          if (SIDE) {
-            // Terms side by side: 16-bit terms share one scale; E4M3 term t
-            // carries 16^t (each holds the previous residual times 16).
+      for (int t = 0; t < TILES; ++t) {
+        if (!active[t]) continue;
+        const int64_t rowid = tile[t] * kTile + row;
+        const uint32_t acc = tmem + lane_base + static_cast<uint32_t>(t) * p.acc_cols;
+        // Column chunks of 16 rotate over the kSets warps of a quarter.
+        for (int c0 = 16 * set; c0 < kp; c0 += 16 * kSets) {
+          float T[16];
+          if (nch > 0) {
+            uint32_t r[16];
+            ptx::tmem_ld16(acc + static_cast<uint32_t>(c0), r);
+            ptx::tmem_wait_ld();
 #pragma unroll
-            for (int t = 1; t < NSPLIT; ++t) {
-              ptx::tmem_ld16(tmem + lane_base + static_cast<uint32_t>(t * kp + c0), r);
-              ptx::tmem_wait_ld();
-              const float wt = TY == kTyE4M3 ? ldexpf(1.f, -4 * t) : 1.f;
+            for (int i = 0; i < 16; ++i) T[i] = __uint_as_float(r[i]);
+            if (SIDE) {
+              // Terms side by side: 16-bit terms share one scale; E4M3 term
+              // u carries 16^u (each holds the previous residual times 16).
 #pragma unroll
-              for (int i = 0; i < 16; ++i) T[i] = fmaf(wt, __uint_as_float(r[i]), T[i]);
+              for (int u = 1; u < NSPLIT; ++u) {
+                ptx::tmem_ld16(acc + static_cast<uint32_t>(u * kp + c0), r);
+                ptx::tmem_wait_ld();
+                const float wt = TY == kTyE4M3 ? ldexpf(1.f, -4 * u) : 1.f;
+#pragma unroll
+                for (int i = 0; i < 16; ++i) T[i] = fmaf(wt, __uint_as_float(r[i]), T[i]);
+              }
             }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) T[i] = 0.f;
           }
-        } else {
+          if (p.ksplit > 1) {
+            // Partial of this K share: row (K1: slot; K2: component, sample).
+            const int64_t prow =
+                IS_K1 ? rowid : static_cast<int64_t>(comp) * p.part_rows + rowid;
+            float4* dst =
+                reinterpret_cast<float4*>(p.part + zsplit * p.part_stride + prow * kp + c0);
 #pragma unroll
-          for (int i = 0; i < 16; ++i) T[i] = 0.f;
-        }
-        if (p.ksplit > 1) {
-          // Partial of this K share: row (K1: slot; K2: component, sample).
-          const int64_t prow = IS_K1 ? rowid : static_cast<int64_t>(comp) * p.part_rows + rowid;
-          float4* dst = reinterpret_cast<float4*>(
-              p.part + zsplit * p.part_stride + prow * kp + c0);
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-            dst[q] = make_float4(T[4 * q], T[4 * q + 1], T[4 * q + 2], T[4 * q + 3]);
-        } else if (IS_K1) {
-          epilogue_k1(e, rowid, c0, T, lane);
-        } else {
-          epilogue_k2(e, rowid, comp, c0, T);
+            for (int q = 0; q < 4; ++q)
+              dst[q] = make_float4(T[4 * q], T[4 * q + 1], T[4 * q + 2], T[4 * q + 3]);
+          } else if (IS_K1) {
+            epilogue_k1(e, rowid, c0, T, lane);
+          } else {
+            epilogue_k2(e, rowid, comp, c0, T);
+          }
         }
       }
     }

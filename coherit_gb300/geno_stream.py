@@ -559,14 +559,14 @@ class GenoBlockStreamer:
 
     def autotune(self, widths, precision: str | None = None, reps: int = 2) -> list:
         """Time candidate launch configurations of the operator for each
-        width (stage size, ring depths, split-K grid, CTAs per cluster sharing
-        each B tile) on these genotypes and
+        width (stage size, ring depths, split-K grid, row tiles per CTA, CTAs
+        per cluster sharing each B tile) on these genotypes and
         keep the fastest for later launches of that width and precision
         (coherit_geno_autotune).  Returns one record per width."""
         out = []
         prec = self._prec_code(precision)
         for k in widths:
-            ch = (C.c_int32 * 7)()
+            ch = (C.c_int32 * 8)()
             best, dflt = C.c_float(), C.c_float()
             _lib.check(self._lib.coherit_geno_autotune(
                 self._h(), int(k), prec, int(reps), ch, C.byref(best), C.byref(dflt),
@@ -574,14 +574,14 @@ class GenoBlockStreamer:
             out.append({"k": int(k), "precision": precision or self.precision,
                         "four_block_stages": bool(ch[0]), "a_ring": int(ch[1]),
                         "b_ring": int(ch[2]), "g_ring": int(ch[6]), "grid_x_sms": int(ch[3]),
-                        "cluster": int(ch[5]),
+                        "cluster": int(ch[5]), "tiles_per_cta": int(ch[7]),
                         "candidates": int(ch[4]),
                         "best_ms": round(best.value, 4), "default_ms": round(dflt.value, 4)})
         return out
 
     def set_launch(self, k: int, precision: str | None = None, *, four_block_stages: bool = True,
                    a_ring: int = 0, b_ring: int = 0, grid_x_sms: int = 4, cluster: int = 1,
-                   g_ring: int = 0, policy: bool = False) -> None:
+                   g_ring: int = 0, tiles: int = 1, policy: bool = False) -> None:
         """Pin the launch configuration of width k (coherit_geno_set_launch);
         ``policy=True`` returns the width to the fixed policy."""
         prec = self._prec_code(precision)
@@ -589,8 +589,8 @@ class GenoBlockStreamer:
             _lib.check(self._lib.coherit_geno_set_launch(self._h(), int(k), prec, None),
                        "set_launch")
             return
-        cfg = (C.c_int32 * 7)(int(bool(four_block_stages)), int(a_ring), int(b_ring),
-                              int(grid_x_sms), 0, int(cluster), int(g_ring))
+        cfg = (C.c_int32 * 8)(int(bool(four_block_stages)), int(a_ring), int(b_ring),
+                              int(grid_x_sms), 0, int(cluster), int(g_ring), int(tiles))
         _lib.check(self._lib.coherit_geno_set_launch(self._h(), int(k), prec, cfg), "set_launch")
 
     def _prec_code(self, precision) -> int:

@@ -234,16 +234,18 @@ int coherit_geno_reserve(coherit_geno_t* h, int32_t k_max, int32_t precision);
  * `precision` (AUTO resolves by width) on this handle's genotypes and stats
  * slot 0 under each candidate configuration -- two- or four-block pipeline
  * stages, tensor-memory A-ring depth, shared-memory B-ring depth, and the
- * grid size (2, 4 or 8 x SMs) the split-K plan fills, and clusters of 2 or
- * 4 CTAs that share each B tile (one multicast copy from L2 instead of one
- * per CTA) -- `reps` timed applications each (CUDA events on `stream`), and
- * keeps the fastest for every later launch of that width and precision on
- * the handle.  Allocates and frees two n x k buffers; synchronises `stream`.
- * Genotype-ring depth is a candidate too (full, or two stages per decoder
- * set where that frees shared memory for another B slot).
- * choice (7 ints, may be NULL): four-block stages (0/1), A-ring slots,
+ * grid size (2, 4 or 8 x SMs) the split-K plan fills, one or two row tiles
+ * per CTA (two MMA-issuing threads on one B supply), and clusters of 2 CTAs
+ * that share each B tile (one multicast copy from L2 instead of one per
+ * CTA) -- `reps` timed applications each (CUDA events on `stream`); the
+ * fastest three and the fixed policy are timed again with 3 x `reps`, and
+ * the fastest is kept for every later launch of that width and precision
+ * on the handle.  Allocates and frees two n x k buffers; synchronises
+ * `stream`.  Genotype-ring depth is a candidate too (full, or two stages per
+ * decoder set where that frees shared memory for another B slot).
+ * choice (8 ints, may be NULL): four-block stages (0/1), A-ring slots,
  * B-ring slots, grid multiple, candidates tried, CTAs per cluster,
- * genotype-ring stages;
+ * genotype-ring stages, row tiles per CTA;
  * best_ms / default_ms: per-application times of the kept and of the
  * fixed-policy configuration.                                             */
 int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32_t reps,
@@ -251,13 +253,14 @@ int coherit_geno_autotune(coherit_geno_t* h, int32_t k, int32_t precision, int32
 
 /* Pin the launch configuration of width k (rounded up to 16) and
  * `precision` (AUTO resolves by width) on this handle, in place of the fixed
- * policy or a tuned choice (no counterpart in the reference): cfg (7 ints,
+ * policy or a tuned choice (no counterpart in the reference): cfg (8 ints,
  * the layout of coherit_geno_autotune's choice) = four-block stages (0/1),
  * A-ring slots, B-ring slots (0 = largest that fits; depths are clamped to
- * what fits), grid multiple (2, 4 or 8), unused, CTAs per cluster (1, 2 or
- * 4), genotype-ring stages (0 = full; else a multiple of the decoder sets,
- * 2 for four-block and 3 for two-block stages).  cfg NULL returns the width
- * to the fixed policy.                                                     */
+ * what fits), grid multiple (2, 4 or 8), unused, CTAs per cluster (1 or 2),
+ * genotype-ring stages (0 = full; else a multiple of the decoder sets, 2
+ * for four-block and 3 for two-block stages), row tiles per CTA (1 or 2;
+ * 2 falls back to 1 where both accumulators and rings do not fit; not with
+ * clusters).  cfg NULL returns the width to the fixed policy.              */
 int coherit_geno_set_launch(coherit_geno_t* h, int32_t k, int32_t precision, const int32_t* cfg);
 
 /* Tensor-core instruction-rate probe (no counterpart in the reference: it
