@@ -83,6 +83,14 @@ class FitConfig:
     optimizer: str = "strict"
     precision: str = "bf16x3"
     sketch_precision: str = "bf16x1"
+    # SLQ probe-batch workspace in bytes.  None: the reference's policy from
+    # gpu_budget_bytes (256 MiB without one, at most 2 GiB), which batches 2
+    # probes per operator application at n = 100,000 and 30 Lanczos steps.
+    # A larger workspace batches more probes per application (each probe's
+    # Lanczos recurrence is independent, so the results do not change) --
+    # on a GPU whose HBM holds the whole probe block, fewer and wider
+    # launches.
+    slq_workspace_bytes: int | None = None
     # SMILE block-weighted GRMs (reml_model.py:42-53): exactly one W mode.
     smile_w_files: Sequence[str] | None = None
     smile_w_file_groups: Sequence[Sequence[str]] | None = None
@@ -555,7 +563,8 @@ class InfinitesimalREMLFitter:
                 n_rand_vec=cfg.n_rand_vec, maxiter=cfg.max_pcg_iters, seed=cfg.seed + r * 9973,
                 h2_init=h2_init, param_init=var_components_init, minq_iter=cfg.minq_iter,
                 slq_samples=cfg.slq_samples, slq_m=cfg.slq_m, slq_mode=cfg.slq_mode,
-                slq_workspace_bytes=default_workspace_bytes(cfg.gpu_budget_bytes),
+                slq_workspace_bytes=(int(cfg.slq_workspace_bytes) if cfg.slq_workspace_bytes
+                                     else default_workspace_bytes(cfg.gpu_budget_bytes)),
                 precond_conf=conf, slq_precond_conf=conf, precond_refresh_fn=refresh,
                 precond_eps=cfg.pcg_ridge, weighted_hv=ops.weighted_hv, stacked_kv=ops.stacked_kv,
                 optimizer=cfg.smile_optimizer if self._smile_operators else cfg.optimizer,

@@ -132,6 +132,10 @@ class _Batcher:
         self.columns = 0
         self.requests_per_launch: list[int] = []
         self.last_launch: torch.cuda.Event | None = None  # completion of the latest launch
+        # (start, end) events of the latest launches (launch number
+        # _events_base + index): device time of the operator.
+        self.launch_events: list[tuple] = []
+        self._events_base = 0
         self._busy_cap_s = 0.25  # longest wait for stragglers while the device is busy
         self.thread = threading.Thread(target=self._loop, name="coherit-batcher", daemon=True)
         self.thread.start()
@@ -159,6 +163,15 @@ class _Batcher:
         if op.error is not None:
             raise op.error
         return op.out[:, 0] if vec else op.out
+
+    def device_ms(self, first: int = 0) -> float:
+        """Device time of launch number `first` onwards, as far as their events
+        are kept (synchronises with the last one)."""
+        evs = self.launch_events[max(0, first - self._events_base):]
+        if not evs:
+            return 0.0
+        evs[-1][1].synchronize()
+        return float(sum(a.elapsed_time(b) for a, b in evs))
 
     def close(self) -> None:
         with self.cv:
@@ -243,14 +256,21 @@ class _Batcher:
         te = np.asarray([0.0 if op.theta_e is None else op.theta_e for op, _, _ in pieces],
                         dtype=np.float32)
         out = torch.empty_like(Vf)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
         with self.lib_lock:
             _lib.check(_lib.load().coherit_geno_kv_batched(
                 st.handle, len(pieces), col_start.ctypes.data, slots.ctypes.data, self.prec,
                 Vf.data_ptr(), K, K, scale.ctypes.data, te.ctypes.data, out.data_ptr(), K,
                 _lib.stream_ptr()), "batched kv")
-        ev = torch.cuda.Event()
+        ev = torch.cuda.Event(enable_timing=True)
         ev.record()
         self.last_launch = ev
+        self.launch_events.append((ev0, ev))
+        if len(self.launch_events) > 8192:  # bounded: keep the latest half
+            drop = len(self.launch_events) // 2
+            del self.launch_events[:drop]
+            self._events_base += drop
         st.op_stats["apps"] += 1
         st.op_stats["cols"] += K
         self.launches += 1
