@@ -125,7 +125,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
+        sm, smax, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         with open(self.path) as f:
             for line in f:
@@ -137,12 +137,18 @@ class ClockSampler:
                     smax.append(float(parts[2]))
                 except ValueError:
                     continue
+                try:
+                    power.append(float(parts[3].split()[0]))
+                except (ValueError, IndexError):
+                    pass
                 for name, val in zip(names, parts[5:9]):
                     if val.lower() == "active":
                         reasons.add(name)
         os.unlink(self.path)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
+                "sm_mhz_min": min(sm) if sm else None,
+                "power_w_median": statistics.median(power) if power else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
@@ -979,11 +985,14 @@ def run_operator_only(args, wl):
     stream = torch.cuda.current_stream()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(0)
+    sampler.start()
     e0.record(stream)
     for _ in range(args.steps):
         st.kv(V, precision=args.precision)
     e1.record(stream)
     torch.cuda.synchronize()
+    clocks = sampler.stop()
     ms = e0.elapsed_time(e1) / args.steps
     launches = _lib.load().coherit_launch_count() - l0
     alg_bytes = st.n * ((st.m + 3) // 4) + 8 * st.n * k + 8 * st.m
@@ -995,7 +1004,7 @@ def run_operator_only(args, wl):
             "config": {"workload": wl.name, "n": wl.n, "m": wl.m, "k": k},
             "hbm_gbs": round(alg_bytes / (ms * 1e-3) / 1e9, 1),
             "tensor_tflops": round(4.0 * wl.n * wl.m * k / (ms * 1e-3) / 1e12, 1),
-            "gpu_launches": int(launches), "peak_source": peak_src}
+            "gpu_launches": int(launches), "clocks": clocks, "peak_source": peak_src}
 
 
 def smile_problem(n, m, block, dev):

@@ -112,3 +112,40 @@ def test_fitter_with_preconditioner_two_components(cuda):
     atoms = st._component_mean_diag_atoms_host.astype(np.float64)
     h2_ref = oreml.heritability(po, 2, atoms)
     assert abs(res.heritability - h2_ref) < 1e-3, (res.heritability, h2_ref)
+
+
+def test_slq_probe_batching_does_not_change_value_or_gradient(cuda):
+    """The SLQ workspace decides how many probes share one operator
+    application (slq.py:24-41); each probe's Lanczos recurrence is
+    independent, so one probe per batch and all probes in one batch give
+    the same log-determinant and gradient up to the FP32 rounding of the
+    products at another block width (1e-5 relative)."""
+    from coherit_gb300 import slq
+
+    n, p, m = 400, 8, 12
+    rng = np.random.default_rng(2)
+    A = rng.standard_normal((n, n // 2))
+    K = torch.as_tensor(A @ A.T / (n // 2), dtype=torch.float32, device=cuda)
+    theta = np.array([0.6, 0.4])
+
+    def Hv(v):
+        return float(theta[0]) * (K @ v) + float(theta[1]) * v
+
+    def pullback(left, right):
+        kl = K @ left
+        res = float(theta[0]) * kl + float(theta[1]) * left
+        scores = torch.stack([torch.sum(right.double() * kl.double()),
+                              torch.sum(right.double() * left.double())])
+        return res, scores
+
+    probes = torch.as_tensor(rng.choice([-1.0, 1.0], size=(n, p)), dtype=torch.float32,
+                             device=cuda)
+    per_probe = 4 * n * (8 * (m + 1) + 32)
+    out = []
+    for ws in (per_probe, 64 * per_probe):
+        assert slq.workspace_layout(n, p, m, ws)["batch_width"] in (1, p)
+        v, g = slq.logdet_value_and_grad(Hv, pullback, n, 0, nsamples=p, m=m,
+                                         workspace_bytes=ws, probes=probes)
+        out.append((float(v), g.cpu().numpy()))
+    assert abs(out[0][0] - out[1][0]) <= 1e-5 * abs(out[1][0])
+    np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-5, atol=1e-8)
