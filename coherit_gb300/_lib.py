@@ -116,6 +116,11 @@ _SIGNATURES = {
         C.c_int,
         [_i64, _i32, _p, _i64, _p, _i64, _p, _p, _p, _p, _p, _p, _p],
     ),
+    "coherit_lowrank_workspace_floats": (C.c_int, [_i64, _i32, _i32, _p]),
+    "coherit_lowrank_apply": (
+        C.c_int,
+        [_i64, _i32, _i32, _p, _i64, _p, _i64, _f32, _p, _i64, _p, _i64, _p, _i64, _p],
+    ),
     "coherit_selftest_mma": (C.c_int, [_i32, _p, _p]),
     "coherit_sparse_create_bed": (
         C.c_int,

@@ -255,19 +255,32 @@ __device__ __forceinline__ void epilogue_k1(const EpiParams& e, int64_t j, int c
   const int g0 = __shfl_sync(0xffffffffu, gi, 0);
   const bool uniform = __all_sync(0xffffffffu, gi == g0);
   const int64_t term = static_cast<int64_t>(e.kp) * kPanel;
-  // abar dsum_j + sum_z d_z dseg_jz for the 16 columns (shifts are 0 beyond k).
+  // abar dsum_j + sum_z d_z dseg_jz for the 16 columns (shifts are 0 beyond
+  // k).  Columns of one request share the slot's dseg row: each run of
+  // columns of one group reads it once (one load per segment, not one per
+  // segment and column).
   float seg[16];
   const float* dev_rows = e.shift + static_cast<int64_t>(e.n_seg + 1) * e.kp;
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    seg[i] = 0.f;
-    const int c = c0 + i;
-    if (c >= e.k) continue;
-    const int grp = group_of(e, c);
+  for (int i = 0; i < 16; ++i) seg[i] = 0.f;
+  for (int i0 = 0; i0 < 16 && c0 + i0 < e.k;) {
+    const int grp = group_of(e, c0 + i0);
+    int i1 = i0 + 1;
+    while (i1 < 16 && c0 + i1 < e.k && group_of(e, c0 + i1) == grp) ++i1;
     const float* ds = e.gdseg[grp] + j * e.n_seg;
-    float acc = 0.f;
-    for (int z = 0; z < e.n_seg; ++z) acc = fmaf(dev_rows[z * e.kp + c], ds[z], acc);
-    seg[i] = fmaf(e.shift[e.n_seg * e.kp + c], e.gdsum[grp][j], acc);
+    for (int z = 0; z < e.n_seg; ++z) {
+      const float d = ds[z];
+      const float* dr = dev_rows + static_cast<int64_t>(z) * e.kp + c0;
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+        if (i >= i0 && i < i1) seg[i] = fmaf(dr[i], d, seg[i]);
+    }
+    const float dsum = e.gdsum[grp][j];
+    const float* abar = e.shift + static_cast<int64_t>(e.n_seg) * e.kp + c0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+      if (i >= i0 && i < i1) seg[i] = fmaf(abar[i], dsum, seg[i]);
+    i0 = i1;
   }
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
@@ -647,10 +660,15 @@ __global__ void k_split_s(const __grid_constant__ EpiParams e) {
   const int kk = static_cast<int>(j % kPanel);
   const int64_t term = static_cast<int64_t>(e.kp) * kPanel;  // elements of one term
   const int top = scale_top(e.ty);
+  // The row's S values in 16-byte loads (kp is a multiple of 16).
+  const float4* srow = reinterpret_cast<const float4*>(e.sf32 + (active ? j : 0) * e.kp);
+  float4 sv4 = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int c = 0; c < e.kp; ++c) {
     float sval = 0.f, mu = 0.f;
+    if ((c & 3) == 0 && active) sv4 = srow[c >> 2];
     if (active && c < e.k) {
-      sval = e.sf32[j * e.kp + c];
+      const int q = c & 3;
+      sval = q == 0 ? sv4.x : q == 1 ? sv4.y : q == 2 ? sv4.z : sv4.w;
       mu = e.gmean[group_of(e, c)][j];
     }
     if (active) {

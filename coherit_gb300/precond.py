@@ -4,9 +4,12 @@ For an orthonormal basis U (n x r) the inverse and inverse square root act
 on the r-dimensional projection only:
     M^{-1} v    = d^{-1} v + U ((dI + C)^{-1} - d^{-1} I) U^T v      (precond.py:42-58)
     M^{-1/2} v  = d^{-1/2} v + U ((dI + C)^{-1/2} - d^{-1/2} I) U^T v (precond.py:61-84)
-The two skinny n x r products run as cuBLAS GEMMs on the device; the r x r
-factorisations (Cholesky, eigh) as cuSOLVER calls.  The Nystrom basis takes
-two operator applications on n x (r + 8) blocks (precond.py:251-276).
+On the GPU both applies run as one library call, out = a V + U (G (U^T V))
+(coherit_lowrank_apply: the two n-long contractions and the r x r product
+in the library's own kernels), with the r x r core G formed once per
+factorisation; host tensors take the explicit formulas above.  The r x r
+factorisations (Cholesky, eigh) are cuSOLVER calls.  The Nystrom basis
+takes two operator applications on n x (r + 8) blocks (precond.py:251-276).
 """
 from __future__ import annotations
 
@@ -32,7 +35,10 @@ class ProjectedCorePrecondConf:
 
 @dataclass
 class ProjectedCoreRuntime:
-    """Theta-specific factorisation (precond.py:29-39)."""
+    """Theta-specific factorisation (precond.py:29-39).  On the GPU also the
+    r x r cores of the fused apply: G = (dI + C)^{-1} - d^{-1} I and, with
+    the eigendecomposition, Q diag(e^{-1/2}) Q^T - d^{-1/2} I, with their
+    scalars 1/d and d^{-1/2} as host floats."""
 
     U: torch.Tensor
     total_rank: int
@@ -41,6 +47,32 @@ class ProjectedCoreRuntime:
     chol: torch.Tensor
     eigvals: Optional[torch.Tensor] = None
     eigvecs: Optional[torch.Tensor] = None
+    core_inv: Optional[torch.Tensor] = None
+    core_invsqrt: Optional[torch.Tensor] = None
+    a_inv: float = 0.0
+    a_invsqrt: float = 0.0
+
+
+def _lowrank_apply(v, U, G, a: float):
+    """a v + U (G (U^T v)) in one library call (coherit_lowrank_apply)."""
+    import ctypes as C
+
+    from . import _lib
+
+    vec = v.ndim == 1
+    V = (v[:, None] if vec else v).to(torch.float32).contiguous()
+    n, k = V.shape
+    r = U.shape[1]
+    lib = _lib.load()
+    floats = C.c_int64()
+    _lib.check(lib.coherit_lowrank_workspace_floats(n, r, k, C.byref(floats)), "low-rank apply")
+    work = torch.empty(int(floats.value), dtype=torch.float32, device=V.device)
+    out = torch.empty_like(V)
+    _lib.check(lib.coherit_lowrank_apply(n, r, k, U.data_ptr(), U.stride(0), G.data_ptr(),
+                                         G.stride(0), float(a), V.data_ptr(), V.stride(0),
+                                         out.data_ptr(), out.stride(0), work.data_ptr(),
+                                         int(floats.value), _lib.stream_ptr()), "low-rank apply")
+    return out[:, 0] if vec else out
 
 
 def _apply_scalar_diag(v: torch.Tensor, d_inv, chol, U) -> torch.Tensor:
@@ -129,8 +161,20 @@ def build_projected_core_runtime(precond_conf, theta_g, diag_H, eps: float = 0.0
     if need_invsqrt:
         ev, eigvecs = torch.linalg.eigh(middle)
         eigvals = torch.clamp(ev, min=1e-8)
-    return ProjectedCoreRuntime(U=U, total_rank=r, d=d, d_inv=1.0 / d, chol=chol,
-                                eigvals=eigvals, eigvecs=eigvecs)
+    rt = ProjectedCoreRuntime(U=U, total_rank=r, d=d, d_inv=1.0 / d, chol=chol,
+                              eigvals=eigvals, eigvecs=eigvecs)
+    if U.is_cuda and U.dtype == torch.float32 and U.is_contiguous():
+        # Cores of the fused apply, formed in FP64 from the factorisations.
+        dd = float(d)
+        eye64 = torch.eye(r, dtype=torch.float64, device=U.device)
+        rt.a_inv = 1.0 / dd
+        rt.core_inv = (torch.cholesky_inverse(chol.double()) - eye64 / dd).float().contiguous()
+        if need_invsqrt:
+            q = eigvecs.double()
+            rt.a_invsqrt = dd ** -0.5
+            rt.core_invsqrt = ((q / torch.sqrt(eigvals.double())[None, :]) @ q.T -
+                               eye64 * dd ** -0.5).float().contiguous()
+    return rt
 
 
 def make_projected_core_precond_from_runtime(runtime) -> Optional[Callable]:
@@ -138,6 +182,8 @@ def make_projected_core_precond_from_runtime(runtime) -> Optional[Callable]:
         return None
 
     def apply(v):
+        if runtime.core_inv is not None and isinstance(v, torch.Tensor) and v.is_cuda:
+            return _lowrank_apply(v, runtime.U, runtime.core_inv, runtime.a_inv)
         return _apply_scalar_diag(v, runtime.d_inv, runtime.chol, runtime.U)
 
     return apply
@@ -148,6 +194,8 @@ def projected_core_apply_invsqrt(runtime: ProjectedCoreRuntime, v):
         raise ValueError(
             "Projected-core runtime missing eigendecomposition required for inverse-square-root apply."
         )
+    if runtime.core_invsqrt is not None and isinstance(v, torch.Tensor) and v.is_cuda:
+        return _lowrank_apply(v, runtime.U, runtime.core_invsqrt, runtime.a_invsqrt)
     return _apply_invsqrt(v, torch.sqrt(runtime.d_inv), runtime.eigvals, runtime.eigvecs,
                           runtime.U)
 

@@ -360,6 +360,20 @@ int coherit_pcg_direction_update(int64_t n, int32_t k, float* P, int64_t ldp,
                                  const double* rnorm2, double* rs_old, const double* threshold,
                                  uint8_t* active, double* rnorm_out, void* stream);
 
+/* Projected-core preconditioner apply (precond.py:42-84): out = a V + U (G
+ * (U^T V)) for the basis U (device, n x r, row stride ldu), the r x r core
+ * G (device, row stride ldg) and V (device, n x k), in the library's own
+ * kernels (FP32, the slice sums of U^T V in FP64).  M^{-1} V takes
+ * G = (dI + C)^{-1} - d^{-1} I and a = 1/d; M^{-1/2} V takes
+ * G = Q diag(e^{-1/2}) Q^T - d^{-1/2} I and a = d^{-1/2}.  work: device
+ * scratch of coherit_lowrank_workspace_floats(n, r, k) floats.  Replaces
+ * _apply_scalar_diag / _apply_invsqrt (precond.py:42-84).                   */
+int coherit_lowrank_workspace_floats(int64_t n, int32_t r, int32_t k, int64_t* floats);
+int coherit_lowrank_apply(int64_t n, int32_t r, int32_t k, const float* U, int64_t ldu,
+                          const float* G, int64_t ldg, float a, const float* V, int64_t ldv,
+                          float* out, int64_t ldo, float* work, int64_t work_floats,
+                          void* stream);
+
 /* ------------------------------------------- rare-variant sparse operator */
 
 /* Rare-variant ("sparse12") genotype matrix: per-SNP lists of the non-zero

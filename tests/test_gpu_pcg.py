@@ -171,3 +171,41 @@ def test_genotype_operator_solve_matches_oracle(cuda):
     rel_err = np.linalg.norm(xs - exact, axis=0) / np.linalg.norm(exact, axis=0)
     assert np.max(rel_err) < 1e-5
     assert abs(it - ito) <= 2
+
+
+def test_lowrank_apply_matches_fp64_formulas(cuda):
+    """The fused projected-core applies (coherit_lowrank_apply) against the
+    explicit formulas in FP64 (precond.py:42-84): M^{-1} V and M^{-1/2} V for
+    an orthonormal basis, odd n and k (partial tiles), vector and block."""
+    from coherit_gb300 import precond as pc
+
+    n, r, k = 5003, 72, 13
+    g = torch.Generator(device="cpu").manual_seed(4)
+    U, _ = torch.linalg.qr(torch.randn(n, r, generator=g, dtype=torch.float64))
+    A = torch.randn(r, r, generator=g, dtype=torch.float64)
+    C = A @ A.T / r
+    d = 0.7
+    U32 = U.float().contiguous().to(cuda)
+    eye = torch.eye(r, dtype=torch.float32, device=cuda)
+    conf = pc.ProjectedCorePrecondConf(
+        U=U32, core_atoms=C.float().to(cuda)[None], total_rank=r, n_grm=1,
+        diag_mode="scalar_identity", diag_atoms=torch.zeros(1, device=cuda),
+        residual_diag_atoms=torch.ones(1, device=cuda), identity=eye)
+    rt = pc.build_projected_core_runtime(conf, torch.ones(1, device=cuda),
+                                         torch.tensor(d, device=cuda), need_invsqrt=True)
+    assert rt.core_inv is not None and rt.core_invsqrt is not None
+    V = torch.randn(n, k, generator=g, dtype=torch.float64)
+    mid = C + d * torch.eye(r, dtype=torch.float64)
+    want = V / d + U @ ((torch.linalg.inv(mid) - torch.eye(r, dtype=torch.float64) / d)
+                        @ (U.T @ V))
+    ev, q = torch.linalg.eigh(mid)
+    isq = (q / torch.sqrt(ev)[None, :]) @ q.T - torch.eye(r, dtype=torch.float64) / d ** 0.5
+    want_sq = V / d ** 0.5 + U @ (isq @ (U.T @ V))
+    Vd = V.float().to(cuda)
+    got = pc.make_projected_core_precond_from_runtime(rt)(Vd).double().cpu()
+    got_sq = pc.projected_core_apply_invsqrt(rt, Vd).double().cpu()
+    for a, b in ((got, want), (got_sq, want_sq)):
+        rel = ((a - b).norm(dim=0) / b.norm(dim=0)).max().item()
+        assert rel < 1e-5, rel
+    vec = pc.make_projected_core_precond_from_runtime(rt)(Vd[:, 3]).double().cpu()
+    assert ((vec - want[:, 3]).norm() / want[:, 3].norm()).item() < 1e-5
