@@ -156,8 +156,8 @@ struct StatsSlot {
   // * mean_j (observed allele sum minus observed count times the FP32 mean;
   // zero up to the rounding of mean_j; 0 for padding slots).
   float* dsum = nullptr;
-  // m_pad x n_seg, device, slot-major: the same sum over the samples of each
-  // centring segment z (4,096 samples).
+  // n_seg x m_pad, device, segment-major (consecutive slots adjacent): the
+  // same sum over the samples of each centring segment z (4,096 samples).
   float* dseg = nullptr;
   float* nseg = nullptr;  // n_seg, device: samples of the slot in each segment
   uint8_t* row_mask = nullptr;  // n_pad bytes, device; nullptr = all samples

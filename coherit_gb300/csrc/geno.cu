@@ -308,7 +308,7 @@ __global__ void k_slot_counts(const uint8_t* __restrict__ geno_t, int64_t m_pad,
   n3o[j] = a3;
 }
 
-// Sums of diff per slot: dseg[j, z] = s1_jz - cnt_jz mu_j over segment z
+// Sums of diff per slot: dseg[z, j] = s1_jz - cnt_jz mu_j over segment z
 // (chunks [64 z, 64 z + 64)) and dsum[j] = s1_j - cnt_j mu_j over all the
 // slot's samples, each in FP64 from integer counts, stored in FP32.
 // nseg[z] = samples of the slot in segment z.
@@ -339,7 +339,7 @@ __global__ void k_slot_seg_dsum(const uint8_t* __restrict__ geno_t, int64_t m_pa
     }
     const double cnt = static_cast<double>(nseg[z]) - static_cast<double>(n3);
     const double s1 = static_cast<double>(n1 + 2 * n2);
-    dseg[j * n_seg + z] = pad ? 0.f : static_cast<float>(s1 - cnt * mu);
+    dseg[static_cast<int64_t>(z) * m_pad + j] = pad ? 0.f : static_cast<float>(s1 - cnt * mu);
     s1_all += s1;
     cnt_all += cnt;
   }

@@ -78,6 +78,7 @@ constexpr int kMaxRA = 6;
 constexpr int kMaxRB = 16;     // B ring depth limit
 constexpr int kMaxGroups = 32;
 constexpr int kMaxScale = 256;
+constexpr int kMaxSplitCols = 128;  // widest scaled-form launch (FP16x2: 2 x 128 <= 256)
 constexpr int kBarrierBytes = 1024;
 
 struct EpiParams {
@@ -88,7 +89,7 @@ struct EpiParams {
   const float* gmean[kMaxGroups];
   const float* ginv[kMaxGroups];
   const float* gdsum[kMaxGroups];  // m_pad sums of diff over the group slot's samples
-  const float* gdseg[kMaxGroups];  // m_pad x n_seg segment sums of diff
+  const float* gdseg[kMaxGroups];  // n_seg x m_pad segment sums of diff (segment-major)
   const float* gnseg[kMaxGroups];  // n_seg samples per segment of the group's slot
   int n_seg;                       // centring segments
   const uint8_t* gmask[kMaxGroups];
@@ -166,6 +167,28 @@ __device__ __forceinline__ void decode_row(const uint4 raw, uint32_t (&a)[32]) {
       a[8 * w + 2 * s + 1] = __byte_perm(L, H, sel >> 16);
     }
   }
+}
+
+// Warp sum of mu * s over the 32 lanes with FP32 arithmetic that keeps the
+// rounding errors: each product as hi + lo (lo = fma(mu, s, -hi), exact), the
+// lane sums by TwoSum (Knuth) with the errors carried in lo.  Returns hi + lo
+// in FP64 (lane 0 adds it to the FP64 accumulator); GB300's FP64 rate is a
+// small fraction of FP32, and one product per row and column fed FP64 warp
+// shuffles before.
+__device__ __forceinline__ double warp_sum_product(float mu, float s) {
+  float hi = mu * s;
+  float lo = fmaf(mu, s, -hi);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, off);
+    const float ol = __shfl_xor_sync(0xffffffffu, lo, off);
+    const float sum = hi + oh;
+    const float bp = sum - hi;
+    const float err = (hi - (sum - bp)) + (oh - bp);
+    hi = sum;
+    lo = lo + ol + err;
+  }
+  return static_cast<double>(hi) + static_cast<double>(lo);
 }
 
 __device__ __forceinline__ void split3(float v, __nv_bfloat16& hi, __nv_bfloat16& mid,
@@ -267,9 +290,9 @@ __device__ __forceinline__ void epilogue_k1(const EpiParams& e, int64_t j, int c
     const int grp = group_of(e, c0 + i0);
     int i1 = i0 + 1;
     while (i1 < 16 && c0 + i1 < e.k && group_of(e, c0 + i1) == grp) ++i1;
-    const float* ds = e.gdseg[grp] + j * e.n_seg;
+    const float* ds = e.gdseg[grp] + j;
     for (int z = 0; z < e.n_seg; ++z) {
-      const float d = ds[z];
+      const float d = ds[static_cast<int64_t>(z) * e.m_pad];
       const float* dr = dev_rows + static_cast<int64_t>(z) * e.kp + c0;
 #pragma unroll
       for (int i = 0; i < 16; ++i)
@@ -308,7 +331,10 @@ __device__ __forceinline__ void epilogue_k1(const EpiParams& e, int64_t j, int c
       unsigned u = __float_as_uint(fabsf(sval));
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) u = max(u, __shfl_xor_sync(0xffffffffu, u, off));
-      if (lane == 0 && c < e.k) atomicMax(&e.smax[c], u);
+      // The column maximum only grows: skip the atomic (all warps of the
+      // launch contend for kp addresses) unless this warp's maximum exceeds
+      // the current one, read from L2.
+      if (lane == 0 && c < e.k && u > __ldcg(&e.smax[c])) atomicMax(&e.smax[c], u);
       continue;
     }
     const int64_t base = pnl * (e.nsplit * term) + btile_off(c, kk);
@@ -319,13 +345,11 @@ __device__ __forceinline__ void epilogue_k1(const EpiParams& e, int64_t j, int c
     if (e.nsplit > 2) e.sbuf[base + 2 * term] = lo;
     if (c >= e.k) continue;
     if (e.sf32 != nullptr) e.sf32[j * e.kp + c] = sval;
-    double v = static_cast<double>(mu) * static_cast<double>(sval);
     if (uniform) {
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      const double v = warp_sum_product(mu, sval);
       if (lane == 0) atomicAdd(&e.rbuf[gi * e.kp + c], v);
     } else {
-      atomicAdd(&e.rbuf[gi * e.kp + c], v);
+      atomicAdd(&e.rbuf[gi * e.kp + c], static_cast<double>(mu) * static_cast<double>(sval));
     }
   }
 }
@@ -620,7 +644,10 @@ __global__ void k_prep_s_from_b(const float* __restrict__ b, int64_t ldb,
       unsigned u = __float_as_uint(fabsf(sval));
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) u = max(u, __shfl_xor_sync(0xffffffffu, u, off));
-      if (lane == 0 && c < e.k) atomicMax(&e.smax[c], u);
+      // The column maximum only grows: skip the atomic (all warps of the
+      // launch contend for kp addresses) unless this warp's maximum exceeds
+      // the current one, read from L2.
+      if (lane == 0 && c < e.k && u > __ldcg(&e.smax[c])) atomicMax(&e.smax[c], u);
       continue;
     }
     if (active) {
@@ -648,12 +675,23 @@ __global__ void k_prep_s_from_b(const float* __restrict__ b, int64_t ldb,
 // (per component when stacked).  One thread per slot; a warp's 32 slots lie
 // in one component (components start on multiples of 256 slots), checked
 // before the warp reduction.
-__global__ void k_split_s(const __grid_constant__ EpiParams e) {
+// Threads per block of k_split_s: its per-column sums of mu S are combined
+// over the block's warps in shared memory before one FP64 atomic per block
+// and column (one per warp and column serialised on the 48-odd addresses).
+constexpr int kSplitThreads = 256;
+
+__global__ void __launch_bounds__(kSplitThreads) k_split_s(const __grid_constant__ EpiParams e) {
+  __shared__ double red[kSplitThreads / 32][kMaxSplitCols];
+  __shared__ int block_g;
   const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   const bool active = j < e.m_pad;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = active ? e.comp_of_slot[j] : 0;
   const int gi = e.stacked ? g : 0;
+  if (threadIdx.x == 0) block_g = gi;
+  __syncthreads();
+  // One component for the whole block: sums per warp into shared memory.
+  const bool block_uniform = __syncthreads_and(gi == block_g) != 0;
   const int g0 = __shfl_sync(0xffffffffu, gi, 0);
   const bool uniform = __all_sync(0xffffffffu, gi == g0);
   const int64_t pnl = j / kPanel;
@@ -689,13 +727,24 @@ __global__ void k_split_s(const __grid_constant__ EpiParams e) {
       }
     }
     if (c >= e.k) continue;
-    double v = static_cast<double>(mu) * static_cast<double>(sval);
-    if (uniform) {
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (block_uniform) {
+      const double v = warp_sum_product(mu, sval);
+      if (lane == 0) red[warp][c] = v;
+    } else if (uniform) {
+      const double v = warp_sum_product(mu, sval);
       if (lane == 0 && v != 0.0) atomicAdd(&e.rbuf[gi * e.kp + c], v);
-    } else if (v != 0.0) {
-      atomicAdd(&e.rbuf[gi * e.kp + c], v);
+    } else {
+      const double v = static_cast<double>(mu) * static_cast<double>(sval);
+      if (v != 0.0) atomicAdd(&e.rbuf[gi * e.kp + c], v);
+    }
+  }
+  if (block_uniform) {
+    __syncthreads();
+    for (int c = threadIdx.x; c < e.k; c += blockDim.x) {
+      double t = 0.0;
+#pragma unroll
+      for (int w = 0; w < kSplitThreads / 32; ++w) t += red[w][c];
+      if (t != 0.0) atomicAdd(&e.rbuf[block_g * e.kp + c], t);
     }
   }
 }
@@ -1278,7 +1327,10 @@ static int launch_operator(coherit_geno* h, const OpDesc& d, int kp, int nsplit,
   }
   if (f16) {
     // S's column maxima are known once every slot tile is done: FP16 tiles now.
-    k_split_s<<<static_cast<unsigned>((h->m_pad + 127) / 128), 128, 0, st>>>(e); note_launch();
+    CO_CHECK(kp <= kMaxSplitCols, COHERIT_E_SHAPE, "scaled forms take at most %d columns",
+             kMaxSplitCols);
+    k_split_s<<<static_cast<unsigned>((h->m_pad + kSplitThreads - 1) / kSplitThreads),
+                kSplitThreads, 0, st>>>(e); note_launch();
     CO_CUDA(cudaGetLastError());
   }
   p.geno = h->geno_s;
