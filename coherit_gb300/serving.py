@@ -118,11 +118,15 @@ class _Batcher:
     """
 
     def __init__(self, streamer: GenoBlockStreamer, precision: str, window_s: float,
-                 max_cols: int, lib_lock: threading.Lock):
+                 max_cols: int, lib_lock: threading.Lock, launch_ms: dict | None = None):
         self.st = streamer
         self.prec = _lib.PRECISIONS[precision]
         self.window_s = float(window_s)
         self.max_cols = int(max_cols)
+        # Measured time of one launch per width (multiples of 16): the
+        # pending columns are then cut into the launches of least total time.
+        self.launch_ms = {int(w): float(t) for w, t in (launch_ms or {}).items()
+                          if int(w) % 16 == 0 and 0 < int(w) <= self.max_cols}
         self.lib_lock = lib_lock
         self.cv = threading.Condition()
         self.pending: list[_Op] = []
@@ -206,17 +210,36 @@ class _Batcher:
                 if left <= 0:
                     break
                 self.cv.wait(timeout=min(left, 0.0005))
+            width = self._first_width(sum(op.V.shape[1] - op.next_col for op in self.pending))
             pieces, cols = [], 0
-            while self.pending and cols < self.max_cols:
+            while self.pending and cols < width:
                 op = self.pending[0]
                 lo = op.next_col
-                hi = min(op.V.shape[1], lo + self.max_cols - cols)
+                hi = min(op.V.shape[1], lo + width - cols)
                 pieces.append((op, lo, hi))
                 cols += hi - lo
                 op.next_col = hi
                 if hi == op.V.shape[1]:
                     self.pending.pop(0)
             return pieces
+
+    def _first_width(self, total: int) -> int:
+        """Width of the next launch: max_cols, or with measured launch times
+        the first launch of the cheapest cut of `total` pending columns into
+        launches of the measured widths (the last may be padded)."""
+        if not self.launch_ms or total <= 0:
+            return self.max_cols
+        widths = sorted(self.launch_ms)
+        units = -(-total // 16)
+        best = [0.0] + [float("inf")] * units
+        first = [0] * (units + 1)
+        for u in range(1, units + 1):
+            for w in widths:
+                rest = max(0, u - w // 16)
+                t = self.launch_ms[w] + best[rest]
+                if t < best[u]:
+                    best[u], first[u] = t, w
+        return max(16, min(first[units] or self.max_cols, self.max_cols))
 
     def _loop(self) -> None:
         while True:
@@ -307,6 +330,10 @@ class REMLServer:
     ``fit_kwargs`` go to ``fit_reml`` (defaults: 30 trace probes, 30 SLQ
     probes x 30 Lanczos steps, PCG tol 1e-5, 20 AI iterations).
 
+    ``launch_ms`` ({width: ms}, e.g. from ``GenoBlockStreamer.autotune``)
+    lets the batcher cut the pending right-hand sides into the launches of
+    least measured total time instead of filling ``max_batch_cols`` first.
+
     ``precond_rank`` > 0 gives every fit's PCG solves a projected-core
     preconditioner of that rank (reml_model.py:863-960, single GRM): a
     Nystrom basis U of the request's own kernel (K over its sample subset)
@@ -320,7 +347,8 @@ class REMLServer:
     def __init__(self, streamer: GenoBlockStreamer, *, max_active: int = 8,
                  hbm_budget_bytes: float | None = None, precision: str = "bf16x3",
                  batch_window_s: float = 0.01, max_batch_cols: int | None = None,
-                 fit_kwargs: dict | None = None, precond_rank: int = 0):
+                 fit_kwargs: dict | None = None, precond_rank: int = 0,
+                 launch_ms: dict | None = None):
         if streamer.n_components != 1:
             raise ValueError("REMLServer serves single-GRM fits (one genotype component).")
         if precision not in _MAX_BATCH_COLS:
@@ -344,7 +372,8 @@ class REMLServer:
                 "reserve stats slots")
         _init_device_linalg(streamer.dev)
         cols = _MAX_BATCH_COLS[precision] if max_batch_cols is None else int(max_batch_cols)
-        self.batcher = _Batcher(streamer, precision, batch_window_s, cols, self._lib_lock)
+        self.batcher = _Batcher(streamer, precision, batch_window_s, cols, self._lib_lock,
+                                launch_ms=launch_ms)
         self.fit_kwargs = dict(n_rand_vec=30, maxiter=500, minq_iter=20, slq_samples=30,
                                slq_m=30, pcg_tol=1e-5, verbose=False)
         if fit_kwargs:

@@ -36,6 +36,9 @@ def _fake_batcher(max_cols, fail_when=None):
     b.requests_per_launch = []
     b.last_launch = None
     b._busy_cap_s = 0.25
+    b.launch_ms = {}
+    b.launch_events = []
+    b._events_base = 0
     b.widths = []
 
     def launch(self, pieces):
@@ -214,3 +217,20 @@ def test_submit_validates_and_estimates_solver_memory():
     srv._closed = True
     with pytest.raises(RuntimeError, match="closed"):
         srv.submit(np.zeros(100))
+
+
+def test_batcher_cuts_pending_columns_by_measured_launch_times():
+    """With measured launch times per width the batcher opens the cheapest
+    cut of the pending columns; without them it fills max_cols."""
+    from coherit_gb300 import serving
+
+    b = serving._Batcher.__new__(serving._Batcher)
+    b.max_cols = 80
+    b.launch_ms = {}
+    assert b._first_width(96) == 80
+    b.launch_ms = {16: 25.1, 32: 26.2, 48: 29.9, 64: 47.2, 80: 47.9}
+    assert b._first_width(6) == 16
+    assert b._first_width(48) == 48
+    assert b._first_width(50) == 64          # one 64-column launch beats 48 + 16
+    assert b._first_width(96) == 48          # 48 + 48 beats 80 + 16
+    assert b._first_width(160) == 80
