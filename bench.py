@@ -565,8 +565,7 @@ def run_ours(args, wl):
         widths = list(range(16, _MAX_BATCH_COLS.get(args.precision, 80) + 1, 16))
         tuner = st.autotune(widths, precision=args.precision, reps=1)
     srv = REMLServer(st, max_active=R, precision=args.precision, fit_kwargs=fit_kwargs(wl),
-                     batch_window_s=args.batch_window,
-                     launch_ms=None if tuner is None else {r["k"]: r["best_ms"] for r in tuner})
+                     batch_window_s=args.batch_window)
 
     cold_fit_s = None
     for w in range(args.warmup):

@@ -333,6 +333,9 @@ class REMLServer:
     ``launch_ms`` ({width: ms}, e.g. from ``GenoBlockStreamer.autotune``)
     lets the batcher cut the pending right-hand sides into the launches of
     least measured total time instead of filling ``max_batch_cols`` first.
+    Off by default: with 8 single-GRM fits at n = 100k, m = 1M it measured
+    10.8k against 11.3k fits/hr (76 launches of 38 columns per step against
+    61 of 48: rounds that are not complete yet get cut narrow).
 
     ``precond_rank`` > 0 gives every fit's PCG solves a projected-core
     preconditioner of that rank (reml_model.py:863-960, single GRM): a
