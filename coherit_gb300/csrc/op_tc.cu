@@ -943,7 +943,7 @@ static int fill_epi(coherit_geno* h, const OpDesc& d, int kp, int nsplit, EpiPar
 struct TcLaunchCfg {
   bool wide;   // StageCfg<4, 2> instead of StageCfg<2, 3>
   int sb;      // blocks per stage of that configuration
-  int cluster; // CTAs per cluster sharing each B tile (1, 2 or 4)
+  int cluster; // CTAs per cluster sharing each B tile (1 or 2)
   int tiles;   // row tiles per CTA (1, or 2 with two MMA-issuing threads)
   int RG;      // genotype ring stages
   int RB, RA;
