@@ -387,12 +387,21 @@ def operator_roofline(st, k, hbm_peak, tensor_peak, reps=10, precision=None):
         kk = 32 if form == "fp8x5" else 16
         instr = 2.0 * info["n_pad"] * info["m_pad"] / (128.0 * kk) * launches
         sm_hz, sms = _sm_clock_hz(), torch.cuda.get_device_properties(st.dev).multi_processor_count
+        n_instr = ns * min(kp, max_cols)
+        # Dense work the instructions execute (every split term, padding
+        # columns included) against the nominal dense rate of their operand
+        # type: 2.25 PFLOP/s for 16-bit operands, 4.5 for E4M3.
+        executed = instr * 2.0 * 128 * n_instr * kk / (ms * 1e-3) / 1e12
+        nominal = 4500.0 if form == "fp8x5" else 2250.0
         roof["mma_issue"] = {
             "instructions_per_application": int(instr),
             "form": form, "k_per_instruction": kk,
-            "n_per_instruction": ns * min(kp, max_cols),
+            "n_per_instruction": n_instr,
             "cycles_per_instruction_per_sm": round(ms * 1e-3 * sm_hz * sms / instr, 1),
-            "sm_clock_mhz_assumed": sm_hz / 1e6}
+            "sm_clock_mhz_assumed": sm_hz / 1e6,
+            "executed_tflops": round(executed, 1),
+            "nominal_dense_tflops": nominal,
+            "executed_frac_of_nominal": round(executed / nominal, 3)}
     return roof
 
 
