@@ -36,6 +36,7 @@ host memory and the variance components returned to the host.
 from __future__ import annotations
 
 import argparse
+import collections
 import json
 import math
 import os
@@ -616,6 +617,7 @@ def run_ours(args, wl):
     # Device time of the batched operator launches inside the timed steps
     # (their own CUDA events): the rest of the step is solver work and idle.
     op_dev_ms = srv.batcher.device_ms(b0)
+    timed_widths = list(srv.batcher.launch_widths[-op_launches:]) if op_launches else []
     # Operator applications the timed fits requested (a launch serves one
     # application of each request it carries).
     op_apps = float(sum(srv.batcher.requests_per_launch[b0:b0 + op_launches]))
@@ -636,7 +638,14 @@ def run_ours(args, wl):
     if rank == 0:
         n_fits = args.steps * R
         fit_apps, fit_cols = op_apps / n_fits, op_cols / n_fits
-        k_typ = max(16, int(round(op_cols / max(op_launches, 1))))
+        # The roofline is taken at the most frequent launch width (columns
+        # rounded up to 16, as the launch pads them; the wider on a tie):
+        # AUTO switches from E4M3 to bf16x3 tiles above 48 columns, so the
+        # mean width would measure a form most launches do not use.
+        widths = collections.Counter(-(-w // 16) * 16 for w in timed_widths)
+        k_typ = (max(widths.items(), key=lambda kv: (kv[1], kv[0]))[0] if widths
+                 else max(16, int(round(op_cols / max(op_launches, 1)))))
+        launch_width_counts = {int(w): int(c) for w, c in sorted(widths.items())}
         roof = operator_roofline(st, k_typ, hbm_peak, tensor_peak, precision=args.precision)
         roof["peak_source"] = peak_src
         single = None
@@ -732,6 +741,7 @@ def run_ours(args, wl):
             "operator_device_ms_per_step": round(op_dev_ms / args.steps, 1),
             "operator_share_of_step": round(op_dev_ms / (dev_s * 1e3), 3),
             "rhs_columns_per_launch": round(op_cols / max(op_launches, 1), 1),
+            "launch_width_counts": launch_width_counts,
             "operator_apps_per_fit": round(fit_apps, 2),
             "rhs_columns_per_fit": round(fit_cols, 1),
             "e2e": {"value": round(e2e_val, 3), "unit": "fits/hr",

@@ -140,6 +140,7 @@ class _Batcher:
         # _events_base + index): device time of the operator.
         self.launch_events: list[tuple] = []
         self._events_base = 0
+        self.launch_widths: list[int] = []  # columns of the latest launches (bounded)
         self._busy_cap_s = 0.25  # longest wait for stragglers while the device is busy
         self.thread = threading.Thread(target=self._loop, name="coherit-batcher", daemon=True)
         self.thread.start()
@@ -290,9 +291,11 @@ class _Batcher:
         ev.record()
         self.last_launch = ev
         self.launch_events.append((ev0, ev))
+        self.launch_widths.append(K)
         if len(self.launch_events) > 8192:  # bounded: keep the latest half
             drop = len(self.launch_events) // 2
             del self.launch_events[:drop]
+            del self.launch_widths[:drop]
             self._events_base += drop
         st.op_stats["apps"] += 1
         st.op_stats["cols"] += K
