@@ -319,3 +319,39 @@ def test_unit_variance_components_report_no_atoms(monkeypatch):
     res = InfinitesimalREMLFitter(cfg, [_Operator()]).fit_infinitesimal(np.ones(8))
     assert res.genetic_trace_atoms is None and res.residual_trace_atoms is None
     assert res.heritability == pytest.approx(0.75)
+
+
+def test_reference_weights_of_the_preconditioner_kernel():
+    """theta_ref (reml_model.py:808-832): the first G variance components
+    clamped at zero and normalised to sum 1; uniform 1/G without them or
+    when they sum to zero; too few components is an error."""
+    import numpy as np
+
+    th = reml_model._theta_ref_from_var_components
+    np.testing.assert_allclose(th(3), [1 / 3] * 3)
+    np.testing.assert_allclose(th(2, [0.2, 0.6, 0.5]), [0.25, 0.75], rtol=1e-6)
+    np.testing.assert_allclose(th(2, [-0.1, 0.4, 0.5]), [0.0, 1.0])
+    np.testing.assert_allclose(th(2, [0.0, 0.0, 1.0]), [0.5, 0.5])
+    with pytest.raises(ValueError, match="length mismatch"):
+        th(3, [0.1, 0.2])
+
+
+def test_slq_workspace_option_reaches_fit_reml(monkeypatch):
+    """FitConfig.slq_workspace_bytes replaces the reference's budget policy
+    (256 MiB without gpu_budget_bytes) when set."""
+    import numpy as np
+
+    seen = []
+
+    def fit(**kwargs):
+        seen.append(kwargs["slq_workspace_bytes"])
+        diag = {"genetic_trace_atoms": np.ones(1), "residual_trace_atoms": np.ones(1),
+                "loglik": 0.0, "ai": np.eye(2), "grad": np.zeros(2)}
+        return np.array([0.3, 0.7]), [], diag
+
+    monkeypatch.setattr(reml_model, "fit_reml", fit)
+    InfinitesimalREMLFitter(FitConfig(precond_rank=0), [_Operator()]).fit_infinitesimal(
+        np.ones(8))
+    InfinitesimalREMLFitter(FitConfig(precond_rank=0, slq_workspace_bytes=3 << 30),
+                            [_Operator()]).fit_infinitesimal(np.ones(8))
+    assert seen == [256 * 1024 ** 2, 3 << 30]
