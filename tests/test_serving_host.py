@@ -234,3 +234,36 @@ def test_batcher_cuts_pending_columns_by_measured_launch_times():
     assert b._first_width(50) == 64          # one 64-column launch beats 48 + 16
     assert b._first_width(96) == 48          # 48 + 48 beats 80 + 16
     assert b._first_width(160) == 80
+
+
+def test_projected_core_of_a_request_on_host_tensors():
+    """REMLServer._projected_core (reml_model.py:863-960 for one GRM):
+    Nystrom basis of the request's kernel, core diag(e) - atom I, identity
+    diagonal with the request's atom; full-cohort requests share one."""
+    srv = serving.REMLServer.__new__(serving.REMLServer)
+    srv.st = types.SimpleNamespace(dev=torch.device("cpu"))
+    srv.precond_rank = 4
+    srv._full_precond = None
+    srv._full_precond_lock = threading.Lock()
+    g = torch.Generator().manual_seed(1)
+    A = torch.randn(60, 8, generator=g)
+    K = (A @ A.T / 8).float()
+    srv._full_K = lambda V: K @ V
+    req = types.SimpleNamespace(n_sub=60, atom=1.25, fit_kwargs={"seed": 3}, mask=None)
+    conf = srv._precond_for(req, None)
+    assert conf is srv._precond_for(req, None)            # shared by full-cohort requests
+    U = conf.U.double()
+    assert conf.total_rank == 4 and conf.n_grm == 1 and conf.diag_mode == "scalar_identity"
+    torch.testing.assert_close(U.T @ U, torch.eye(4, dtype=torch.float64), atol=1e-4, rtol=0)
+    core = conf.core_atoms[0].double()
+    ev = torch.diagonal(core) + 1.25
+    torch.testing.assert_close(core - torch.diag(torch.diagonal(core)),
+                               torch.zeros(4, 4, dtype=torch.float64))
+    # The basis spans the leading eigenvectors: U^T K U = diag(e).
+    torch.testing.assert_close((U.T @ K.double() @ U).diagonal(), ev, atol=1e-3, rtol=1e-3)
+    assert float(conf.diag_atoms[0]) == 1.25
+    sub = types.SimpleNamespace(n_sub=60, atom=0.5, fit_kwargs={}, mask=np.ones(60, bool))
+    other = srv._precond_for(sub, lambda V: K @ V)       # a subset request builds its own
+    assert other is not conf
+    srv.precond_rank = 0
+    assert srv._precond_for(req, None) is None
