@@ -164,16 +164,26 @@ def build_projected_core_runtime(precond_conf, theta_g, diag_H, eps: float = 0.0
     rt = ProjectedCoreRuntime(U=U, total_rank=r, d=d, d_inv=1.0 / d, chol=chol,
                               eigvals=eigvals, eigvecs=eigvecs)
     if U.is_cuda and U.dtype == torch.float32 and U.is_contiguous():
-        # Cores of the fused apply, formed in FP64 from the factorisations.
-        dd = float(d)
-        eye64 = torch.eye(r, dtype=torch.float64, device=U.device)
-        rt.a_inv = 1.0 / dd
-        rt.core_inv = (torch.cholesky_inverse(chol.double()) - eye64 / dd).float().contiguous()
-        if need_invsqrt:
-            q = eigvecs.double()
-            rt.a_invsqrt = dd ** -0.5
-            rt.core_invsqrt = ((q / torch.sqrt(eigvals.double())[None, :]) @ q.T -
-                               eye64 * dd ** -0.5).float().contiguous()
+        fused_cores(rt)
+    return rt
+
+
+def fused_cores(rt: ProjectedCoreRuntime) -> ProjectedCoreRuntime:
+    """Fill the r x r cores of the fused apply out = a V + U (G (U^T V)),
+    formed in FP64 from the factorisations:
+        M^{-1}:    G = (dI + C)^{-1} - d^{-1} I,             a = 1/d
+        M^{-1/2}:  G = Q diag(e^{-1/2}) Q^T - d^{-1/2} I,    a = d^{-1/2}
+    (the latter only with the eigendecomposition)."""
+    dd = float(rt.d)
+    r = rt.total_rank
+    eye64 = torch.eye(r, dtype=torch.float64, device=rt.chol.device)
+    rt.a_inv = 1.0 / dd
+    rt.core_inv = (torch.cholesky_inverse(rt.chol.double()) - eye64 / dd).float().contiguous()
+    if rt.eigvals is not None and rt.eigvecs is not None:
+        q = rt.eigvecs.double()
+        rt.a_invsqrt = dd ** -0.5
+        rt.core_invsqrt = ((q / torch.sqrt(rt.eigvals.double())[None, :]) @ q.T -
+                           eye64 * dd ** -0.5).float().contiguous()
     return rt
 
 

@@ -825,3 +825,33 @@ def test_preconditioner_refresh_follows_accepted_non_final_steps(monkeypatch):
     assert refreshes and ("conf", len(refreshes)) in seen_conf
     with pytest.raises(RuntimeError, match="returned no configuration"):
         reml.fit_reml(*args, **kw, precond_refresh_fn=lambda theta: None)
+
+
+def test_fused_cores_reproduce_the_explicit_applies():
+    """The r x r cores the GPU's fused apply uses (a V + U (G (U^T V)))
+    reproduce M^{-1} V and M^{-1/2} V of the explicit formulas
+    (precond.py:42-84), computed here on host tensors."""
+    import torch
+
+    from coherit_gb300 import precond as pc
+
+    g = torch.Generator().manual_seed(7)
+    n, r, k = 300, 12, 5
+    U, _ = torch.linalg.qr(torch.randn(n, r, generator=g, dtype=torch.float64))
+    A = torch.randn(r, r, generator=g, dtype=torch.float64)
+    C = (A @ A.T / r).float()
+    conf = pc.ProjectedCorePrecondConf(
+        U=U.float(), core_atoms=C[None], total_rank=r, n_grm=1, diag_mode="scalar_identity",
+        diag_atoms=torch.zeros(1), residual_diag_atoms=torch.ones(1), identity=torch.eye(r))
+    rt = pc.build_projected_core_runtime(conf, torch.ones(1), torch.tensor(0.8),
+                                         need_invsqrt=True)
+    assert rt.core_inv is None                       # host tensors: explicit applies
+    pc.fused_cores(rt)
+    V = torch.randn(n, k, generator=g)
+    Uf = rt.U
+    fused = rt.a_inv * V + Uf @ (rt.core_inv @ (Uf.T @ V))
+    explicit = pc.make_projected_core_precond_from_runtime(rt)(V)
+    torch.testing.assert_close(fused, explicit, rtol=1e-4, atol=1e-5)
+    fused_sq = rt.a_invsqrt * V + Uf @ (rt.core_invsqrt @ (Uf.T @ V))
+    torch.testing.assert_close(fused_sq, pc.projected_core_apply_invsqrt(rt, V),
+                               rtol=1e-4, atol=1e-5)
