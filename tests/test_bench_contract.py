@@ -45,3 +45,20 @@ def test_gpu_arm_fails_without_a_gpu():
     out = _run("--steps", "1", "--warmup", "1")
     assert out.returncode != 0
     assert out.stdout.strip() == ""
+
+
+def test_bench_helpers_pick_the_form_and_the_peak():
+    """AUTO's per-width form, split-term counts and the peak the roofline
+    divides by (sustained bf16 for the serving step's operator)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    assert bench._resolve("auto", 48) == "fp8x5" and bench._resolve("auto", 49) == "bf16x3"
+    assert bench._resolve("fp16x2", 16) == "fp16x2"
+    assert [bench._nsplit(p) for p in ("bf16x3", "fp8x5", "fp16x2", "fp32")] == [3, 5, 2, 0]
+    hbm, burst, src_b = bench._peaks()
+    _, sust, src_s = bench._peaks(sustained=True)
+    assert hbm > 0 and burst >= sust > 0
+    assert "sustained" in src_s or src_s == "fallback"
